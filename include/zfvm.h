@@ -1,0 +1,183 @@
+/*
+ * zfvm.h -- C ABI of the GB300 rate-of-change / SSP-RK solver.
+ *
+ * Every entry point returns an int status (ZFVM_OK = 0).  The reference
+ * reports failures through LOG_ERR (log + abort); here a non-zero status is
+ * returned instead and zfvm_last_error() gives the message of the calling
+ * thread's last failure.  A mesh or solver handle is externally synchronised:
+ * one host thread at a time, like the reference's non-re-entrant objects
+ * (LocalReconstruction keeps mutable caches).  Distinct handles may be driven
+ * from distinct threads; each solver owns one CUDA stream.
+ *
+ * Layouts at this boundary are the reference's: cell-major AoS conserved
+ * variables (rho, m1, m2, m3, E) as in GridVariables
+ * (model/grid_variables_decl.hpp:17-36); vertex coordinates n x 3 and
+ * cell->vertex indices n x (n_dims + 1) as in the .msh.h5 schema
+ * (grid/grid.cpp:889-901).
+ */
+#ifndef ZFVM_H
+#define ZFVM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum zfvm_status {
+  ZFVM_OK = 0,
+  ZFVM_EINVAL = 1,        /* bad argument or unsupported configuration      */
+  ZFVM_ENOMEM = 2,        /* host or device allocation failed               */
+  ZFVM_ENONPHYSICAL = 3,  /* rho <= 0, E <= 0 or a non-finite state         */
+  ZFVM_ENEWTON = 4,       /* local equilibrium solve did not converge       */
+  ZFVM_ETIMEDOUT = 5,     /* a host wait passed its deadline                */
+  ZFVM_ECUDA = 6,         /* CUDA runtime error                             */
+  ZFVM_ESETUP = 7         /* mesh / stencil set-up failed                   */
+};
+
+#define ZFVM_MAX_STENCILS 5
+#define ZFVM_MAX_L2G 40
+#define ZFVM_MAX_STENCIL_SIZE 24
+
+typedef struct zfvm_rawmesh zfvm_rawmesh;
+typedef struct zfvm_mesh zfvm_mesh;
+typedef struct zfvm_solver zfvm_solver;
+
+/* ---- meshes ---------------------------------------------------------------
+ * Synthetic generators (the reference loads gmsh meshes, grid/grid.cpp:907-922).
+ * kind 0: periodic unit square, iparams = {n, halo}, dparams = {jitter}
+ * kind 1: disk, iparams = {n_rings}, dparams = {radius, jitter}
+ * kind 2: unit cube of tetrahedra, iparams = {n}, dparams = {jitter}
+ * The mesh is renumbered along a Hilbert curve when `renumber` is non-zero
+ * (src/renumber_grid.cpp:46-135). */
+int zfvm_rawmesh_generate(int32_t kind, const int64_t *iparams, const double *dparams,
+                          uint64_t seed, int32_t renumber, zfvm_rawmesh **out);
+int zfvm_rawmesh_sizes(const zfvm_rawmesh *m, int32_t *n_dims, int64_t *n_vertices,
+                       int64_t *n_cells, int32_t *has_ghosts);
+/* Copies vertices (n_vertices x 3), vertex_indices (n_cells x (n_dims+1)),
+ * ghost mask (n_cells, may be NULL) and periodic sources (n_cells, may be NULL). */
+int zfvm_rawmesh_copy(const zfvm_rawmesh *m, double *vertices, int64_t *vertex_indices,
+                      uint8_t *ghost, int64_t *source);
+int zfvm_rawmesh_destroy(zfvm_rawmesh *m);
+
+typedef struct {
+  int32_t n_dims;                 /* 2 (triangles) or 3 (tetrahedra)                 */
+  int64_t n_vertices;
+  int64_t n_cells;
+  const double *vertices;         /* n_vertices x 3                                   */
+  const int64_t *vertex_indices;  /* n_cells x (n_dims + 1)                           */
+  const uint8_t *ghost;           /* optional ghost-cell mask (grid.cpp:1122-1137)    */
+  const int64_t *source;          /* optional periodic source of every ghost cell     */
+  int32_t quad_edge;              /* quadrature.edge   (numerical_experiment.cpp:193) */
+  int32_t quad_volume;            /* quadrature.volume                                */
+  int32_t quad_moments;           /* quadrature.moments                               */
+  int32_t n_stencils;             /* reconstruction.orders / biases / overfit_factors */
+  int32_t orders[ZFVM_MAX_STENCILS];
+  int32_t biased[ZFVM_MAX_STENCILS];
+  double overfit[ZFVM_MAX_STENCILS];
+} zfvm_mesh_desc;
+
+/* Geometry, stencil families and least-squares pseudo-inverses
+ * (Grid::Grid grid.cpp:651-723, compute_stencil_families stencil_family.cpp:99-118,
+ * LSQSolver lsq_solver.cpp:104-112).  Host only; device arrays are made by
+ * zfvm_solver_create. */
+int zfvm_mesh_create(const zfvm_mesh_desc *desc, zfvm_mesh **out);
+int zfvm_mesh_destroy(zfvm_mesh *m);
+
+typedef struct {
+  int32_t n_dims;
+  int64_t n_cells, n_interior_cells, n_edges, n_interior_edges;
+  int32_t n_cell_qp, n_face_qp, n_moments;
+  double min_inradius, max_circum_radius, total_volume;
+} zfvm_mesh_info;
+int zfvm_mesh_get_info(const zfvm_mesh *m, zfvm_mesh_info *info);
+
+/* Export the stencil families: n_stencils[n], k_high[n], n_l2g[n],
+ * l2g[n * ZFVM_MAX_L2G], order/size/bias[n * ZFVM_MAX_STENCILS],
+ * local[n * ZFVM_MAX_STENCILS * ZFVM_MAX_STENCIL_SIZE]. */
+int zfvm_mesh_get_stencils(const zfvm_mesh *m, int8_t *n_stencils, int8_t *k_high, int8_t *n_l2g,
+                           int32_t *l2g, int8_t *order, int8_t *size, int8_t *bias, int8_t *local);
+/* Export the pseudo-inverse of stencil k of cell i, (cols x rows) row-major. */
+int zfvm_mesh_get_pinv(const zfvm_mesh *m, int64_t cell, int32_t k, double *P, int32_t *rows,
+                       int32_t *cols);
+/* Geometry export: volumes[n], inradii[n], centers[n x 3], flags[n]. */
+int zfvm_mesh_get_geometry(const zfvm_mesh *m, double *volumes, double *inradii, double *centers,
+                           uint8_t *flags);
+
+/* ---- initial data (cell averages with the volume quadrature) ---------------
+ * kind 0: isentropic vortex (2D) / vortex tube along z (3D);
+ *         dparams = {gamma, beta, x0, y0, length, rho_inf, u_inf, v_inf, p_inf}
+ * kind 1: polytrope rho = rho_c - k r^2 / 4 ... for gamma = 2, K and phi = k r^2/2,
+ *         plus a Gaussian pressure bump;
+ *         dparams = {gamma, K, rho_c, k_phi, amplitude, width, x0, y0}
+ * Output: n_cells x 5 AoS. */
+int zfvm_initial_conditions(const zfvm_mesh *m, int32_t kind, const double *dparams,
+                            double *cvars);
+
+/* ---- scheme ---------------------------------------------------------------- */
+enum zfvm_flux { ZFVM_FLUX_HLLC = 0, ZFVM_FLUX_RUSANOV = 1 };
+enum zfvm_equilibrium { ZFVM_EQ_NONE = 0, ZFVM_EQ_ISENTROPIC = 1 };
+enum zfvm_gravity { ZFVM_GRAVITY_NONE = 0, ZFVM_GRAVITY_CONSTANT_RADIAL = 1, ZFVM_GRAVITY_HARMONIC_RADIAL = 2 };
+enum zfvm_flux_bc { ZFVM_FLUX_BC_NONE = 0, ZFVM_FLUX_BC_CONSTANT = 1, ZFVM_FLUX_BC_ISENTROPIC = 2 };
+enum zfvm_boundary { ZFVM_BC_NONE = 0, ZFVM_BC_PERIODIC = 1 };
+enum zfvm_precision { ZFVM_FP64 = 0, ZFVM_MIXED = 1 };
+
+typedef struct {
+  int32_t flux;                 /* zfvm_flux                                        */
+  double gamma;                 /* euler.eos.gamma                                  */
+  double specific_gas_constant; /* euler.eos.specific-gas-constant                  */
+  double linear_weights[ZFVM_MAX_STENCILS];
+  double epsilon;               /* reconstruction.smoothness_indicator.epsilon      */
+  double exponent;              /* reconstruction.smoothness_indicator.exponent     */
+  int32_t rk_stages;            /* 1 forward Euler, 2 SSP2, 3 SSP3                  */
+  double cfl_number;            /* ode.cfl_number                                   */
+  int32_t equilibrium;          /* well-balancing.mode: none / isentropic           */
+  int32_t gravity;              /* zfvm_gravity                                     */
+  double gravity_strength;      /* g for constant, k for phi = k r^2 / 2            */
+  int32_t flux_bc;              /* flux-bc.mode                                     */
+  int32_t boundary;             /* ghost-cell boundary condition                    */
+  int32_t precision;            /* zfvm_precision                                   */
+  int32_t steps_per_recompute;  /* reconstruction.steps_per_recompute (must be 1)   */
+  double recompute_threshold;
+} zfvm_scheme_desc;
+
+int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *scheme, zfvm_solver **out);
+int zfvm_solver_destroy(zfvm_solver *s);
+
+/* Upload / download the state (n_cells x 5 AoS host doubles) and the time. */
+int zfvm_set_state(zfvm_solver *s, const double *cvars, double t);
+int zfvm_get_state(zfvm_solver *s, double *cvars, double *t);
+
+/* One evaluation of the summed rate of change of the current state
+ * (SumRatesOfChange::compute, ode/rate_of_change.cpp:21-27); output n_cells x 5.
+ * Ghost-cell rows are zero. */
+int zfvm_rate_of_change(zfvm_solver *s, double *tendency);
+
+/* CFL time step of the current state (LocalCFL, local_cfl_condition_impl.hpp:24-40). */
+int zfvm_cfl_dt(zfvm_solver *s, double *dt);
+
+/* One Runge-Kutta step of size dt (RungeKutta::compute_step, runge_kutta.cpp:146-171). */
+int zfvm_step(zfvm_solver *s, double dt);
+
+/* TimeLoop (fvm_loops/time_loop.cpp:36-81) without IO: steps with the CFL time
+ * step until `n_steps` steps are done (if > 0) or t reaches t_end (if > 0),
+ * dt = min(dt_cfl, t_end - t).  The clock stays on the device; the whole loop is
+ * replayed from a CUDA graph in chunks of `graph_steps`. */
+int zfvm_advance(zfvm_solver *s, int64_t n_steps, double t_end, double *t_out, int64_t *steps_out);
+
+/* Device-timed loop for benchmarks: runs `n_steps` fixed-count steps and returns
+ * the milliseconds measured with CUDA events on the solver's stream. */
+int zfvm_advance_timed(zfvm_solver *s, int64_t n_steps, float *ms);
+
+/* Number of kernel launches one step issues. */
+int zfvm_launches_per_step(const zfvm_solver *s, int32_t *launches);
+
+/* Bytes of device memory the solver holds. */
+int zfvm_device_bytes(const zfvm_solver *s, int64_t *bytes);
+
+const char *zfvm_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,15 @@
+"""Relative L1 / Linf differences of conserved variables (per variable)."""
+import numpy as np
+
+
+def rel_errors(a: np.ndarray, ref: np.ndarray, mask=None, cols=(0, 1, 2, 4)):
+    if mask is not None:
+        a, ref = a[mask], ref[mask]
+    l1, linf = [], []
+    for v in cols:
+        d = np.abs(a[:, v] - ref[:, v])
+        s1 = np.abs(ref[:, v]).sum()
+        sinf = np.abs(ref[:, v]).max()
+        l1.append(d.sum() / s1 if s1 > 0 else d.sum())
+        linf.append(d.max() / sinf if sinf > 0 else d.max())
+    return max(l1), max(linf)

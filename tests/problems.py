@@ -1,0 +1,49 @@
+"""Problem set-ups shared by tests, smoke() and the benchmark.
+
+Each returns (raw_mesh, mesh, scheme, initial_state).  The configurations are
+the workloads of the benchmark suite (C1 periodic vortex, C2 well-balanced
+polytrope, C3 tetrahedral vortex tube), optionally at smaller sizes.
+"""
+from __future__ import annotations
+
+import zisafvm_gb300 as z
+
+
+def vortex_2d(n: int = 160, halo: int = 3, flux: int = z.FLUX_RUSANOV, seed: int = 1):
+    """C1: periodic unit square, n x n squares of two triangles, jitter 0.2 h,
+    isentropic vortex (beta 5, core length 0.1) on rho = 1, u = (1, 1), p = 1,
+    CWENO-AO order 3, SSP3, CFL 0.45."""
+    raw = z.RawMesh.generate("periodic_square", n=n, halo=halo, jitter=0.2, seed=seed)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2), quad=(3, 3, 2))
+    scheme = z.Scheme(flux=flux, gamma=1.4, linear_weights=[100.0, 1.0, 1.0, 1.0], epsilon=1e-6, exponent=4.0,
+                      rk_stages=3, cfl_number=0.45, boundary=z.BC_PERIODIC)
+    u0 = mesh.initial_conditions("vortex", gamma=1.4, beta=5.0, x0=0.5, y0=0.5, length=0.1)
+    return raw, mesh, scheme, u0
+
+
+def polytrope_2d(n_rings: int = 178, amplitude: float = 1e-4, seed: int = 7, precision: int = z.FP64):
+    """C2: disk of radius 1 (~2 pi n_rings^2 triangles), gamma = 2, K = 1,
+    phi = r^2 / 2, polytrope rho = 1 - r^2 / 4 plus a Gaussian pressure bump of
+    width 0.05 at r = 0.3; CWENO-AO order 3, HLLC, SSP3, CFL 0.45, isentropic
+    well-balancing and equilibrium flux boundary."""
+    raw = z.RawMesh.generate("disk", n=n_rings, radius=1.0, jitter=0.2, seed=seed)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2), quad=(3, 3, 2))
+    scheme = z.Scheme(flux=z.FLUX_HLLC, gamma=2.0, linear_weights=[100.0, 1.0, 1.0, 1.0], epsilon=1e-6,
+                      exponent=4.0, rk_stages=3, cfl_number=0.45, equilibrium=z.EQ_ISENTROPIC,
+                      gravity=z.GRAVITY_HARMONIC_RADIAL, gravity_strength=1.0, flux_bc=z.FLUX_BC_ISENTROPIC,
+                      precision=precision)
+    u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amplitude,
+                                 width=0.05, x0=0.3, y0=0.0)
+    return raw, mesh, scheme, u0
+
+
+def vortex_tube_3d(n: int = 70, order: int = 3, seed: int = 1):
+    """C3: unit cube of n^3 x 6 jittered tetrahedra, vortex tube along z,
+    HLLC, SSP3, CFL 0.3, constant flux boundary."""
+    raw = z.RawMesh.generate("cube", n=n, jitter=0.1, seed=seed)
+    quad = (2, 2, 2) if order == 3 else (2, 2, 1)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(order, 3), quad=quad)
+    scheme = z.Scheme(flux=z.FLUX_HLLC, gamma=1.4, linear_weights=[100.0, 1.0, 1.0, 1.0, 1.0], epsilon=1e-6,
+                      exponent=4.0, rk_stages=3, cfl_number=0.3, flux_bc=z.FLUX_BC_CONSTANT)
+    u0 = mesh.initial_conditions("vortex", gamma=1.4, beta=5.0, x0=0.5, y0=0.5, length=0.1, v_inf=1.0, u_inf=1.0)
+    return raw, mesh, scheme, u0

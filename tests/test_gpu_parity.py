@@ -1,0 +1,163 @@
+"""GPU solver vs the CPU oracle, through the C ABI.
+
+FP64 parity bar (the benchmark spec's tolerance): relative L1 and Linf of the
+conserved variables within 1e-12 after N steps; single right-hand-side
+evaluations and CFL steps within 1e-13.
+"""
+import numpy as np
+import pytest
+
+from metrics import rel_errors
+from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+
+pytestmark = pytest.mark.gpu
+
+TOL_RHS = 1e-13
+TOL_RUN = 1e-12
+
+
+def _oracle(olib, raw, mesh, scheme, threads=0):
+    import os
+    o = olib.Oracle(raw, mesh.stencils(), scheme.oracle_vector(), quad=mesh.quad,
+                    threads=threads or os.cpu_count())
+    return o
+
+
+@pytest.mark.parametrize("flux", [0, 1])
+def test_rate_of_change_2d(zlib, olib, flux):
+    z = zlib
+    raw, mesh, scheme, u0 = vortex_2d(n=24, halo=3, flux=flux)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t_gpu = s.rate_of_change()
+    t_ref = _oracle(olib, raw, mesh, scheme).rate_of_change(u0)
+    inner = raw.ghost == 0
+    scale = np.abs(t_ref[inner]).max(axis=0)
+    for v in (0, 1, 2, 4):
+        err = np.abs(t_gpu[inner, v] - t_ref[inner, v]).max() / scale[v]
+        assert err < TOL_RHS, (v, err)
+
+
+def test_cfl_dt(zlib, olib):
+    z = zlib
+    raw, mesh, scheme, u0 = vortex_2d(n=24, halo=3)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    dt_ref = _oracle(olib, raw, mesh, scheme).cfl_dt(u0)
+    assert abs(s.cfl_dt() - dt_ref) <= 1e-15 * dt_ref
+
+
+@pytest.mark.parametrize("flux", [0, 1])
+def test_steps_2d(zlib, olib, flux):
+    z = zlib
+    raw, mesh, scheme, u0 = vortex_2d(n=24, halo=3, flux=flux)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t_gpu, n_gpu = s.advance(n_steps=10)
+    u_gpu, _ = s.get_state()
+    u_ref, t_ref, n_ref = _oracle(olib, raw, mesh, scheme).run(u0, n_steps=10)
+    assert n_gpu == n_ref == 10
+    assert abs(t_gpu - t_ref) <= 1e-13 * t_ref
+    l1, linf = rel_errors(u_gpu, u_ref, raw.ghost == 0)
+    assert l1 < TOL_RUN and linf < TOL_RUN, (l1, linf)
+
+
+def test_fixed_dt_step(zlib, olib):
+    z = zlib
+    raw, mesh, scheme, u0 = vortex_2d(n=16, halo=3)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    s.step(1e-3)
+    u_gpu, t = s.get_state()
+    u_ref = _oracle(olib, raw, mesh, scheme).step(u0, 1e-3)
+    assert abs(t - 1e-3) < 1e-18
+    l1, linf = rel_errors(u_gpu, u_ref, raw.ghost == 0)
+    assert linf < TOL_RHS
+
+
+def test_c1_full_100_steps(zlib, olib):
+    """Configuration C1 at full size: 51,200 cells, 100 steps, Rusanov."""
+    z = zlib
+    raw, mesh, scheme, u0 = vortex_2d(n=160, halo=3)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t_gpu, n_gpu = s.advance(n_steps=100)
+    u_gpu, _ = s.get_state()
+    u_ref, t_ref, n_ref = _oracle(olib, raw, mesh, scheme).run(u0, n_steps=100)
+    assert n_gpu == n_ref == 100
+    l1, linf = rel_errors(u_gpu, u_ref, raw.ghost == 0)
+    print(f"C1 100 steps: rel L1 {l1:.3e}  rel Linf {linf:.3e}  t {t_gpu:.6e}")
+    assert l1 < TOL_RUN and linf < TOL_RUN
+
+
+def test_polytrope_rhs(zlib, olib):
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=20, amplitude=1e-3)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t_gpu = s.rate_of_change()
+    t_ref = _oracle(olib, raw, mesh, scheme).rate_of_change(u0)
+    scale = np.abs(t_ref).max(axis=0)
+    for v in (0, 1, 2, 4):
+        err = np.abs(t_gpu[:, v] - t_ref[:, v]).max() / scale[v]
+        assert err < 1e-9, (v, err)
+
+
+def test_polytrope_well_balanced(zlib):
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=30, amplitude=0.0)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t = s.rate_of_change()
+    assert np.abs(t).max() < 1e-10
+    s.advance(n_steps=20)
+    u, _ = s.get_state()
+    drift = np.abs(u - u0).max(axis=0)[[0, 4]] / np.abs(u0).max(axis=0)[[0, 4]]
+    assert drift.max() < 1e-10, drift
+
+
+def test_polytrope_steps(zlib, olib):
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=24, amplitude=1e-2)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    s.advance(n_steps=5)
+    u_gpu, t_gpu = s.get_state()
+    u_ref, t_ref, _ = _oracle(olib, raw, mesh, scheme).run(u0, n_steps=5)
+    # compare the deviation from the initial state: the perturbation is the signal
+    d_gpu, d_ref = u_gpu - u0, u_ref - u0
+    err = np.abs(d_gpu - d_ref).max() / np.abs(d_ref).max()
+    assert err < 1e-9, err
+    assert abs(t_gpu - t_ref) < 1e-12 * t_ref
+
+
+@pytest.mark.parametrize("order", [2, 3])
+def test_tets_rhs(zlib, olib, order):
+    z = zlib
+    raw, mesh, scheme, u0 = vortex_tube_3d(n=6, order=order)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t_gpu = s.rate_of_change()
+    t_ref = _oracle(olib, raw, mesh, scheme).rate_of_change(u0)
+    scale = np.abs(t_ref).max(axis=0)
+    for v in range(5):
+        if scale[v] == 0:
+            continue
+        err = np.abs(t_gpu[:, v] - t_ref[:, v]).max() / scale[v]
+        assert err < TOL_RHS * 10, (v, err)
+
+
+def test_error_status_nonphysical(zlib):
+    """A negative density is reported as ENONPHYSICAL, not a crash."""
+    z = zlib
+    raw, mesh, scheme, u0 = vortex_2d(n=8, halo=3)
+    bad = u0.copy()
+    bad[int(np.where(raw.ghost == 0)[0][5]), 0] = -1.0
+    s = z.Solver(mesh, scheme)
+    s.set_state(bad)
+    with pytest.raises(z.ZfvmError) as e:
+        s.rate_of_change()
+    assert e.value.code == 3
+    # the context stays usable
+    s.set_state(u0)
+    s.rate_of_change()

@@ -1,0 +1,91 @@
+"""Known-answer tests of the oracle, restated from the reference's own unit tests.
+
+Each case cites the reference test it pins (paths inside the ZisaFVM repository).
+"""
+import numpy as np
+import pytest
+
+
+def test_hllc_consistency(olib):
+    # test/zisa/unit_test/flux/hllc.cpp:10-26: F_HLLC(u, u) = F(u), gamma = 1.6, tol 1e-12
+    u = [1.0, -0.2, 0.3, 0.8, 12.0]
+    nf = olib.flux(0, 1.6, u, u)
+    pf = olib.euler_flux(1.6, u)
+    assert np.allclose(nf, pf, rtol=1e-12, atol=1e-12)
+
+
+def test_rusanov_consistency(olib):
+    # the Rusanov flux is consistent in the same sense
+    u = [1.3, 0.4, -0.1, 0.0, 5.0]
+    assert np.allclose(olib.flux(1, 1.4, u, u), olib.euler_flux(1.4, u), rtol=1e-14, atol=1e-14)
+
+
+def test_hllc_supersonic_upwind(olib):
+    # s_L >= 0: the HLLC flux is the left physical flux (hllc.hpp:160-176)
+    uL = [1.0, 5.0, 0.0, 0.0, 20.0]
+    uR = [0.8, 4.0, 0.0, 0.0, 15.0]
+    assert np.allclose(olib.flux(0, 1.4, uL, uR), olib.euler_flux(1.4, uL), rtol=1e-14)
+
+
+def test_poly2d_examples(olib):
+    # test/zisa/unit_test/math/poly2d.cpp:133-166, tolerance 1e-14
+    coeffs = [1.0, 2.0, 3.0, 4.0, 5.0, 6.0]
+    moments = [0.0, 0.0, 0.0, 1.0, 2.0, 3.0]
+    x0 = olib.poly_eval(2, coeffs, moments, [0, 0, 0], 1.0, [0, 0, 0])
+    assert abs(x0 - (1.0 - 4.0 - 10.0 - 18.0)) <= 1e-14 * 31
+    x, y = -3.0, 2.0
+    exact = 1.0 + 2.0 * x + 3.0 * y + 4.0 * (x * x - 1.0) + 5.0 * (x * y - 2.0) + 6.0 * (y * y - 3.0)
+    assert abs(olib.poly_eval(2, coeffs, moments, [0, 0, 0], 1.0, [x, y, 0]) - exact) <= 1e-14 * abs(exact)
+
+
+def test_poly3d_example(olib):
+    # test/zisa/unit_test/math/poly2d.cpp:201-275 (first variable)
+    c = [1.0, 2.0, -1.0, -3.0, 2.0, 4.0, 2.0, 1.0, 1.0, 3.0]
+    m = [0.0, 0.0, 0.0, 0.0, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0]
+    x, y, z = -3.0, 2.0, 0.2
+    exact = (c[0] + c[1] * x + c[2] * y + c[3] * z + c[4] * (x * x - 1.0) + c[5] * (x * y - 2.0)
+             + c[6] * (x * z - 3.0) + c[7] * (y * y - 4.0) + c[8] * (y * z - 5.0) + c[9] * (z * z - 6.0))
+    assert abs(olib.poly_eval(3, c, m, [0, 0, 0], 1.0, [x, y, z]) - exact) <= 1e-14 * abs(exact)
+
+
+@pytest.mark.parametrize("stages,window,dts", [(1, (0.9, 1.1), (1e-3, 1e-4)), (2, (1.9, 2.1), (1e-3, 1e-4)),
+                                                (3, (2.9, 3.1), (1e-1, 1e-2))])
+def test_runge_kutta_rates(olib, stages, window, dts):
+    # test/zisa/unit_test/ode/runge_kutta.cpp:91-199
+    assert olib.rk_ode_error(stages, 0, 0.01) < 1e-12
+    for ode in (1, 2):
+        coarse, fine = (olib.rk_ode_error(stages, ode, dt) for dt in dts)
+        if fine > 1e-12:
+            rate = (np.log(fine) - np.log(coarse)) / (np.log(dts[1]) - np.log(dts[0]))
+            assert window[0] <= rate <= window[1], (ode, rate)
+
+
+def test_local_equilibrium(olib):
+    # test/zisa/unit_test/model/local_equilibrium.cpp:15-60: gamma 1.2, R 0.9,
+    # ConstantGravityRadial(0.9), quad degree 2, tolerance 1e-9
+    tri = [[1.0, 1.0, 0.0], [1.01, 1.0, 0.0], [1.0, 1.01, 0.0]]
+    x_ref = [0.5, 0.6, 0.0]
+    theta = [10.0, 3.0]
+    rhoE_bar = olib.equilibrium_average(1.2, 1, 0.9, theta, x_ref, tri, 2)
+    x = [1.1, 2.1, 0.0]
+    st, approx, th = olib.local_equilibrium(1.2, 0.9, 1, 0.9, tri, 2, rhoE_bar, x)
+    assert st == 0
+    assert np.allclose(approx, _isentropic_point(1.2, 0.9, theta, x_ref, x), rtol=1e-9)
+    tri2 = [[1.2, 1.1, 0.0], [1.21, 1.1, 0.0], [1.2, 1.11, 0.0]]
+    exact2 = olib.equilibrium_average(1.2, 1, 0.9, theta, x_ref, tri2, 2)
+    approx2 = olib.equilibrium_average(1.2, 1, 0.9, th, _first_qp(tri), tri2, 2)
+    assert np.allclose(approx2, exact2, rtol=1e-9)
+
+
+def _isentropic_point(gamma, g, theta, x_ref, x):
+    # h(x) = h_ref + phi(x_ref) - phi(x), phi = g |x|; rho = ((gamma-1)/gamma h/K)^(1/(gamma-1))
+    h = theta[0] + g * np.linalg.norm(x_ref) - g * np.linalg.norm(x)
+    rho = ((gamma - 1.0) / gamma * h / theta[1]) ** (1.0 / (gamma - 1.0))
+    return np.array([rho, theta[1] * rho ** gamma / (gamma - 1.0)])
+
+
+def _first_qp(tri):
+    # x_ref of LocalEquilibriumBase::solve_exact is the first quadrature point of
+    # the degree-2 rule: barycentric (2/3, 1/6, 1/6)
+    t = np.asarray(tri, float)
+    return list(2.0 / 3.0 * t[0] + 1.0 / 6.0 * t[1] + 1.0 / 6.0 * t[2])

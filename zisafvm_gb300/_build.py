@@ -1,0 +1,84 @@
+"""Build recipe for the native library ``libzfvm.so`` (host C++ + CUDA for sm_103a).
+
+The library is built in-tree (``zisafvm_gb300/libzfvm.so``) with g++ and nvcc
+only; translation units compile in parallel.  Host code is compiled with
+``-ffp-contract=off`` so the set-up arithmetic (geometry, stencils, LSQ
+operators) is bit-identical on x86-64 and aarch64 hosts.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+BUILD = PKG / "_build"
+LIB = PKG / "libzfvm.so"
+INCLUDE = PKG.parent / "include"
+
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
+NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
+             "--expt-relaxed-constexpr"]
+
+HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp"]
+CUDA_SOURCES = ["solver.cu", "inst_s2o3.cu", "inst_s2o2.cu", "inst_s3o3.cu", "inst_s3o2.cu"]
+
+
+def _headers() -> list[Path]:
+    return list(CSRC.glob("*.hpp")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "zfvm.h"]
+
+
+def _stale(obj: Path, src: Path, deps: list[Path]) -> bool:
+    if not obj.exists():
+        return True
+    t = obj.stat().st_mtime
+    return any(p.stat().st_mtime > t for p in [src, *deps])
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def build(verbose: bool = False, force: bool = False) -> Path:
+    """Compile every translation unit that changed and link ``libzfvm.so``."""
+    if shutil.which(NVCC) is None and not os.path.exists(NVCC):
+        raise RuntimeError(f"nvcc not found at {NVCC}")
+    BUILD.mkdir(exist_ok=True)
+    deps = _headers()
+    jobs = []
+    objs = []
+    for name in HOST_SOURCES:
+        src, obj = CSRC / name, BUILD / (name + ".o")
+        objs.append(obj)
+        if force or _stale(obj, src, deps):
+            jobs.append(["g++", *CXXFLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)])
+    for name in CUDA_SOURCES:
+        src, obj = CSRC / name, BUILD / (name + ".o")
+        objs.append(obj)
+        if force or _stale(obj, src, deps):
+            jobs.append([NVCC, *NVCCFLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)])
+    workers = max(1, min(len(jobs), os.cpu_count() or 4))
+    if jobs:
+        with ThreadPoolExecutor(max_workers=workers) as ex:
+            for cmd, _ in zip(jobs, ex.map(_run, jobs)):
+                if verbose:
+                    print(" ".join(cmd), file=sys.stderr)
+    if force or jobs or not LIB.exists():
+        tmp = LIB.with_suffix(".so.tmp")
+        _run([NVCC, "-shared", *ARCH, "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose=True, force="--force" in sys.argv)
+    print(LIB)

@@ -1,0 +1,731 @@
+// GB300 rate-of-change and SSP-RK time stepping: host side of the solver.
+//
+// One Runge-Kutta stage is three kernels (solver_kernels.cuh):
+//   k_reconstruct  one thread per cell: stencil gather, local equilibrium,
+//                  CWENO-AO combination, face-point values and gravity source;
+//   k_face_flux    one thread per face: HLLC / Rusanov or the boundary flux;
+//   k_update       one thread per cell: signed flux gather, RK stage
+//                  combination and the CFL candidate of the new state.
+// A one-thread k_clock kernel opens every step: it turns the CFL minimum of the
+// previous step into dt, clips it to t_end and stops the loop when done, so the
+// whole time loop replays from a CUDA graph without host round trips.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "mesh_obj.hpp"
+#include "solver_kernels.cuh"
+
+namespace zfvm {
+namespace dev {
+
+// mode 0: open a step; mode 1: close the last step only
+__global__ void k_clock(Clock *c, double cfl, int mode) {
+  if (c->started) {
+    c->t += c->dt;
+    c->step += 1;
+    c->started = 0;
+  }
+  if (mode == 1 || c->done) return;
+  bool fin = (c->n_steps > 0 && c->step >= c->n_steps) ||
+             (c->t_end > 0.0 && c->t_end - c->t <= 1e-12 * c->t_end) || c->status != 0;
+  if (fin) {
+    c->done = 1;
+    return;
+  }
+  double dt = c->fixed_dt > 0.0 ? c->fixed_dt : cfl * __longlong_as_double((long long)c->cfl_min);
+  if (c->t_end > 0.0) dt = fmin(dt, c->t_end - c->t);
+  c->dt = dt;
+  c->cfl_min = 0x7ff0000000000000ull;
+  c->started = 1;
+}
+
+// state AoS (n x 5) <-> SoA (NV x ld); the 2D layout drops the third momentum
+__global__ void k_aos_to_soa(const double *aos, double *soa, int n, int ld, int nv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  for (int v = 0; v < nv - 1; ++v) soa[v * ld + i] = aos[i * 5 + v];
+  soa[(nv - 1) * ld + i] = aos[i * 5 + 4];
+}
+
+__global__ void k_soa_to_aos(const double *soa, double *aos, int n, int ld, int nv, const int *src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j = src[i];
+  double r[5] = {0, 0, 0, 0, 0};
+  for (int v = 0; v < nv - 1; ++v) r[v] = soa[v * ld + j];
+  r[4] = soa[(nv - 1) * ld + j];
+  for (int v = 0; v < 5; ++v) aos[i * 5 + v] = r[v];
+}
+
+}  // namespace dev
+}  // namespace zfvm
+
+// ======================================================================= host
+using namespace zfvm;
+using namespace zfvm::dev;
+
+namespace {
+
+struct CudaError {
+  cudaError_t err;
+  std::string where;
+};
+
+#define CK(x)                                                            \
+  do {                                                                   \
+    cudaError_t e_ = (x);                                                \
+    if (e_ != cudaSuccess) throw CudaError{e_, #x};                      \
+  } while (0)
+
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  void alloc(size_t count) {
+    n = count;
+    if (count) CK(cudaMalloc((void **)&p, count * sizeof(T)));
+  }
+  void upload(const std::vector<T> &h) {
+    alloc(h.size());
+    if (n) CK(cudaMemcpy(p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+  }
+  void zero(cudaStream_t s) {
+    if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct zfvm_solver {
+  zfvm_mesh *mesh = nullptr;
+  zfvm_scheme_desc scheme{};
+  int nd = 2, nv = 4, nf = 3, nqf = 2, nqc = 3, ld = 0, lde = 0;
+  int n_cells = 0, n_edges = 0;
+  int shape_id = -1;
+  cudaStream_t stream = nullptr;
+  Params P{};
+  DevData D{};
+  // device buffers
+  DBuf<uint8_t> flags, bloc, fkL, fkR, factive;
+  DBuf<int> l2g, cface, fL, fR, src_map;
+  DBuf<double> pinv, center, inv_len, mom, inv_vol, r_eff, fqx, fqw, frame, farea;
+  DBuf<double> phi_cq, gphi_cq, cqx, cqw, phi_fq;
+  DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos;
+  DBuf<Clock> clock;
+  bool has_src = false, has_eq = false;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  int64_t device_bytes = 0;
+};
+
+namespace {
+
+struct ShapeKey {
+  int nd, R0, C0, NB, RB, CB, nqf, nqc;
+};
+
+template <class S>
+bool matches(const ShapeKey &k) {
+  return k.nd == S::ND && k.R0 == S::R0 && k.C0 == S::C0 && k.NB == S::NB && k.RB == S::RB &&
+         k.CB == S::CB && k.nqf == S::NQF && k.nqc == S::NQC;
+}
+
+
+StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
+  StageArgs a{};
+  a.q = stage == 0 ? s->u0.p : s->ux.p;
+  a.fv = s->fv.p;
+  a.nf = s->nfb.p;
+  a.src = s->has_src ? s->srcb.p : nullptr;
+  a.eqth = s->has_eq ? s->eqth.p : nullptr;
+  a.u0 = s->u0.p;
+  a.ux = s->ux.p;
+  for (int k = 0; k < 4; ++k) a.k[k] = s->kbuf.p ? s->kbuf.p + (size_t)k * s->nv * s->ld : nullptr;
+  a.tend_out = tend_out;
+  a.stage = stage;
+  return a;
+}
+
+LaunchCfg launch_cfg(zfvm_solver *s) {
+  return LaunchCfg{s->n_cells, s->n_edges, s->has_eq, s->has_src, s->scheme.flux == ZFVM_FLUX_HLLC ? 0 : 1, s->stream};
+}
+
+void dispatch_stage(zfvm_solver *s, StageArgs &a) {
+  LaunchCfg c = launch_cfg(s);
+  switch (s->shape_id) {
+    case 0: launch_stage_s2o3(s->D, s->P, a, c); break;
+    case 1: launch_stage_s2o2(s->D, s->P, a, c); break;
+    case 2: launch_stage_s3o3(s->D, s->P, a, c); break;
+    case 3: launch_stage_s3o2(s->D, s->P, a, c); break;
+  }
+  CK(cudaGetLastError());
+}
+
+void launch_cfl(zfvm_solver *s) {
+  LaunchCfg c = launch_cfg(s);
+  switch (s->shape_id) {
+    case 0: launch_cfl_s2o3(s->D, s->P, s->u0.p, c); break;
+    case 1: launch_cfl_s2o2(s->D, s->P, s->u0.p, c); break;
+    case 2: launch_cfl_s3o3(s->D, s->P, s->u0.p, c); break;
+    case 3: launch_cfl_s3o2(s->D, s->P, s->u0.p, c); break;
+  }
+  CK(cudaGetLastError());
+}
+
+void enqueue_step(zfvm_solver *s) {
+  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 0);
+  CK(cudaGetLastError());
+  for (int st = 0; st < s->P.n_stages; ++st) {
+    StageArgs a = stage_args(s, st, nullptr);
+    dispatch_stage(s, a);
+  }
+}
+
+int status_to_code(int st, std::string &msg) {
+  if (st & kStNewton) {
+    msg = "local equilibrium solve is not converging";
+    return ZFVM_ENEWTON;
+  }
+  if (st & kStNonPhysical) {
+    msg = "non-physical state (rho <= 0 or E_int <= 0) in the scaling";
+    return ZFVM_ENONPHYSICAL;
+  }
+  if (st & kStNonFinite) {
+    msg = "non-finite state after a step";
+    return ZFVM_ENONPHYSICAL;
+  }
+  return ZFVM_OK;
+}
+
+Clock read_clock(zfvm_solver *s) {
+  Clock c;
+  CK(cudaMemcpyAsync(&c, s->clock.p, sizeof(Clock), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return c;
+}
+
+void write_clock(zfvm_solver *s, const Clock &c) {
+  CK(cudaMemcpyAsync(s->clock.p, &c, sizeof(Clock), cudaMemcpyHostToDevice, s->stream));
+}
+
+int build_solver(zfvm_solver *s) {
+  zfvm_mesh *m = s->mesh;
+  const Grid &g = m->grid;
+  const StencilFamilies &fam = m->fam;
+  const auto &sc = s->scheme;
+  s->nd = g.n_dims;
+  s->nv = g.n_dims + 2;
+  s->nf = g.n_dims + 1;
+  s->nqf = g.n_face_qp;
+  s->nqc = g.n_cell_qp;
+  s->n_cells = (int)g.n_cells;
+  s->n_edges = (int)g.n_edges;
+  s->ld = (int)((g.n_cells + 31) / 32 * 32);
+  s->lde = (int)((g.n_edges + 31) / 32 * 32);
+  const int ld = s->ld, lde = s->lde, nd = s->nd, nv = s->nv, nf = s->nf;
+  const index_t n = g.n_cells;
+
+  // ---- shape of the stencil family
+  const auto &sp = m->sparams;
+  const int ns = (int)sp.orders.size();
+  if (ns < 2 || sp.biased[0] != 0) return fail(ZFVM_EINVAL, "the first stencil must be the central one");
+  for (int k = 2; k < ns; ++k)
+    if (sp.orders[k] != sp.orders[1] || sp.overfit[k] != sp.overfit[1] || !sp.biased[k])
+      return fail(ZFVM_EINVAL, "all one-sided stencils must share order and overfit factor");
+  ShapeKey key;
+  key.nd = nd;
+  key.R0 = (int)required_stencil_size(sp.orders[0] - 1, sp.overfit[0], nd) - 1;
+  key.C0 = poly_dof(sp.orders[0] - 1, nd) - 1;
+  key.NB = ns - 1;
+  key.RB = (int)required_stencil_size(sp.orders[1] - 1, sp.overfit[1], nd) - 1;
+  key.CB = poly_dof(sp.orders[1] - 1, nd) - 1;
+  key.nqf = s->nqf;
+  key.nqc = s->nqc;
+  if (matches<S2o3>(key))
+    s->shape_id = 0;
+  else if (matches<S2o2>(key))
+    s->shape_id = 1;
+  else if (matches<S3o3>(key))
+    s->shape_id = 2;
+  else if (matches<S3o2>(key))
+    s->shape_id = 3;
+  else
+    return fail(ZFVM_EINVAL, "unsupported stencil / quadrature shape for the GPU kernels");
+  const int R0 = key.R0, C0 = key.C0, NB = key.NB, RB = key.RB, CB = key.CB;
+  const int NC = std::max(C0, CB), NP = R0 * C0 + NB * RB * CB, MAXL = R0 + 1 + NB * RB;
+
+  // ---- scheme parameters
+  if (sc.rk_stages < 1 || sc.rk_stages > 3) return fail(ZFVM_EINVAL, "rk_stages must be 1, 2 or 3");
+  if (sc.steps_per_recompute != 1)
+    return fail(ZFVM_EINVAL, "steps_per_recompute must be 1 (the equilibrium is refreshed every stage)");
+  s->has_eq = sc.equilibrium == ZFVM_EQ_ISENTROPIC;
+  s->has_src = sc.gravity != ZFVM_GRAVITY_NONE;
+  if (s->has_eq && !s->has_src) return fail(ZFVM_EINVAL, "isentropic well-balancing needs gravity");
+  if (sc.flux_bc == ZFVM_FLUX_BC_ISENTROPIC && !s->has_eq)
+    return fail(ZFVM_EINVAL, "isentropic flux boundary needs isentropic well-balancing");
+  Params &P = s->P;
+  P.gamma = sc.gamma;
+  double tot = 0.0;
+  for (int k = 0; k < ns; ++k) tot += sc.linear_weights[k];
+  for (int k = 0; k < ns; ++k) P.lw[k] = sc.linear_weights[k] / tot;
+  P.inv_lw0 = 1.0 / P.lw[0];
+  P.epsilon = sc.epsilon;
+  P.exponent = sc.exponent;
+  P.cfl = sc.cfl_number;
+  P.nqc = s->nqc;
+  P.nqf = s->nqf;
+  P.flux_bc = sc.flux_bc;
+  P.n_stages = sc.rk_stages;
+  std::memset(P.a, 0, sizeof(P.a));
+  std::memset(P.b, 0, sizeof(P.b));
+  if (sc.rk_stages == 1) {
+    P.b[0] = 1.0;
+  } else if (sc.rk_stages == 2) {
+    P.a[1][0] = 1.0;
+    P.b[0] = 0.5, P.b[1] = 0.5;
+  } else {
+    // SSP3 tableau (ode/runge_kutta.cpp:213-224)
+    P.a[1][0] = 1.0;
+    P.a[2][0] = 0.25, P.a[2][1] = 0.25;
+    P.b[0] = 1.0 / 6, P.b[1] = 1.0 / 6, P.b[2] = 2.0 / 3;
+  }
+  {
+    RefRule cr = nd == 2 ? triangle_rule(m->quad.volume) : tetra_rule(m->quad.volume);
+    for (size_t q = 0; q < cr.w.size() && q < 16; ++q) P.what_c[q] = cr.w[q];
+  }
+
+  // ---- per-cell arrays
+  std::vector<uint8_t> h_flags(ld, 0), h_bloc((size_t)NB * RB * ld, 0);
+  std::vector<int> h_l2g((size_t)MAXL * ld, 0), h_cface((size_t)nf * ld, -1), h_src(ld, 0);
+  std::vector<double> h_pinv((size_t)NP * ld, 0.0), h_center((size_t)nd * ld, 0.0), h_il(ld, 0.0),
+      h_mom((size_t)NC * ld, 0.0), h_iv(ld, 0.0), h_reff(ld, 1e300);
+  for (index_t i = 0; i < n; ++i) {
+    h_flags[i] = g.flags[i];
+    h_src[i] = (int)g.source[i];
+    h_iv[i] = 1.0 / g.volumes[i];
+    h_il[i] = 1.0 / g.char_length[i];
+    for (int k = 0; k < nd; ++k) h_center[k * ld + i] = g.cell_centers[i][k];
+    for (int c = 3; c <= NC; ++c) h_mom[(c - 1) * ld + i] = g.moments[i * g.n_moments + c];
+    for (int f = 0; f < nf; ++f) {
+      index_t e = g.edge_indices[i * nf + f];
+      int side = g.left[e] == i ? 0 : 1;
+      h_cface[f * ld + i] = (int)(2 * e + side);
+    }
+    h_reff[g.source[i]] = std::min(h_reff[g.source[i]], g.inradii[i]);
+    const bool active = (g.flags[i] & kInterior) || (g.flags[i] & kGhostL1);
+    if (!active) continue;
+    if (fam.k_high[i] != 0) return fail(ZFVM_EINVAL, "cell whose highest-order stencil is not the central one");
+    const int nl = fam.n_l2g[i];
+    if (nl > MAXL) return fail(ZFVM_EINVAL, "combined stencil larger than the kernel's capacity");
+    for (int l = 0; l < MAXL; ++l) {
+      index_t gl = l < nl ? fam.l2g[i * kMaxL2G + l] : i;
+      h_l2g[(size_t)l * ld + i] = (int)g.source[gl];
+    }
+    // central stencil: local indices are 0..size-1 by construction
+    {
+      const int k = 0;
+      const size_t id = i * kMaxStencils + k;
+      const int sz = fam.size[id];
+      for (int r = 0; r < sz; ++r)
+        if (fam.local[id * kMaxStencilSize + r] != r) return fail(ZFVM_EINVAL, "unexpected central stencil layout");
+      const int rows = m->pinv_rows[id], cols = m->pinv_cols[id];
+      if (rows > R0 || cols > C0) return fail(ZFVM_EINVAL, "central stencil larger than the kernel shape");
+      for (int c = 0; c < cols; ++c)
+        for (int r = 0; r < rows; ++r) h_pinv[((size_t)c * R0 + r) * ld + i] = m->pinv[id][(size_t)c * rows + r];
+    }
+    for (int k = 1; k < ns; ++k) {
+      const size_t id = i * kMaxStencils + k;
+      const int rows = m->pinv_rows[id], cols = m->pinv_cols[id];
+      if (rows > RB || cols > CB) return fail(ZFVM_EINVAL, "one-sided stencil larger than the kernel shape");
+      for (int r = 0; r < RB; ++r)
+        h_bloc[((size_t)(k - 1) * RB + r) * ld + i] =
+            r < rows ? (uint8_t)fam.local[id * kMaxStencilSize + r + 1] : 0;
+      for (int c = 0; c < cols; ++c)
+        for (int r = 0; r < rows; ++r)
+          h_pinv[((size_t)R0 * C0 + ((k - 1) * CB + c) * RB + r) * ld + i] = m->pinv[id][(size_t)c * rows + r];
+    }
+  }
+  // ---- faces
+  const int nqf = s->nqf;
+  std::vector<int> h_fL(lde, 0), h_fR(lde, -1);
+  std::vector<uint8_t> h_fkL(lde, 0), h_fkR(lde, 0), h_fact(lde, 0);
+  std::vector<double> h_fqx((size_t)nqf * nd * lde, 0.0), h_fqw((size_t)nqf * lde, 0.0),
+      h_frame((size_t)nd * nd * lde, 0.0), h_farea(lde, 0.0);
+  for (index_t e = 0; e < g.n_edges; ++e) {
+    index_t L = g.left[e], R = g.right[e];
+    h_fL[e] = (int)L;
+    h_fR[e] = (int)R;
+    for (int f = 0; f < nf; ++f) {
+      if (g.edge_indices[L * nf + f] == e) h_fkL[e] = (uint8_t)f;
+      if (R >= 0 && g.edge_indices[R * nf + f] == e) h_fkR[e] = (uint8_t)f;
+    }
+    bool Lint = g.flags[L] & kInterior, Rint = R >= 0 && (g.flags[R] & kInterior);
+    if (R >= 0)
+      h_fact[e] = Lint || Rint;
+    else
+      h_fact[e] = Lint && sc.flux_bc != ZFVM_FLUX_BC_NONE;
+    for (int q = 0; q < nqf; ++q) {
+      h_fqw[(size_t)q * lde + e] = g.face_qw[e * nqf + q];
+      for (int k = 0; k < nd; ++k) h_fqx[((size_t)q * nd + k) * lde + e] = g.face_qx[e * nqf + q][k];
+    }
+    Vec3 fr[3] = {g.face_normal[e], g.face_t1[e], g.face_t2[e]};
+    for (int a2 = 0; a2 < nd; ++a2)
+      for (int k = 0; k < nd; ++k) h_frame[((size_t)a2 * nd + k) * lde + e] = fr[a2][k];
+    h_farea[e] = g.face_area[e];
+  }
+  // ---- gravity potential at quadrature points (phi = g r or k r^2 / 2 radially)
+  const int nqc = s->nqc;
+  std::vector<double> h_phi_cq, h_gphi_cq, h_cqx, h_cqw, h_phi_fq;
+  if (s->has_src) {
+    auto phi = [&](const Vec3 &x) {
+      double r = norm(x);
+      return sc.gravity == ZFVM_GRAVITY_CONSTANT_RADIAL ? sc.gravity_strength * r : 0.5 * sc.gravity_strength * r * r;
+    };
+    auto gphi = [&](const Vec3 &x, int dir) {
+      // Gravity::dphi_dx = phi'(r) x_dir / (r + 1e-50)  (model/gravity_decl.hpp:24-36,85-88)
+      double r = norm(x);
+      double dphi = sc.gravity == ZFVM_GRAVITY_CONSTANT_RADIAL ? sc.gravity_strength : sc.gravity_strength * r;
+      return dphi * (x[dir] / (r + 1e-50));
+    };
+    h_phi_cq.assign((size_t)nqc * ld, 0.0);
+    h_gphi_cq.assign((size_t)nqc * nd * ld, 0.0);
+    h_cqx.assign((size_t)nqc * nd * ld, 0.0);
+    h_cqw.assign((size_t)nqc * ld, 0.0);
+    h_phi_fq.assign((size_t)nqf * lde, 0.0);
+    for (index_t i = 0; i < n; ++i)
+      for (int q = 0; q < nqc; ++q) {
+        const Vec3 &x = g.cell_qx[i * nqc + q];
+        h_phi_cq[(size_t)q * ld + i] = phi(x);
+        h_cqw[(size_t)q * ld + i] = g.cell_qw[i * nqc + q];
+        for (int k = 0; k < nd; ++k) {
+          h_gphi_cq[((size_t)q * nd + k) * ld + i] = gphi(x, k);
+          h_cqx[((size_t)q * nd + k) * ld + i] = x[k];
+        }
+      }
+    for (index_t e = 0; e < g.n_edges; ++e)
+      for (int q = 0; q < nqf; ++q) h_phi_fq[(size_t)q * lde + e] = phi(g.face_qx[e * nqf + q]);
+  }
+
+  CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  s->flags.upload(h_flags);
+  s->bloc.upload(h_bloc);
+  s->l2g.upload(h_l2g);
+  s->cface.upload(h_cface);
+  s->src_map.upload(h_src);
+  s->pinv.upload(h_pinv);
+  s->center.upload(h_center);
+  s->inv_len.upload(h_il);
+  s->mom.upload(h_mom);
+  s->inv_vol.upload(h_iv);
+  s->r_eff.upload(h_reff);
+  s->fL.upload(h_fL);
+  s->fR.upload(h_fR);
+  s->fkL.upload(h_fkL);
+  s->fkR.upload(h_fkR);
+  s->factive.upload(h_fact);
+  s->fqx.upload(h_fqx);
+  s->fqw.upload(h_fqw);
+  s->frame.upload(h_frame);
+  s->farea.upload(h_farea);
+  if (s->has_src) {
+    s->phi_cq.upload(h_phi_cq);
+    s->gphi_cq.upload(h_gphi_cq);
+    s->cqx.upload(h_cqx);
+    s->cqw.upload(h_cqw);
+    s->phi_fq.upload(h_phi_fq);
+    s->srcb.alloc((size_t)nv * ld);
+  }
+  if (s->has_eq) s->eqth.alloc((size_t)3 * ld);
+  s->u0.alloc((size_t)nv * ld);
+  s->ux.alloc((size_t)nv * ld);
+  s->kbuf.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
+  s->fv.alloc((size_t)nf * nqf * nv * ld);
+  s->nfb.alloc((size_t)nv * lde);
+  s->tend.alloc((size_t)nv * ld);
+  s->aos.alloc((size_t)5 * n);
+  s->clock.alloc(1);
+  for (auto *b : {&s->u0, &s->ux, &s->kbuf, &s->fv, &s->nfb, &s->tend}) b->zero(s->stream);
+  if (s->has_src) s->srcb.zero(s->stream);
+  if (s->has_eq) s->eqth.zero(s->stream);
+  Clock c{};
+  c.cfl_min = 0x7ff0000000000000ull;
+  write_clock(s, c);
+  CK(cudaStreamSynchronize(s->stream));
+
+  DevData &D = s->D;
+  D.n_cells = s->n_cells;
+  D.ld = ld;
+  D.n_edges = s->n_edges;
+  D.lde = lde;
+  D.flags = s->flags.p;
+  D.l2g = s->l2g.p;
+  D.pinv = s->pinv.p;
+  D.bloc = s->bloc.p;
+  D.center = s->center.p;
+  D.inv_len = s->inv_len.p;
+  D.mom = s->mom.p;
+  D.cface = s->cface.p;
+  D.inv_vol = s->inv_vol.p;
+  D.r_eff = s->r_eff.p;
+  D.fL = s->fL.p;
+  D.fR = s->fR.p;
+  D.fkL = s->fkL.p;
+  D.fkR = s->fkR.p;
+  D.factive = s->factive.p;
+  D.fqx = s->fqx.p;
+  D.fqw = s->fqw.p;
+  D.frame = s->frame.p;
+  D.farea = s->farea.p;
+  D.phi_cq = s->phi_cq.p;
+  D.gphi_cq = s->gphi_cq.p;
+  D.cqx = s->cqx.p;
+  D.cqw = s->cqw.p;
+  D.phi_fq = s->phi_fq.p;
+  D.clock = s->clock.p;
+
+  int64_t bytes = 0;
+  auto add = [&](size_t nbytes) { bytes += (int64_t)nbytes; };
+  add(s->flags.n + s->bloc.n + s->fkL.n + s->fkR.n + s->factive.n);
+  add(4 * (s->l2g.n + s->cface.n + s->fL.n + s->fR.n + s->src_map.n));
+  add(8 * (s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
+           s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
+           s->ux.n + s->kbuf.n + s->fv.n + s->nfb.n + s->srcb.n + s->eqth.n + s->tend.n + s->aos.n));
+  s->device_bytes = bytes;
+  return ZFVM_OK;
+}
+
+int cuda_fail(const CudaError &e) {
+  return fail(ZFVM_ECUDA, e.where + ": " + cudaGetErrorString(e.err));
+}
+
+void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt) {
+  Clock c = read_clock(s);
+  c.done = 0;
+  c.started = 0;
+  c.step = 0;
+  c.n_steps = n_steps;
+  c.t_end = t_end;
+  c.fixed_dt = fixed_dt;
+  write_clock(s, c);
+}
+
+void build_graph(zfvm_solver *s, int steps) {
+  if (s->graph && s->graph_steps == steps) return;
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < steps; ++k) enqueue_step(s);
+  CK(cudaStreamEndCapture(s->stream, &g));
+  CK(cudaGraphInstantiate(&s->graph, g, 0));
+  cudaGraphDestroy(g);
+  s->graph_steps = steps;
+}
+
+}  // namespace
+
+#define SOLVER_GUARD_BEGIN try {
+#define SOLVER_GUARD_END                                  \
+  }                                                       \
+  catch (const CudaError &e) {                            \
+    return cuda_fail(e);                                  \
+  }                                                       \
+  catch (const SetupError &e) {                           \
+    return fail(ZFVM_ESETUP, e.what());                   \
+  }                                                       \
+  catch (const std::bad_alloc &) {                        \
+    return fail(ZFVM_ENOMEM, "host allocation failed");   \
+  }
+
+extern "C" int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *sc, zfvm_solver **out) {
+  if (!m || !sc || !out) return fail(ZFVM_EINVAL, "null argument");
+  if (sc->precision != ZFVM_FP64) return fail(ZFVM_EINVAL, "precision not available in this build");
+  if (!(sc->gamma > 1.0) || !(sc->cfl_number > 0.0)) return fail(ZFVM_EINVAL, "bad gamma or cfl_number");
+  auto s = std::make_unique<zfvm_solver>();
+  s->mesh = m;
+  s->scheme = *sc;
+  SOLVER_GUARD_BEGIN
+  int st = build_solver(s.get());
+  if (st != ZFVM_OK) return st;
+  *out = s.release();
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_solver_destroy(zfvm_solver *s) {
+  if (!s) return ZFVM_OK;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->stream) {
+    cudaStreamSynchronize(s->stream);
+    cudaStreamDestroy(s->stream);
+  }
+  delete s;
+  return ZFVM_OK;
+}
+
+extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
+  if (!s || !cvars) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
+  const size_t n = s->n_cells;
+  CK(cudaMemcpyAsync(s->aos.p, cvars, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  k_aos_to_soa<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->aos.p, s->u0.p, (int)n, s->ld, s->nv);
+  CK(cudaGetLastError());
+  Clock c{};
+  c.t = t;
+  c.cfl_min = 0x7ff0000000000000ull;
+  write_clock(s, c);
+  launch_cfl(s);
+  CK(cudaStreamSynchronize(s->stream));
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_get_state(zfvm_solver *s, double *cvars, double *t) {
+  if (!s) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
+  const size_t n = s->n_cells;
+  k_soa_to_aos<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->aos.p, (int)n, s->ld, s->nv, s->src_map.p);
+  CK(cudaGetLastError());
+  if (cvars) CK(cudaMemcpyAsync(cvars, s->aos.p, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  Clock c = read_clock(s);
+  if (t) *t = c.t;
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_rate_of_change(zfvm_solver *s, double *tendency) {
+  if (!s || !tendency) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
+  Clock c = read_clock(s);
+  c.done = 0;
+  c.status = 0;
+  write_clock(s, c);
+  CK(cudaMemsetAsync(s->tend.p, 0, s->tend.n * sizeof(double), s->stream));
+  StageArgs a = stage_args(s, 0, s->tend.p);
+  dispatch_stage(s, a);
+  const size_t n = s->n_cells;
+  std::vector<int> ident(n);
+  for (size_t i = 0; i < n; ++i) ident[i] = (int)i;
+  DBuf<int> idb;
+  idb.upload(ident);
+  k_soa_to_aos<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->tend.p, s->aos.p, (int)n, s->ld, s->nv, idb.p);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(tendency, s->aos.p, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  Clock c2 = read_clock(s);
+  std::string msg;
+  int code = status_to_code(c2.status, msg);
+  if (code) return fail(code, msg);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_cfl_dt(zfvm_solver *s, double *dt) {
+  if (!s || !dt) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
+  Clock c = read_clock(s);
+  c.cfl_min = 0x7ff0000000000000ull;
+  write_clock(s, c);
+  launch_cfl(s);
+  c = read_clock(s);
+  *dt = s->P.cfl * __builtin_bit_cast(double, c.cfl_min);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_step(zfvm_solver *s, double dt) {
+  if (!s || !(dt > 0.0)) return fail(ZFVM_EINVAL, "bad argument");
+  SOLVER_GUARD_BEGIN
+  reset_clock_for_run(s, 1, 0.0, dt);
+  enqueue_step(s);
+  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
+  CK(cudaGetLastError());
+  Clock c = read_clock(s);
+  std::string msg;
+  int code = status_to_code(c.status, msg);
+  if (code) return fail(code, msg);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_advance(zfvm_solver *s, int64_t n_steps, double t_end, double *t_out, int64_t *steps_out) {
+  if (!s) return fail(ZFVM_EINVAL, "null solver");
+  if (n_steps <= 0 && !(t_end > 0.0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > 0");
+  SOLVER_GUARD_BEGIN
+  reset_clock_for_run(s, n_steps, t_end, 0.0);
+  const int chunk = 16;
+  build_graph(s, chunk);
+  int64_t launched = 0;
+  while (true) {
+    CK(cudaGraphLaunch(s->graph, s->stream));
+    launched += chunk;
+    if (n_steps > 0 && launched >= n_steps) break;
+    if (launched % (chunk * 8) == 0 || n_steps <= 0) {
+      Clock c = read_clock(s);
+      if (c.done) break;
+    }
+  }
+  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
+  CK(cudaGetLastError());
+  Clock c = read_clock(s);
+  if (t_out) *t_out = c.t;
+  if (steps_out) *steps_out = c.step;
+  std::string msg;
+  int code = status_to_code(c.status, msg);
+  if (code) return fail(code, msg);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_advance_timed(zfvm_solver *s, int64_t n_steps, float *ms) {
+  if (!s || !ms || n_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  SOLVER_GUARD_BEGIN
+  reset_clock_for_run(s, n_steps, 0.0, 0.0);
+  const int chunk = (int)std::min<int64_t>(n_steps, 16);
+  build_graph(s, chunk);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaEventRecord(e0, s->stream));
+  int64_t launched = 0;
+  while (launched < n_steps) {
+    CK(cudaGraphLaunch(s->graph, s->stream));
+    launched += chunk;
+  }
+  CK(cudaEventRecord(e1, s->stream));
+  CK(cudaEventSynchronize(e1));
+  CK(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
+  Clock c = read_clock(s);
+  std::string msg;
+  int code = status_to_code(c.status, msg);
+  if (code) return fail(code, msg);
+  if (c.step != n_steps) return fail(ZFVM_EINVAL, "step count mismatch in the timed loop");
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_launches_per_step(const zfvm_solver *s, int32_t *launches) {
+  if (!s || !launches) return fail(ZFVM_EINVAL, "null argument");
+  *launches = 1 + 3 * s->P.n_stages;
+  return ZFVM_OK;
+}
+
+extern "C" int zfvm_device_bytes(const zfvm_solver *s, int64_t *bytes) {
+  if (!s || !bytes) return fail(ZFVM_EINVAL, "null argument");
+  *bytes = s->device_bytes;
+  return ZFVM_OK;
+}

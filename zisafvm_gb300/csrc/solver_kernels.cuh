@@ -1,0 +1,755 @@
+// Device kernels of the GB300 rate-of-change and SSP-RK time stepping.
+//
+// One Runge-Kutta stage is three kernels:
+//   k_reconstruct  one thread per cell: gather the stencil cell averages, the
+//                  (optional) local hydrostatic equilibrium, CWENO-AO
+//                  combination of the LSQ polynomials, evaluation at the
+//                  cell's face quadrature points and the gravity source.
+//   k_face_flux    one thread per face: numerical flux (HLLC / Rusanov) from
+//                  the two face-point values, or the boundary flux.
+//   k_update       one thread per cell: signed gather of the face fluxes,
+//                  RK stage combination, CFL candidate of the new state.
+// A one-thread k_clock kernel opens every step: it turns the CFL minimum of the
+// previous step into dt, clips it to t_end and stops the loop when done, so the
+// whole time loop runs from a CUDA graph without host round trips.
+//
+// The arithmetic is the reference's (ZisaFVM: reconstruction/cweno_ao.cpp,
+// hybrid_weno.cpp, fvm_loops/flux_loop.hpp, gravity_source_loop.hpp,
+// ode/runge_kutta.cpp, model/local_cfl_condition_impl.hpp), rearranged for the
+// GPU: the LSQ solve uses a pseudo-inverse built on the host, the stencil values
+// are reconstructed unscaled and the EulerScaling enters only the smoothness
+// indicators, and the face-flux scatter is a deterministic cell-centric gather
+// instead of OpenMP atomics.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "grid.hpp"
+#include "physics.cuh"
+
+namespace zfvm {
+namespace dev {
+
+enum StatusBits : int { kStNonPhysical = 1, kStNewton = 2, kStNonFinite = 4 };
+
+struct Clock {
+  double t, dt, t_end, fixed_dt;
+  unsigned long long cfl_min;  // bits of a positive double
+  long long step, n_steps;
+  int done, started, status, pad;
+};
+
+// Device arrays shared by all kernels (struct of pointers, passed by value).
+struct DevData {
+  int n_cells, ld, n_edges, lde;
+  const uint8_t *flags;
+  const int *l2g;        // [MAXL][ld] through the periodic source map
+  const double *pinv;    // [NP][ld]
+  const uint8_t *bloc;   // [NB*RB][ld]
+  const double *center;  // [ND][ld]
+  const double *inv_len; // [ld]
+  const double *mom;     // [NC][ld] (C_1 .. C_NC of the final polynomial)
+  const int *cface;      // [NF][ld]  2 * edge + side, -1 when absent
+  const double *inv_vol; // [ld]
+  const double *r_eff;   // [ld] in-radius, minimum over the cell and its ghost images
+  const int *fL, *fR;    // [lde]
+  const uint8_t *fkL, *fkR, *factive;
+  const double *fqx;     // [NQF][ND][lde]
+  const double *fqw;     // [NQF][lde]
+  const double *frame;   // [ND*ND][lde]: normal, tangent 1 (, tangent 2)
+  const double *farea;   // [lde]
+  // equilibrium / gravity
+  const double *phi_cq;  // [NQC][ld]
+  const double *gphi_cq; // [NQC][ND][ld]
+  const double *cqx;     // [NQC][ND][ld]
+  const double *cqw;     // [NQC][ld]
+  const double *phi_fq;  // [NQF][lde]
+  Clock *clock;
+};
+
+struct Params {
+  double gamma;
+  double lw[5];      // normalised linear weights
+  double inv_lw0;    // 1 / lw[0]
+  double epsilon, exponent;
+  double cfl;
+  double what_c[16]; // reference-cell volume weights (sum to one)
+  int nqc, nqf;
+  int flux_bc;       // 0 none, 1 constant, 2 isentropic
+  int n_stages;
+  double a[4][4], b[4];
+};
+
+struct StageArgs {
+  const double *q;   // stage state
+  double *fv;        // face values [NF*NQF*NV][ld]
+  double *nf;        // face fluxes [NV][lde]
+  double *src;       // per-cell source [NV][ld]
+  double *eqth;      // per-cell equilibrium (h, K, found) [3][ld]
+  double *u0;        // state at the start of the step
+  double *ux;        // next stage state
+  double *k[4];      // stage tendencies
+  double *tend_out;  // when non-null: write the tendency and do no RK update
+  int stage;
+};
+
+template <int NDIM_, int R0_, int C0_, int NB_, int RB_, int CB_, int NQF_, int NQC_>
+struct Shape {
+  static constexpr int ND = NDIM_, NV = NDIM_ + 2, NF = NDIM_ + 1;
+  static constexpr int R0 = R0_, C0 = C0_, NB = NB_, RB = RB_, CB = CB_;
+  static constexpr int NC = C0_ > CB_ ? C0_ : CB_;
+  static constexpr int NP = R0_ * C0_ + NB_ * RB_ * CB_;
+  static constexpr int MAXL = R0_ + 1 + NB_ * RB_;
+  static constexpr int NQF = NQF_, NQC = NQC_;
+};
+
+__device__ __forceinline__ double powd(double x, double y) {
+  if (y == 1.0) return x;
+  if (y == 2.0) return x * x;
+  return pow(x, y);
+}
+
+// Non-constant monomials of the scaled offset X in poly_index order
+// (math/poly2d_impl.hpp:176-183), minus the normalized moments.
+template <int ND, int NC>
+__device__ __forceinline__ void basis(const double *X, const double *C, double *phi) {
+  if (ND == 2) {
+    const double x = X[0], y = X[1];
+    double m[5] = {x, y, x * x, x * y, y * y};
+#pragma unroll
+    for (int c = 0; c < NC; ++c) phi[c] = m[c] - C[c];
+  } else {
+    const double x = X[0], y = X[1], z = X[2];
+    double m[9] = {x, y, z, x * x, x * y, x * z, y * y, y * z, z * z};
+#pragma unroll
+    for (int c = 0; c < NC; ++c) phi[c] = m[c] - C[c];
+  }
+}
+
+// Isentropic equilibrium (model/isentropic_equilibrium.hpp:27-63 with
+// IdealGasEOS::rhoE(EnthalpyEntropy), ideal_gas_eos.hpp:162-168):
+//   h(x) = h_ref + phi_ref - phi(x),  rho = ((gamma-1)/gamma h / K)^(1/(gamma-1)),
+//   E = K rho^gamma / (gamma-1).
+struct EqEval {
+  double gamma, gm1, inv_gm1;
+  __device__ __forceinline__ void at(double h_ref, double K, double phi_ref, double phi, double &rho,
+                                     double &E) const {
+    double h = h_ref + phi_ref - phi;
+    double base = 1.0 / K * gm1 / gamma * h;
+    rho = powd(base, inv_gm1);
+    double p = K * powd(rho, gamma);
+    E = p / gm1;
+  }
+};
+
+// Average of the equilibrium over a cell from its quadrature-point potentials.
+template <int NQC>
+__device__ __forceinline__ void eq_average(const EqEval &ev, const double *what, double h, double K,
+                                           double phi_ref, const double *phi, double &rb, double &Eb) {
+  double r, e;
+  ev.at(h, K, phi_ref, phi[0], r, e);
+  rb = what[0] * r;
+  Eb = what[0] * e;
+#pragma unroll
+  for (int q = 1; q < NQC; ++q) {
+    ev.at(h, K, phi_ref, phi[q], r, e);
+    rb += what[q] * r;
+    Eb += what[q] * e;
+  }
+}
+
+// LocalEquilibriumBase::solve_exact + quasi_newton (local_equilibrium_impl.hpp:40-94,
+// math/quasi_newton.hpp:12-50, rolling_convergence_rate.hpp): finite-difference
+// Jacobian, atol = 1e-13 * guess, at most 20 iterations.  Returns 0 when the
+// equilibrium was found, 1 when it was not (the reference then extrapolates
+// zeros), 2 when the iteration diverged (the reference aborts).
+template <int NQC>
+__device__ int solve_equilibrium(const EqEval &ev, const double *what, const double *phi, double rho_bar,
+                                 double E_bar, double &h_out, double &K_out) {
+  const double gamma = ev.gamma;
+  const double phi_ref = phi[0];
+  const double p_g = E_bar * ev.gm1;
+  const double h0 = gamma / ev.gm1 * p_g / rho_bar;
+  const double K0 = p_g / pow(rho_bar, gamma);
+  const double atol0 = 1e-13 * h0, atol1 = 1e-13 * K0;
+  auto f = [&](double h, double K, double &f0, double &f1) {
+    double rb, Eb;
+    eq_average<NQC>(ev, what, h, K, phi_ref, phi, rb, Eb);
+    f0 = rho_bar - rb;
+    f1 = E_bar - Eb;
+  };
+  double x0 = h0, x1 = K0, fx0, fx1;
+  f(x0, x1, fx0, fx1);
+  double dx0 = 2.0 * atol0 + 1.0, dx1 = 2.0 * atol1 + 1.0;
+  double hist0[3] = {0, 0, 0}, hist1[3] = {0, 0, 0};
+  int n_hist = 0;
+  int iter = 0;
+  while (!(fabs(dx0) <= atol0 && fabs(dx1) <= atol1) && iter < 20) {
+    double eps0 = 1e-6 * fabs(x0), eps1 = 1e-6 * fabs(x1);
+    double a0, a1, b0, b1;
+    f(x0 + 0.5 * eps0, x1, a0, a1);
+    f(x0 - 0.5 * eps0, x1, b0, b1);
+    double d00 = (a0 - b0) / eps0, d01 = (a1 - b1) / eps0;
+    f(x0, x1 + 0.5 * eps1, a0, a1);
+    f(x0, x1 - 0.5 * eps1, b0, b1);
+    double d10 = (a0 - b0) / eps1, d11 = (a1 - b1) / eps1;
+    double inv_det = 1.0 / (d00 * d11 - d01 * d10);
+    dx0 = inv_det * (d11 * fx0 - d10 * fx1);
+    dx1 = inv_det * (-d01 * fx0 + d00 * fx1);
+    x0 -= dx0;
+    x1 -= dx1;
+    f(x0, x1, fx0, fx1);
+    hist0[0] = hist0[1], hist0[1] = hist0[2], hist0[2] = dx0;
+    hist1[0] = hist1[1], hist1[1] = hist1[2], hist1[2] = dx1;
+    ++n_hist;
+    if (iter >= 4) {
+      bool conv = (hist0[2] <= atol0) && (hist1[2] <= atol1);
+      if (!conv) {
+        double r0 = log(fabs(hist0[2]) / fabs(hist0[1])) / log(fabs(hist0[1]) / fabs(hist0[0]));
+        double r1 = log(fabs(hist1[2]) / fabs(hist1[1])) / log(fabs(hist1[1]) / fabs(hist1[0]));
+        if (!(r0 >= 0.0 && r1 >= 0.0)) {
+          h_out = h0;
+          K_out = K0;
+          return 2;
+        }
+      }
+    }
+    ++iter;
+  }
+  if (iter == 20 && !(fabs(dx0) <= 1000.0 * atol0 && fabs(dx1) <= 1000.0 * atol1)) {
+    h_out = h0;
+    K_out = K0;
+    return 1;
+  }
+  h_out = x0;
+  K_out = x1;
+  return 0;
+}
+
+__device__ __forceinline__ void set_status(Clock *c, int bits) { atomicOr(&c->status, bits); }
+
+// --------------------------------------------------------------- kernels
+template <class S, int EQ, int SRC>
+__global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Params P, StageArgs a) {
+  constexpr int NV = S::NV, ND = S::ND, NF = S::NF, NC = S::NC;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.n_cells) return;
+  if (d.clock->done) return;
+  const uint8_t fl = d.flags[i];
+  if (!(fl & (kInterior | kGhostL1))) return;
+  const int ld = d.ld;
+  const double *__restrict__ q = a.q;
+  const double gamma = P.gamma;
+  EqEval ev{gamma, gamma - 1.0, 1.0 / (gamma - 1.0)};
+
+  const int j0 = d.l2g[i];
+  double u0[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) u0[v] = q[v * ld + j0];
+  const double rho = u0[0];
+  const double eint = u0[NV - 1] - kinetic_energy<NV>(u0);
+  if (!(rho > 0.0) || !(eint > 0.0)) {
+    set_status(d.clock, kStNonPhysical);
+    return;
+  }
+  // EulerScaling (model/characteristic_scale.hpp:23-32): {rho, c, c, c, E_int}
+  const double cs = sqrt(gamma * (eint * (gamma - 1.0)) / rho);
+  double inv_s2[NV];
+  inv_s2[0] = 1.0 / (rho * rho);
+#pragma unroll
+  for (int v = 1; v < NV - 1; ++v) inv_s2[v] = 1.0 / (cs * cs);
+  inv_s2[NV - 1] = 1.0 / (eint * eint);
+
+  // local equilibrium of this cell from its own average
+  double eh = 0.0, eK = 0.0, phi_ref = 0.0;
+  bool found = false;
+  double phi_own[S::NQC];
+  if (EQ) {
+#pragma unroll
+    for (int qq = 0; qq < S::NQC; ++qq) phi_own[qq] = d.phi_cq[qq * ld + i];
+    phi_ref = phi_own[0];
+    int st = solve_equilibrium<S::NQC>(ev, P.what_c, phi_own, rho, eint, eh, eK);
+    found = st == 0;
+    if (st == 2) set_status(d.clock, kStNewton);
+    a.eqth[i] = eh;
+    a.eqth[ld + i] = eK;
+    a.eqth[2 * ld + i] = found ? 1.0 : 0.0;
+  }
+  // deviation of a stencil cell from this cell's equilibrium
+  auto load_dev = [&](int j, double *out) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[v] = q[v * ld + j];
+    if (EQ && found) {
+      double phi_j[S::NQC];
+#pragma unroll
+      for (int qq = 0; qq < S::NQC; ++qq) phi_j[qq] = d.phi_cq[qq * ld + j];
+      double rb, Eb;
+      eq_average<S::NQC>(ev, P.what_c, eh, eK, phi_ref, phi_j, rb, Eb);
+      out[0] -= rb;
+      out[NV - 1] -= Eb;
+    }
+  };
+  double dev0[NV];
+  if (EQ) {
+    // the own cell goes through the same path so padded rows cancel exactly
+    load_dev(j0, dev0);
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dev0[v] = u0[v];
+  }
+
+  // LSQ fits: coefficients 1..C of every stencil, unscaled
+  double b0[S::C0][NV];
+#pragma unroll
+  for (int c = 0; c < S::C0; ++c)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) b0[c][v] = 0.0;
+#pragma unroll 2
+  for (int r = 0; r < S::R0; ++r) {
+    double dq[NV];
+    load_dev(d.l2g[(r + 1) * ld + i], dq);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) dq[v] -= dev0[v];
+#pragma unroll
+    for (int c = 0; c < S::C0; ++c) {
+      const double pc = d.pinv[(c * S::R0 + r) * ld + i];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) b0[c][v] += pc * dq[v];
+    }
+  }
+  double bb[S::NB][S::CB][NV];
+#pragma unroll
+  for (int k = 0; k < S::NB; ++k) {
+#pragma unroll
+    for (int c = 0; c < S::CB; ++c)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) bb[k][c][v] = 0.0;
+#pragma unroll
+    for (int r = 0; r < S::RB; ++r) {
+      const int l = d.bloc[(k * S::RB + r) * ld + i];
+      double dq[NV];
+      load_dev(d.l2g[l * ld + i], dq);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) dq[v] -= dev0[v];
+#pragma unroll
+      for (int c = 0; c < S::CB; ++c) {
+        const double pc = d.pinv[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
+      }
+    }
+  }
+
+  // CWENO-AO: p_c = (p_opt - sum_k g_k p_k) / g_c   (cweno_ao.cpp:35-53)
+  double pf[NC][NV];
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double x = c < S::C0 ? b0[c][v] : 0.0;
+#pragma unroll
+      for (int k = 0; k < S::NB; ++k)
+        if (c < S::CB) x -= P.lw[k + 1] * bb[k][c][v];
+      pf[c][v] = x * P.inv_lw0;
+    }
+  // smoothness indicators in the scaled variables (poly2d_impl.hpp:325-337)
+  auto indicator = [&](auto coef, int ncoef) {
+    double m = 0.0;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double s = 0.0;
+      for (int c = 0; c < ncoef; ++c) s += coef(c, v) * coef(c, v);
+      m = fmax(m, s * inv_s2[v]);
+    }
+    return m;
+  };
+  double alpha[S::NB + 1];
+  auto weight = [&](double IS, double g) {
+    double pw = P.exponent == 4.0 ? (IS * IS) * (IS * IS) : pow(IS, P.exponent);
+    return g / (P.epsilon + pw);
+  };
+  alpha[0] = weight(indicator([&](int c, int v) { return pf[c][v]; }, S::C0), P.lw[0]);
+#pragma unroll
+  for (int k = 0; k < S::NB; ++k)
+    alpha[k + 1] = weight(indicator([&](int c, int v) { return bb[k][c][v]; }, S::CB), P.lw[k + 1]);
+  double al_tot = 0.0;
+#pragma unroll
+  for (int k = 0; k <= S::NB; ++k) al_tot += alpha[k];
+  // eno_hybridize (hybrid_weno.cpp:109-128)
+  {
+    const double w0 = alpha[0] / al_tot;
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double x = w0 * pf[c][v];
+#pragma unroll
+        for (int k = 0; k < S::NB; ++k)
+          if (c < S::CB) x += (alpha[k + 1] / al_tot) * bb[k][c][v];
+        pf[c][v] = x;
+      }
+  }
+
+  double xc[ND], C[NC];
+#pragma unroll
+  for (int k = 0; k < ND; ++k) xc[k] = d.center[k * ld + i];
+  const double il = d.inv_len[i];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) C[c] = d.mom[c * ld + i];
+  auto delta_at = [&](const double *x, double *du) {
+    double X[ND], phi[NC];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) X[k] = (x[k] - xc[k]) * il;
+    basis<ND, NC>(X, C, phi);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double s = dev0[v];
+#pragma unroll
+      for (int c = 0; c < NC; ++c) s += pf[c][v] * phi[c];
+      du[v] = s;
+    }
+  };
+
+  double s_acc[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) s_acc[v] = 0.0;
+
+  // values at the face quadrature points of this cell
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const int cf = d.cface[f * ld + i];
+    if (cf < 0) continue;
+    const int e = cf >> 1;
+    const double sgn = (cf & 1) ? -1.0 : 1.0;
+#pragma unroll
+    for (int qq = 0; qq < S::NQF; ++qq) {
+      double x[ND];
+#pragma unroll
+      for (int k = 0; k < ND; ++k) x[k] = d.fqx[(qq * ND + k) * d.lde + e];
+      double u[NV];
+      delta_at(x, u);
+      if (EQ && found) {
+        double r, E;
+        ev.at(eh, eK, phi_ref, d.phi_fq[qq * d.lde + e], r, E);
+        u[0] += r;
+        u[NV - 1] += E;
+        if (SRC) {
+          // surface part of the well-balanced source: p_eq n_out
+          const double p_eq = E * ev.gm1;
+          const double w = d.fqw[qq * d.lde + e];
+#pragma unroll
+          for (int k = 0; k < ND; ++k) s_acc[1 + k] += w * (p_eq * sgn * d.frame[k * d.lde + e]);
+        }
+      }
+      double *out = a.fv + ((size_t)((f * S::NQF + qq) * NV)) * ld + i;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) out[(size_t)v * ld] = u[v];
+    }
+  }
+
+  if (SRC) {
+    // volume part: (0, -rho' grad phi, -m . grad phi), rho' = delta (well-balanced)
+    // or the full reconstruction (gravity_source_loop.hpp:60-84,121-148)
+#pragma unroll
+    for (int qq = 0; qq < S::NQC; ++qq) {
+      double x[ND], g[ND];
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        x[k] = d.cqx[(qq * ND + k) * ld + i];
+        g[k] = d.gphi_cq[(qq * ND + k) * ld + i];
+      }
+      double du[NV];
+      delta_at(x, du);
+      double r = du[0];
+      if (EQ && found) {
+        // du already is the deviation; its density is the source density
+      }
+      const double w = d.cqw[qq * ld + i];
+      double mg = 0.0;
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        s_acc[1 + k] += w * (-r * g[k]);
+        mg += du[1 + k] * g[k];
+      }
+      s_acc[NV - 1] += w * (-mg);
+    }
+    const double iv = d.inv_vol[i];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.src[v * ld + i] = s_acc[v] * iv;
+  }
+}
+
+template <int NV, int ND>
+__device__ __forceinline__ void to_face(const double *u, const double *fr, int lde, int e, double *w) {
+  w[0] = u[0];
+  w[NV - 1] = u[NV - 1];
+#pragma unroll
+  for (int a = 0; a < ND; ++a) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) s += u[1 + k] * fr[(a * ND + k) * lde + e];
+    w[1 + a] = s;
+  }
+}
+
+template <int NV, int ND>
+__device__ __forceinline__ void from_face(double *f, const double *fr, int lde, int e) {
+  double m[ND];
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    double s = 0.0;
+#pragma unroll
+    for (int a = 0; a < ND; ++a) s += f[1 + a] * fr[(a * ND + k) * lde + e];
+    m[k] = s;
+  }
+#pragma unroll
+  for (int k = 0; k < ND; ++k) f[1 + k] = m[k];
+}
+
+template <class S, int FLUX>
+__global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params P, StageArgs a) {
+  constexpr int NV = S::NV, ND = S::ND;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= d.n_edges) return;
+  if (d.clock->done) return;
+  if (!d.factive[e]) return;
+  const int lde = d.lde, ld = d.ld;
+  const int L = d.fL[e], R = d.fR[e];
+  double nf[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) nf[v] = 0.0;
+  if (R >= 0) {
+    const int kL = d.fkL[e], kR = d.fkR[e];
+#pragma unroll
+    for (int qq = 0; qq < S::NQF; ++qq) {
+      double uL[NV], uR[NV], wL[NV], wR[NV];
+      const double *pL = a.fv + ((size_t)((kL * S::NQF + qq) * NV)) * ld + L;
+      const double *pR = a.fv + ((size_t)((kR * S::NQF + qq) * NV)) * ld + R;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        uL[v] = pL[(size_t)v * ld];
+        uR[v] = pR[(size_t)v * ld];
+      }
+      to_face<NV, ND>(uL, d.frame, lde, e, wL);
+      to_face<NV, ND>(uR, d.frame, lde, e, wR);
+      double f[NV];
+      if (FLUX == 0)
+        hllc_flux<NV>(wL, wR, P.gamma, f);
+      else
+        rusanov_flux<NV>(wL, wR, P.gamma, f);
+      const double w = d.fqw[qq * lde + e];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) nf[v] += w * f[v];
+    }
+    from_face<NV, ND>(nf, d.frame, lde, e);
+  } else if (P.flux_bc == 1) {
+    // FluxBC (boundary/flux_bc.hpp:25-42): physical flux of the cell average
+    double u[NV], w[NV], f[NV];
+    const int j = d.l2g[L];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) u[v] = a.q[v * ld + j];
+    to_face<NV, ND>(u, d.frame, lde, e, w);
+    euler_flux<NV>(w, pressure<NV>(w, P.gamma), f);
+    from_face<NV, ND>(f, d.frame, lde, e);
+    const double area = d.farea[e];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) nf[v] = area * f[v];
+  } else if (P.flux_bc == 2) {
+    // EquilibriumFluxBC (boundary/equilibrium_flux_bc.hpp:36-62): the equilibrium
+    // of the boundary cell extrapolated to the face; zero velocity, so F = p n.
+    const double found = a.eqth[2 * ld + L];
+    if (found != 0.0) {
+      EqEval ev{P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0)};
+      const double eh = a.eqth[L], eK = a.eqth[ld + L], phi_ref = d.phi_cq[L];
+      double pn = 0.0;
+#pragma unroll
+      for (int qq = 0; qq < S::NQF; ++qq) {
+        double r, E;
+        ev.at(eh, eK, phi_ref, d.phi_fq[qq * lde + e], r, E);
+        pn += d.fqw[qq * lde + e] * (E * ev.gm1);
+      }
+#pragma unroll
+      for (int k = 0; k < ND; ++k) nf[1 + k] = pn * d.frame[k * lde + e];
+    }
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) a.nf[v * lde + e] = nf[v];
+}
+
+template <int NV>
+__device__ __forceinline__ double cfl_candidate(const double *u, double gamma, double r) {
+  double m2 = 0.0;
+#pragma unroll
+  for (int k = 1; k < NV - 1; ++k) m2 += u[k] * u[k];
+  double v2 = m2 / (u[0] * u[0]);
+  double p = pressure<NV>(u, gamma);
+  double c = sqrt(gamma * p / u[0]);
+  return r / (sqrt(v2) + c);
+}
+
+__device__ __forceinline__ void block_min_to_clock(double cand, Clock *clock) {
+  // positive doubles order like their bit patterns; NaN bits sort above +inf
+  unsigned long long bits = __double_as_longlong(cand);
+  if (!(cand >= 0.0)) bits = 0x7ff0000000000000ull;  // ignored: status flags the state
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+    bits = other < bits ? other : bits;
+  }
+  __shared__ unsigned long long warp_min[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) warp_min[wid] = bits;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    bits = lane < nw ? warp_min[lane] : 0x7ff0000000000000ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long other = __shfl_xor_sync(0xffffffffu, bits, o);
+      bits = other < bits ? other : bits;
+    }
+    if (lane == 0) atomicMin(&clock->cfl_min, bits);
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(128) k_update(const DevData d, const Params P, StageArgs a) {
+  constexpr int NV = S::NV, NF = S::NF;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool last = a.stage == P.n_stages - 1;
+  double cand = INFINITY;
+  if (!d.clock->done && i < d.n_cells && (d.flags[i] & kInterior)) {
+    const int ld = d.ld, lde = d.lde;
+    double tend[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) tend[v] = 0.0;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const int cf = d.cface[f * ld + i];
+      if (cf < 0) continue;
+      const int e = cf >> 1;
+      const bool right = cf & 1;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const double x = a.nf[v * lde + e];
+        tend[v] += right ? x : -x;
+      }
+    }
+    const double iv = d.inv_vol[i];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) tend[v] *= iv;
+    if (a.src) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) tend[v] += a.src[v * ld + i];
+    }
+    if (a.tend_out) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) a.tend_out[v * ld + i] = tend[v];
+    } else {
+      const int s = a.stage;
+      const double dt = d.clock->dt;
+      const double *coef = last ? P.b : P.a[s + 1];
+      double un[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double dudt = 0.0;
+        for (int j = 0; j < s; ++j)
+          if (coef[j] != 0.0) dudt += coef[j] * a.k[j][v * ld + i];
+        if (coef[s] != 0.0) dudt += coef[s] * tend[v];
+        un[v] = a.u0[v * ld + i] + dt * dudt;
+      }
+      if (!last) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          a.k[s][v * ld + i] = tend[v];
+          a.ux[v * ld + i] = un[v];
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) a.u0[v * ld + i] = un[v];
+        cand = cfl_candidate<NV>(un, P.gamma, d.r_eff[i]);
+        bool finite = true;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) finite = finite && isfinite(un[v]);
+        if (!finite) set_status(d.clock, kStNonFinite);
+      }
+    }
+  }
+  if (last && !a.tend_out) block_min_to_clock(cand, d.clock);
+}
+
+template <class S>
+__global__ void __launch_bounds__(128) k_cfl(const DevData d, const Params P, const double *u) {
+  constexpr int NV = S::NV;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double cand = INFINITY;
+  if (i < d.n_cells && (d.flags[i] & kInterior)) {
+    double w[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) w[v] = u[v * d.ld + i];
+    cand = cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
+  }
+  block_min_to_clock(cand, d.clock);
+}
+
+// ------------------------------------------------------------ launching
+struct LaunchCfg {
+  int n_cells, n_edges;
+  bool eq, src;
+  int flux;
+  cudaStream_t stream;
+};
+
+// 2D CWENO-AO order 3: central 11 cells (A 10x5), three one-sided 4 cells (A 3x2)
+using S2o3 = Shape<2, 10, 5, 3, 3, 2, 2, 4>;
+// 2D order 2 ({2,2,2,2}, overfit {3,2,2,2}): central 7 (6x2), one-sided 5 (4x2)
+using S2o2 = Shape<2, 6, 2, 3, 4, 2, 2, 4>;
+// 3D order 3 (overfit {2,1.5,...}): central 19 (18x9), one-sided 5 (4x3);
+// degree-2 rules: 3 points per face, 4 per tetrahedron
+using S3o3 = Shape<3, 18, 9, 4, 4, 3, 3, 4>;
+// 3D order 2 (overfit {3,2,...}): central 10 (9x3), one-sided 7 (6x3)
+using S3o2 = Shape<3, 9, 3, 4, 6, 3, 3, 4>;
+
+template <class S>
+void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
+  const int nb = (c.n_cells + 127) / 128, nbe = (c.n_edges + 127) / 128;
+  if (c.eq && c.src)
+    k_reconstruct<S, 1, 1><<<nb, 128, 0, c.stream>>>(D, P, a);
+  else if (c.eq)
+    k_reconstruct<S, 1, 0><<<nb, 128, 0, c.stream>>>(D, P, a);
+  else if (c.src)
+    k_reconstruct<S, 0, 1><<<nb, 128, 0, c.stream>>>(D, P, a);
+  else
+    k_reconstruct<S, 0, 0><<<nb, 128, 0, c.stream>>>(D, P, a);
+  if (c.flux == 0)
+    k_face_flux<S, 0><<<nbe, 128, 0, c.stream>>>(D, P, a);
+  else
+    k_face_flux<S, 1><<<nbe, 128, 0, c.stream>>>(D, P, a);
+  k_update<S><<<nb, 128, 0, c.stream>>>(D, P, a);
+}
+
+template <class S>
+void launch_cfl_t(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) {
+  const int nb = (c.n_cells + 127) / 128;
+  k_cfl<S><<<nb, 128, 0, c.stream>>>(D, P, u);
+}
+
+#define ZFVM_DECLARE_SHAPE(name)                                                                  \
+  void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c); \
+  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c);
+#define ZFVM_DEFINE_SHAPE(name, S)                                                                \
+  void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) { \
+    launch_stage_t<S>(D, P, a, c);                                                                \
+  }                                                                                               \
+  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) { \
+    launch_cfl_t<S>(D, P, u, c);                                                                  \
+  }
+
+ZFVM_DECLARE_SHAPE(s2o3)
+ZFVM_DECLARE_SHAPE(s2o2)
+ZFVM_DECLARE_SHAPE(s3o3)
+ZFVM_DECLARE_SHAPE(s3o2)
+
+}  // namespace dev
+}  // namespace zfvm
