@@ -169,6 +169,11 @@ int zfvm_advance(zfvm_solver *s, int64_t n_steps, double t_end, double *t_out, i
  * the milliseconds measured with CUDA events on the solver's stream. */
 int zfvm_advance_timed(zfvm_solver *s, int64_t n_steps, float *ms);
 
+/* Average per-launch device time (ms) of the three stage kernels
+ * {reconstruct, face flux, update}, measured with CUDA events around every
+ * launch on the solver's stream over `n_steps` CFL steps (no graph). */
+int zfvm_kernel_times(zfvm_solver *s, int64_t n_steps, float *ms);
+
 /* Number of kernel launches one step issues. */
 int zfvm_launches_per_step(const zfvm_solver *s, int32_t *launches);
 

@@ -110,6 +110,7 @@ def load_library() -> C.CDLL:
         "zfvm_advance": [vp, i64, C.c_double, dp, C.POINTER(i64)],
         "zfvm_advance_timed": [vp, i64, C.POINTER(C.c_float)],
         "zfvm_launches_per_step": [vp, C.POINTER(i32)],
+        "zfvm_kernel_times": [vp, i64, C.POINTER(C.c_float)],
         "zfvm_device_bytes": [vp, C.POINTER(i64)],
     }
     for name, args in sig.items():
@@ -368,6 +369,12 @@ class Solver:
         ms = C.c_float()
         _check(load_library().zfvm_advance_timed(self._h, n_steps, C.byref(ms)))
         return float(ms.value)
+
+    def kernel_times(self, n_steps: int) -> dict:
+        """Average per-launch milliseconds of {reconstruct, face_flux, update}."""
+        ms = (C.c_float * 3)()
+        _check(load_library().zfvm_kernel_times(self._h, n_steps, ms))
+        return {"reconstruct": ms[0], "face_flux": ms[1], "update": ms[2]}
 
     def launches_per_step(self) -> int:
         n = C.c_int32()

@@ -156,11 +156,13 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
 }
 
 LaunchCfg launch_cfg(zfvm_solver *s) {
-  return LaunchCfg{s->n_cells, s->n_edges, s->has_eq, s->has_src, s->scheme.flux == ZFVM_FLUX_HLLC ? 0 : 1, s->stream};
+  return LaunchCfg{s->n_cells, s->n_edges, s->has_eq,   s->has_src,
+                   s->scheme.flux == ZFVM_FLUX_HLLC ? 0 : 1, s->stream, nullptr};
 }
 
-void dispatch_stage(zfvm_solver *s, StageArgs &a) {
+void dispatch_stage(zfvm_solver *s, StageArgs &a, cudaEvent_t *ev = nullptr) {
   LaunchCfg c = launch_cfg(s);
+  c.ev = ev;
   switch (s->shape_id) {
     case 0: launch_stage_s2o3(s->D, s->P, a, c); break;
     case 1: launch_stage_s2o2(s->D, s->P, a, c); break;
@@ -663,7 +665,7 @@ extern "C" int zfvm_advance(zfvm_solver *s, int64_t n_steps, double t_end, doubl
   if (n_steps <= 0 && !(t_end > 0.0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > 0");
   SOLVER_GUARD_BEGIN
   reset_clock_for_run(s, n_steps, t_end, 0.0);
-  const int chunk = 16;
+  const int chunk = n_steps > 0 ? (int)std::min<int64_t>(n_steps, 16) : 16;
   build_graph(s, chunk);
   int64_t launched = 0;
   while (true) {
@@ -728,4 +730,38 @@ extern "C" int zfvm_device_bytes(const zfvm_solver *s, int64_t *bytes) {
   if (!s || !bytes) return fail(ZFVM_EINVAL, "null argument");
   *bytes = s->device_bytes;
   return ZFVM_OK;
+}
+
+extern "C" int zfvm_kernel_times(zfvm_solver *s, int64_t n_steps, float *ms) {
+  if (!s || !ms || n_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  SOLVER_GUARD_BEGIN
+  reset_clock_for_run(s, n_steps, 0.0, 0.0);
+  const int S = s->P.n_stages;
+  std::vector<cudaEvent_t> ev((size_t)n_steps * S * 4);
+  for (auto &e : ev) CK(cudaEventCreate(&e));
+  for (int64_t k = 0; k < n_steps; ++k) {
+    k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 0);
+    for (int st = 0; st < S; ++st) {
+      StageArgs a = stage_args(s, st, nullptr);
+      dispatch_stage(s, a, &ev[((size_t)k * S + st) * 4]);
+    }
+  }
+  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
+  CK(cudaStreamSynchronize(s->stream));
+  double acc[3] = {0, 0, 0};
+  for (size_t b = 0; b < ev.size(); b += 4)
+    for (int j = 0; j < 3; ++j) {
+      float t;
+      CK(cudaEventElapsedTime(&t, ev[b + j], ev[b + j + 1]));
+      acc[j] += t;
+    }
+  const double launches = (double)n_steps * S;
+  for (int j = 0; j < 3; ++j) ms[j] = (float)(acc[j] / launches);
+  for (auto &e : ev) cudaEventDestroy(e);
+  Clock c = read_clock(s);
+  std::string msg;
+  int code = status_to_code(c.status, msg);
+  if (code) return fail(code, msg);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
 }

@@ -131,29 +131,41 @@ __device__ __forceinline__ void basis(const double *X, const double *C, double *
 // IdealGasEOS::rhoE(EnthalpyEntropy), ideal_gas_eos.hpp:162-168):
 //   h(x) = h_ref + phi_ref - phi(x),  rho = ((gamma-1)/gamma h / K)^(1/(gamma-1)),
 //   E = K rho^gamma / (gamma-1).
+// The reference evaluates `1.0 / K * (gamma - 1.0) / gamma * h` left to right, so
+// the factor in front of h depends on K only and is computed once per
+// equilibrium; the result is bit-identical.
 struct EqEval {
   double gamma, gm1, inv_gm1;
   __device__ __forceinline__ void at(double h_ref, double K, double phi_ref, double phi, double &rho,
                                      double &E) const {
-    double h = h_ref + phi_ref - phi;
-    double base = 1.0 / K * gm1 / gamma * h;
-    rho = powd(base, inv_gm1);
-    double p = K * powd(rho, gamma);
-    E = p / gm1;
+    Bound b = bind(h_ref, K, phi_ref);
+    b.at(*this, phi, rho, E);
+  }
+  struct Bound {
+    double hr, f, K;
+    __device__ __forceinline__ void at(const EqEval &ev, double phi, double &rho, double &E) const {
+      double h = hr - phi;
+      rho = powd(f * h, ev.inv_gm1);
+      double p = K * powd(rho, ev.gamma);
+      E = ev.gm1 == 1.0 ? p : p / ev.gm1;
+    }
+  };
+  __device__ __forceinline__ Bound bind(double h_ref, double K, double phi_ref) const {
+    return Bound{h_ref + phi_ref, 1.0 / K * gm1 / gamma, K};
   }
 };
 
 // Average of the equilibrium over a cell from its quadrature-point potentials.
 template <int NQC>
-__device__ __forceinline__ void eq_average(const EqEval &ev, const double *what, double h, double K,
-                                           double phi_ref, const double *phi, double &rb, double &Eb) {
+__device__ __forceinline__ void eq_average(const EqEval &ev, const double *what, const EqEval::Bound &b,
+                                           const double *phi, double &rb, double &Eb) {
   double r, e;
-  ev.at(h, K, phi_ref, phi[0], r, e);
+  b.at(ev, phi[0], r, e);
   rb = what[0] * r;
   Eb = what[0] * e;
 #pragma unroll
   for (int q = 1; q < NQC; ++q) {
-    ev.at(h, K, phi_ref, phi[q], r, e);
+    b.at(ev, phi[q], r, e);
     rb += what[q] * r;
     Eb += what[q] * e;
   }
@@ -171,11 +183,11 @@ __device__ int solve_equilibrium(const EqEval &ev, const double *what, const dou
   const double phi_ref = phi[0];
   const double p_g = E_bar * ev.gm1;
   const double h0 = gamma / ev.gm1 * p_g / rho_bar;
-  const double K0 = p_g / pow(rho_bar, gamma);
+  const double K0 = p_g / powd(rho_bar, gamma);
   const double atol0 = 1e-13 * h0, atol1 = 1e-13 * K0;
   auto f = [&](double h, double K, double &f0, double &f1) {
     double rb, Eb;
-    eq_average<NQC>(ev, what, h, K, phi_ref, phi, rb, Eb);
+    eq_average<NQC>(ev, what, ev.bind(h, K, phi_ref), phi, rb, Eb);
     f0 = rho_bar - rb;
     f1 = E_bar - Eb;
   };
@@ -276,6 +288,7 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
     a.eqth[ld + i] = eK;
     a.eqth[2 * ld + i] = found ? 1.0 : 0.0;
   }
+  const EqEval::Bound eqb = ev.bind(eh, eK, phi_ref);
   // deviation of a stencil cell from this cell's equilibrium
   auto load_dev = [&](int j, double *out) {
 #pragma unroll
@@ -285,7 +298,7 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
 #pragma unroll
       for (int qq = 0; qq < S::NQC; ++qq) phi_j[qq] = d.phi_cq[qq * ld + j];
       double rb, Eb;
-      eq_average<S::NQC>(ev, P.what_c, eh, eK, phi_ref, phi_j, rb, Eb);
+      eq_average<S::NQC>(ev, P.what_c, eqb, phi_j, rb, Eb);
       out[0] -= rb;
       out[NV - 1] -= Eb;
     }
@@ -431,7 +444,7 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
       delta_at(x, u);
       if (EQ && found) {
         double r, E;
-        ev.at(eh, eK, phi_ref, d.phi_fq[qq * d.lde + e], r, E);
+        eqb.at(ev, d.phi_fq[qq * d.lde + e], r, E);
         u[0] += r;
         u[NV - 1] += E;
         if (SRC) {
@@ -563,10 +576,11 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
       EqEval ev{P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0)};
       const double eh = a.eqth[L], eK = a.eqth[ld + L], phi_ref = d.phi_cq[L];
       double pn = 0.0;
+      const EqEval::Bound eqb = ev.bind(eh, eK, phi_ref);
 #pragma unroll
       for (int qq = 0; qq < S::NQF; ++qq) {
         double r, E;
-        ev.at(eh, eK, phi_ref, d.phi_fq[qq * lde + e], r, E);
+        eqb.at(ev, d.phi_fq[qq * lde + e], r, E);
         pn += d.fqw[qq * lde + e] * (E * ev.gm1);
       }
 #pragma unroll
@@ -699,6 +713,7 @@ struct LaunchCfg {
   bool eq, src;
   int flux;
   cudaStream_t stream;
+  cudaEvent_t *ev;  // optional: 4 events recorded around the three stage kernels
 };
 
 // 2D CWENO-AO order 3: central 11 cells (A 10x5), three one-sided 4 cells (A 3x2)
@@ -714,6 +729,7 @@ using S3o2 = Shape<3, 9, 3, 4, 6, 3, 3, 4>;
 template <class S>
 void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
   const int nb = (c.n_cells + 127) / 128, nbe = (c.n_edges + 127) / 128;
+  if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
     k_reconstruct<S, 1, 1><<<nb, 128, 0, c.stream>>>(D, P, a);
   else if (c.eq)
@@ -722,11 +738,14 @@ void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const Launc
     k_reconstruct<S, 0, 1><<<nb, 128, 0, c.stream>>>(D, P, a);
   else
     k_reconstruct<S, 0, 0><<<nb, 128, 0, c.stream>>>(D, P, a);
+  if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0)
     k_face_flux<S, 0><<<nbe, 128, 0, c.stream>>>(D, P, a);
   else
     k_face_flux<S, 1><<<nbe, 128, 0, c.stream>>>(D, P, a);
+  if (c.ev) cudaEventRecord(c.ev[2], c.stream);
   k_update<S><<<nb, 128, 0, c.stream>>>(D, P, a);
+  if (c.ev) cudaEventRecord(c.ev[3], c.stream);
 }
 
 template <class S>
