@@ -337,6 +337,32 @@ def main():
         "gpu_launches": solver.launches_per_step() * args.steps,
         "clocks": clk.summary(),
     }
+    if args.precision == "mixed":
+        # error of the mixed form against the FP64 form after the same steps
+        import dataclasses
+        from metrics import perturbation_rel_l1, state_rel_l1
+        s64 = z.Solver(mesh, dataclasses.replace(scheme, precision=z.FP64))
+        s64.set_state(u0)
+        s32 = z.Solver(mesh, scheme)
+        s32.set_state(u0)
+        n_cmp = min(args.steps, 100)
+        s64.advance(n_steps=n_cmp)
+        s32.advance(n_steps=n_cmp)
+        u64, _ = s64.get_state()
+        u32, _ = s32.get_state()
+        mask = raw.ghost == 0 if raw.ghost is not None else None
+        line["error_vs_fp64"] = {"steps": n_cmp, "state_rel_l1": state_rel_l1(u32, u64, mask),
+                                 "perturbation_rel_l1": perturbation_rel_l1(u32, u64, u0, mask)}
+        if scheme.equilibrium:
+            eq_raw, eq_mesh, eq_scheme, eq_u0, _ = workload(args.workload, args.precision)
+            u_eq = eq_mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=0.0)
+            s_eq = z.Solver(eq_mesh, eq_scheme)
+            s_eq.set_state(u_eq)
+            res = float(np.abs(s_eq.rate_of_change()).max())
+            s_eq.advance(n_steps=n_cmp)
+            u_end, _ = s_eq.get_state()
+            drift = float((np.abs(u_end - u_eq).max(axis=0) / np.abs(u_eq).max(axis=0))[[0, 4]].max())
+            line["well_balanced"] = {"max_abs_dudt": res, "rel_drift": drift, "steps": n_cmp}
     if rank == 0:
         try:
             line["cpu_baseline"] = cpu_baseline(raw, mesh, scheme, u0, desc)

@@ -13,3 +13,18 @@ def rel_errors(a: np.ndarray, ref: np.ndarray, mask=None, cols=(0, 1, 2, 4)):
         l1.append(d.sum() / s1 if s1 > 0 else d.sum())
         linf.append(d.max() / sinf if sinf > 0 else d.max())
     return max(l1), max(linf)
+
+
+def state_rel_l1(a: np.ndarray, ref: np.ndarray, mask=None, cols=(0, 1, 2, 3, 4)):
+    """||a - ref||_1 / ||ref||_1 over all cells and conserved variables."""
+    if mask is not None:
+        a, ref = a[mask], ref[mask]
+    c = list(cols)
+    return float(np.abs(a[:, c] - ref[:, c]).sum() / np.abs(ref[:, c]).sum())
+
+
+def perturbation_rel_l1(a: np.ndarray, ref: np.ndarray, base: np.ndarray, mask=None):
+    """Relative L1 error of the perturbation a - base against ref - base."""
+    if mask is not None:
+        a, ref, base = a[mask], ref[mask], base[mask]
+    return float(np.abs((a - base) - (ref - base)).sum() / np.abs(ref - base).sum())

@@ -1,0 +1,89 @@
+"""Mixed FP32/FP64 form against the FP64 form (and the oracle).
+
+Bars (north-star): relative L1 error of the conserved variables versus FP64
+<= 1e-6 after N steps; well-balanced residual on the unperturbed equilibrium
+<= 1e-10 (max |du/dt| and drift after N steps, relative).
+"""
+import numpy as np
+import pytest
+
+import zisafvm_gb300 as z
+from metrics import perturbation_rel_l1, rel_errors, state_rel_l1
+from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+
+pytestmark = pytest.mark.gpu
+
+TOL_MIXED = 1e-6
+TOL_WB = 1e-10
+
+
+def _pair(mesh, scheme, u0):
+    s64 = z.Solver(mesh, scheme)
+    sch32 = z.Scheme(**{**scheme.__dict__, "precision": z.MIXED})
+    s32 = z.Solver(mesh, sch32)
+    s64.set_state(u0)
+    s32.set_state(u0)
+    return s64, s32
+
+
+def test_mixed_c1_vortex(zlib):
+    raw, mesh, scheme, u0 = vortex_2d(n=160, halo=3)
+    s64, s32 = _pair(mesh, scheme, u0)
+    s64.advance(n_steps=100)
+    s32.advance(n_steps=100)
+    u64, t64 = s64.get_state()
+    u32, t32 = s32.get_state()
+    l1, linf = rel_errors(u32, u64, raw.ghost == 0)
+    print(f"mixed C1 100 steps: rel L1 {l1:.3e} rel Linf {linf:.3e}")
+    assert l1 < TOL_MIXED
+    assert abs(t32 - t64) < 1e-6 * t64
+
+
+def test_mixed_rate_of_change_matches_fp64(zlib):
+    raw, mesh, scheme, u0 = vortex_2d(n=32, halo=3, flux=z.FLUX_HLLC)
+    s64, s32 = _pair(mesh, scheme, u0)
+    t64, t32 = s64.rate_of_change(), s32.rate_of_change()
+    inner = raw.ghost == 0
+    err = np.abs(t32[inner] - t64[inner]).max(axis=0) / np.abs(t64[inner]).max(axis=0)
+    assert np.nanmax(err[[0, 1, 2, 4]]) < 1e-5, err
+
+
+def test_mixed_well_balanced(zlib):
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=40, amplitude=0.0, precision=z.MIXED)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t = s.rate_of_change()
+    res = np.abs(t).max()
+    print(f"mixed WB residual max|du/dt| = {res:.3e}")
+    assert res < TOL_WB
+    s.advance(n_steps=30)
+    u, _ = s.get_state()
+    drift = (np.abs(u - u0).max(axis=0) / np.abs(u0).max(axis=0))[[0, 4]].max()
+    print(f"mixed WB drift after 30 steps = {drift:.3e}")
+    assert drift < TOL_WB
+
+
+@pytest.mark.parametrize("amplitude", [1e-4, 1e-2])
+def test_mixed_polytrope_perturbation(zlib, amplitude):
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=60, amplitude=amplitude)
+    s64, s32 = _pair(mesh, scheme, u0)
+    s64.advance(n_steps=40)
+    s32.advance(n_steps=40)
+    u64, _ = s64.get_state()
+    u32, _ = s32.get_state()
+    l1 = state_rel_l1(u32, u64)
+    pert_err = perturbation_rel_l1(u32, u64, u0)
+    print(f"A={amplitude:g}: state rel L1 {l1:.3e}, perturbation rel L1 {pert_err:.3e}")
+    assert l1 < TOL_MIXED
+    assert pert_err < 1e-4
+
+
+def test_mixed_tets(zlib):
+    raw, mesh, scheme, u0 = vortex_tube_3d(n=8, order=3)
+    s64, s32 = _pair(mesh, scheme, u0)
+    s64.advance(n_steps=10)
+    s32.advance(n_steps=10)
+    u64, _ = s64.get_state()
+    u32, _ = s32.get_state()
+    l1, linf = rel_errors(u32, u64)
+    assert l1 < TOL_MIXED, (l1, linf)

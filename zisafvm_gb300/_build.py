@@ -80,5 +80,5 @@ def build(verbose: bool = False, force: bool = False) -> Path:
 
 
 if __name__ == "__main__":
-    build(verbose=True, force="--force" in sys.argv)
+    build(verbose="--verbose" in sys.argv, force="--force" in sys.argv)
     print(LIB)

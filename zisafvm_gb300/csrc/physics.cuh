@@ -109,3 +109,96 @@ __device__ __forceinline__ void rusanov_flux(const R *uL, const R *uR, R gamma, 
 
 }  // namespace dev
 }  // namespace zfvm
+
+namespace zfvm {
+namespace dev {
+
+// Perturbation form of the fluxes around a resting base state w = (rho_w, 0, E_w)
+// (an equilibrium at the face point).  Inputs are the deviations dL, dR of the
+// two face states from w; the output is F(w + dL, w + dR) - F(w), where
+// F(w) = (0, p_w, 0, 0) in the face frame.  The pressure is carried as
+// p_w + dp with dp = (gamma - 1)(dE - E_kin) and HLLC's c_K - 1 is formed
+// directly, so every small quantity keeps its own relative precision in FP32
+// and a vanishing perturbation gives an exactly vanishing result.
+template <int NV, class R>
+struct DevSide {
+  R rho, m[NV - 2], dE, E, dp, p, v, a, H;
+  __device__ __forceinline__ void set(const R *d, R rho_w, R E_w, R p_w, R gamma) {
+    rho = rho_w + d[0];
+    R m2 = R(0);
+#pragma unroll
+    for (int k = 0; k < NV - 2; ++k) {
+      m[k] = d[1 + k];
+      m2 += m[k] * m[k];
+    }
+    dE = d[NV - 1];
+    E = E_w + dE;
+    dp = (dE - R(0.5) * m2 / rho) * (gamma - R(1));
+    p = p_w + dp;
+    v = m[0] / rho;
+    a = sqrt(gamma * p / rho);
+    H = (E + p) / rho;
+  }
+  // F(u) - F(w) for this side
+  __device__ __forceinline__ void dflux(R *f) const {
+    f[0] = m[0];
+    f[1] = v * m[0] + dp;
+#pragma unroll
+    for (int k = 1; k < NV - 2; ++k) f[1 + k] = v * m[k];
+    f[NV - 1] = v * (E + p);
+  }
+};
+
+template <int NV, class R>
+__device__ __forceinline__ void hllc_flux_dev(const R *dL, const R *dR, R rho_w, R E_w, R gamma, R *df) {
+  const R p_w = E_w * (gamma - R(1));
+  DevSide<NV, R> L, Rr;
+  L.set(dL, rho_w, E_w, p_w, gamma);
+  Rr.set(dR, rho_w, E_w, p_w, gamma);
+  const R ratio = sqrt(Rr.rho / L.rho);
+  auto roe = [&](R a, R b) { return (a + b * ratio) / (R(1) + ratio); };
+  const R v_t = roe(L.v, Rr.v);
+  const R H_t = roe(L.H, Rr.H);
+  R vroe2 = R(0);
+#pragma unroll
+  for (int k = 0; k < NV - 2; ++k) {
+    R a = roe(L.m[k] / L.rho, Rr.m[k] / Rr.rho);
+    vroe2 += a * a;
+  }
+  const R a_t = sqrt((gamma - R(1)) * (H_t - R(0.5) * vroe2));
+  const R sL = fmin(L.v - L.a, v_t - a_t);
+  const R sR = fmax(Rr.v + Rr.a, v_t + a_t);
+  const R s_star = (Rr.m[0] * (sR - Rr.v) - L.m[0] * (sL - L.v) + (L.dp - Rr.dp)) /
+                   (Rr.rho * (sR - Rr.v) - L.rho * (sL - L.v));
+  const bool left = R(0) <= s_star;
+  const DevSide<NV, R> &K = left ? L : Rr;
+  K.dflux(df);
+  if (sL < R(0) && R(0) <= sR) {
+    const R sK = left ? sL : sR;
+    const R vK = K.v;
+    const R cm1 = (s_star - vK) / (sK - s_star);  // c_K - 1
+    const R cK = R(1) + cm1;
+    df[0] += sK * (cm1 * K.rho);
+    df[1] += sK * (cK * K.rho * s_star - K.m[0]);
+#pragma unroll
+    for (int k = 1; k < NV - 2; ++k) df[1 + k] += sK * (cm1 * K.m[k]);
+    df[NV - 1] += sK * (cm1 * K.E + cK * (s_star - vK) * (K.rho * s_star + K.p / (sK - vK)));
+  }
+}
+
+template <int NV, class R>
+__device__ __forceinline__ void rusanov_flux_dev(const R *dL, const R *dR, R rho_w, R E_w, R gamma, R *df) {
+  const R p_w = E_w * (gamma - R(1));
+  DevSide<NV, R> L, Rr;
+  L.set(dL, rho_w, E_w, p_w, gamma);
+  Rr.set(dR, rho_w, E_w, p_w, gamma);
+  const R smax = fmax(fabs(L.v) + L.a, fabs(Rr.v) + Rr.a);
+  R fL[NV], fR[NV];
+  L.dflux(fL);
+  Rr.dflux(fR);
+#pragma unroll
+  for (int k = 0; k < NV; ++k) df[k] = R(0.5) * (fL[k] + fR[k]) - R(0.5) * smax * (dR[k] - dL[k]);
+}
+
+}  // namespace dev
+}  // namespace zfvm

@@ -118,10 +118,11 @@ struct zfvm_solver {
   DBuf<uint8_t> flags, bloc, fkL, fkR, factive;
   DBuf<int> l2g, cface, fL, fR, src_map;
   DBuf<double> pinv, center, inv_len, mom, inv_vol, r_eff, fqx, fqw, frame, farea;
-  DBuf<double> phi_cq, gphi_cq, cqx, cqw, phi_fq;
-  DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos;
+  DBuf<float> pinv32, fv32;
+  DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
+  DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos, dev0;
   DBuf<Clock> clock;
-  bool has_src = false, has_eq = false;
+  bool has_src = false, has_eq = false, mixed = false;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   int64_t device_bytes = 0;
@@ -144,6 +145,8 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   StageArgs a{};
   a.q = stage == 0 ? s->u0.p : s->ux.p;
   a.fv = s->fv.p;
+  a.fv32 = s->fv32.p;
+  a.dev0 = s->dev0.p;
   a.nf = s->nfb.p;
   a.src = s->has_src ? s->srcb.p : nullptr;
   a.eqth = s->has_eq ? s->eqth.p : nullptr;
@@ -152,11 +155,13 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   for (int k = 0; k < 4; ++k) a.k[k] = s->kbuf.p ? s->kbuf.p + (size_t)k * s->nv * s->ld : nullptr;
   a.tend_out = tend_out;
   a.stage = stage;
+  const bool last = stage == s->P.n_stages - 1;
+  for (int j = 0; j < 4; ++j) a.coef[j] = last ? s->P.b[j] : (stage + 1 < 4 ? s->P.a[stage + 1][j] : 0.0);
   return a;
 }
 
 LaunchCfg launch_cfg(zfvm_solver *s) {
-  return LaunchCfg{s->n_cells, s->n_edges, s->has_eq,   s->has_src,
+  return LaunchCfg{s->n_cells, s->n_edges,  s->has_eq, s->has_src, s->mixed,
                    s->scheme.flux == ZFVM_FLUX_HLLC ? 0 : 1, s->stream, nullptr};
 }
 
@@ -270,6 +275,7 @@ int build_solver(zfvm_solver *s) {
   if (sc.steps_per_recompute != 1)
     return fail(ZFVM_EINVAL, "steps_per_recompute must be 1 (the equilibrium is refreshed every stage)");
   s->has_eq = sc.equilibrium == ZFVM_EQ_ISENTROPIC;
+  s->mixed = sc.precision == ZFVM_MIXED;
   s->has_src = sc.gravity != ZFVM_GRAVITY_NONE;
   if (s->has_eq && !s->has_src) return fail(ZFVM_EINVAL, "isentropic well-balancing needs gravity");
   if (sc.flux_bc == ZFVM_FLUX_BC_ISENTROPIC && !s->has_eq)
@@ -287,6 +293,7 @@ int build_solver(zfvm_solver *s) {
   P.nqf = s->nqf;
   P.flux_bc = sc.flux_bc;
   P.n_stages = sc.rk_stages;
+  P.gamma2 = sc.gamma == 2.0 ? 1 : 0;
   std::memset(P.a, 0, sizeof(P.a));
   std::memset(P.b, 0, sizeof(P.b));
   if (sc.rk_stages == 1) {
@@ -386,7 +393,7 @@ int build_solver(zfvm_solver *s) {
   }
   // ---- gravity potential at quadrature points (phi = g r or k r^2 / 2 radially)
   const int nqc = s->nqc;
-  std::vector<double> h_phi_cq, h_gphi_cq, h_cqx, h_cqw, h_phi_fq;
+  std::vector<double> h_phi_cq, h_phi_m1, h_phi_var, h_gphi_cq, h_cqx, h_cqw, h_phi_fq;
   if (s->has_src) {
     auto phi = [&](const Vec3 &x) {
       double r = norm(x);
@@ -399,6 +406,8 @@ int build_solver(zfvm_solver *s) {
       return dphi * (x[dir] / (r + 1e-50));
     };
     h_phi_cq.assign((size_t)nqc * ld, 0.0);
+    h_phi_m1.assign(ld, 0.0);
+    h_phi_var.assign(ld, 0.0);
     h_gphi_cq.assign((size_t)nqc * nd * ld, 0.0);
     h_cqx.assign((size_t)nqc * nd * ld, 0.0);
     h_cqw.assign((size_t)nqc * ld, 0.0);
@@ -413,6 +422,18 @@ int build_solver(zfvm_solver *s) {
           h_cqx[((size_t)q * nd + k) * ld + i] = x[k];
         }
       }
+    // <phi> and <(phi - <phi>)^2> with the reference-cell weights
+    for (index_t i = 0; i < n; ++i) {
+      double m1 = P.what_c[0] * h_phi_cq[i];
+      for (int q = 1; q < nqc; ++q) m1 += P.what_c[q] * h_phi_cq[(size_t)q * ld + i];
+      double var = 0.0;
+      for (int q = 0; q < nqc; ++q) {
+        double dphi = h_phi_cq[(size_t)q * ld + i] - m1;
+        var += P.what_c[q] * (dphi * dphi);
+      }
+      h_phi_m1[i] = m1;
+      h_phi_var[i] = var;
+    }
     for (index_t e = 0; e < g.n_edges; ++e)
       for (int q = 0; q < nqf; ++q) h_phi_fq[(size_t)q * lde + e] = phi(g.face_qx[e * nqf + q]);
   }
@@ -423,7 +444,7 @@ int build_solver(zfvm_solver *s) {
   s->l2g.upload(h_l2g);
   s->cface.upload(h_cface);
   s->src_map.upload(h_src);
-  s->pinv.upload(h_pinv);
+  if (!s->mixed) s->pinv.upload(h_pinv);
   s->center.upload(h_center);
   s->inv_len.upload(h_il);
   s->mom.upload(h_mom);
@@ -440,6 +461,8 @@ int build_solver(zfvm_solver *s) {
   s->farea.upload(h_farea);
   if (s->has_src) {
     s->phi_cq.upload(h_phi_cq);
+    s->phi_m1.upload(h_phi_m1);
+    s->phi_var.upload(h_phi_var);
     s->gphi_cq.upload(h_gphi_cq);
     s->cqx.upload(h_cqx);
     s->cqw.upload(h_cqw);
@@ -450,12 +473,20 @@ int build_solver(zfvm_solver *s) {
   s->u0.alloc((size_t)nv * ld);
   s->ux.alloc((size_t)nv * ld);
   s->kbuf.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
-  s->fv.alloc((size_t)nf * nqf * nv * ld);
+  if (s->mixed) {
+    std::vector<float> h32(h_pinv.begin(), h_pinv.end());
+    s->pinv32.upload(h32);
+    s->fv32.alloc((size_t)nf * nqf * nv * ld);
+    s->dev0.alloc((size_t)nv * ld);
+  } else {
+    s->fv.alloc((size_t)nf * nqf * nv * ld);
+  }
   s->nfb.alloc((size_t)nv * lde);
   s->tend.alloc((size_t)nv * ld);
   s->aos.alloc((size_t)5 * n);
   s->clock.alloc(1);
-  for (auto *b : {&s->u0, &s->ux, &s->kbuf, &s->fv, &s->nfb, &s->tend}) b->zero(s->stream);
+  for (auto *b : {&s->u0, &s->ux, &s->kbuf, &s->fv, &s->nfb, &s->tend, &s->dev0}) b->zero(s->stream);
+  s->fv32.zero(s->stream);
   if (s->has_src) s->srcb.zero(s->stream);
   if (s->has_eq) s->eqth.zero(s->stream);
   Clock c{};
@@ -471,6 +502,9 @@ int build_solver(zfvm_solver *s) {
   D.flags = s->flags.p;
   D.l2g = s->l2g.p;
   D.pinv = s->pinv.p;
+  D.pinv32 = s->pinv32.p;
+  D.phi_m1 = s->phi_m1.p;
+  D.phi_var = s->phi_var.p;
   D.bloc = s->bloc.p;
   D.center = s->center.p;
   D.inv_len = s->inv_len.p;
@@ -498,7 +532,8 @@ int build_solver(zfvm_solver *s) {
   auto add = [&](size_t nbytes) { bytes += (int64_t)nbytes; };
   add(s->flags.n + s->bloc.n + s->fkL.n + s->fkR.n + s->factive.n);
   add(4 * (s->l2g.n + s->cface.n + s->fL.n + s->fR.n + s->src_map.n));
-  add(8 * (s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
+  add(4 * (s->pinv32.n + s->fv32.n));
+  add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
            s->ux.n + s->kbuf.n + s->fv.n + s->nfb.n + s->srcb.n + s->eqth.n + s->tend.n + s->aos.n));
   s->device_bytes = bytes;
@@ -552,7 +587,7 @@ void build_graph(zfvm_solver *s, int steps) {
 
 extern "C" int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *sc, zfvm_solver **out) {
   if (!m || !sc || !out) return fail(ZFVM_EINVAL, "null argument");
-  if (sc->precision != ZFVM_FP64) return fail(ZFVM_EINVAL, "precision not available in this build");
+  if (sc->precision != ZFVM_FP64 && sc->precision != ZFVM_MIXED) return fail(ZFVM_EINVAL, "unknown precision");
   if (!(sc->gamma > 1.0) || !(sc->cfl_number > 0.0)) return fail(ZFVM_EINVAL, "bad gamma or cfl_number");
   auto s = std::make_unique<zfvm_solver>();
   s->mesh = m;

@@ -20,10 +20,23 @@
 // are reconstructed unscaled and the EulerScaling enters only the smoothness
 // indicators, and the face-flux scatter is a deterministic cell-centric gather
 // instead of OpenMP atomics.
+//
+// Two precisions share the kernels (template flag MIXED):
+//   FP64   everything in double.
+//   MIXED  the cell averages, the equilibrium (Newton solve, equilibrium
+//          averages and point values), the RK accumulation and the CFL time
+//          step stay FP64; the reconstruction of the deviation from the
+//          equilibrium, the smoothness indicators / nonlinear weights and the
+//          numerical flux run in FP32.  The flux is computed in deviation form
+//          around the left cell's FP64 face state w:
+//            F = F64(w) + [F32(w + dL, w + dR) - F32(w)],
+//          which is exact in exact arithmetic (both fluxes are consistent) and
+//          gives an exactly zero FP32 part on an unperturbed equilibrium.
 #pragma once
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <type_traits>
 
 #include "grid.hpp"
 #include "physics.cuh"
@@ -46,6 +59,7 @@ struct DevData {
   const uint8_t *flags;
   const int *l2g;        // [MAXL][ld] through the periodic source map
   const double *pinv;    // [NP][ld]
+  const float *pinv32;   // [NP][ld] (mixed precision)
   const uint8_t *bloc;   // [NB*RB][ld]
   const double *center;  // [ND][ld]
   const double *inv_len; // [ld]
@@ -60,7 +74,9 @@ struct DevData {
   const double *frame;   // [ND*ND][lde]: normal, tangent 1 (, tangent 2)
   const double *farea;   // [lde]
   // equilibrium / gravity
-  const double *phi_cq;  // [NQC][ld]
+  const double *phi_cq;  // [NQC][ld] potential at the cell quadrature points
+  const double *phi_m1;  // [ld] quadrature average of phi over the cell
+  const double *phi_var; // [ld] quadrature average of (phi - phi_m1)^2
   const double *gphi_cq; // [NQC][ND][ld]
   const double *cqx;     // [NQC][ND][ld]
   const double *cqw;     // [NQC][ld]
@@ -78,12 +94,15 @@ struct Params {
   int nqc, nqf;
   int flux_bc;       // 0 none, 1 constant, 2 isentropic
   int n_stages;
+  int gamma2;        // gamma == 2: closed-form equilibrium cell averages
   double a[4][4], b[4];
 };
 
 struct StageArgs {
   const double *q;   // stage state
-  double *fv;        // face values [NF*NQF*NV][ld]
+  double *fv;        // FP64: face values [NF*NQF*NV][ld]
+  float *fv32;       // MIXED: polynomial part at the face points [NF*NQF*NV][ld]
+  double *dev0;      // MIXED: cell-average deviation of every cell [NV][ld]
   double *nf;        // face fluxes [NV][lde]
   double *src;       // per-cell source [NV][ld]
   double *eqth;      // per-cell equilibrium (h, K, found) [3][ld]
@@ -91,6 +110,7 @@ struct StageArgs {
   double *ux;        // next stage state
   double *k[4];      // stage tendencies
   double *tend_out;  // when non-null: write the tendency and do no RK update
+  double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
   int stage;
 };
 
@@ -112,16 +132,16 @@ __device__ __forceinline__ double powd(double x, double y) {
 
 // Non-constant monomials of the scaled offset X in poly_index order
 // (math/poly2d_impl.hpp:176-183), minus the normalized moments.
-template <int ND, int NC>
-__device__ __forceinline__ void basis(const double *X, const double *C, double *phi) {
+template <int ND, int NC, class R>
+__device__ __forceinline__ void basis(const R *X, const R *C, R *phi) {
   if (ND == 2) {
-    const double x = X[0], y = X[1];
-    double m[5] = {x, y, x * x, x * y, y * y};
+    const R x = X[0], y = X[1];
+    R m[5] = {x, y, x * x, x * y, y * y};
 #pragma unroll
     for (int c = 0; c < NC; ++c) phi[c] = m[c] - C[c];
   } else {
-    const double x = X[0], y = X[1], z = X[2];
-    double m[9] = {x, y, z, x * x, x * y, x * z, y * y, y * z, z * z};
+    const R x = X[0], y = X[1], z = X[2];
+    R m[9] = {x, y, z, x * x, x * y, x * z, y * y, y * z, z * z};
 #pragma unroll
     for (int c = 0; c < NC; ++c) phi[c] = m[c] - C[c];
   }
@@ -136,11 +156,6 @@ __device__ __forceinline__ void basis(const double *X, const double *C, double *
 // equilibrium; the result is bit-identical.
 struct EqEval {
   double gamma, gm1, inv_gm1;
-  __device__ __forceinline__ void at(double h_ref, double K, double phi_ref, double phi, double &rho,
-                                     double &E) const {
-    Bound b = bind(h_ref, K, phi_ref);
-    b.at(*this, phi, rho, E);
-  }
   struct Bound {
     double hr, f, K;
     __device__ __forceinline__ void at(const EqEval &ev, double phi, double &rho, double &E) const {
@@ -155,19 +170,29 @@ struct EqEval {
   }
 };
 
-// Average of the equilibrium over a cell from its quadrature-point potentials.
+// Quadrature average of the equilibrium over a cell.  For gamma = 2 the
+// density is linear and the energy quadratic in phi, so the average follows
+// exactly from the cell's <phi> and <(phi - <phi>)^2>:
+//   rho_bar = f (h_r - <phi>),  E_bar = K f^2 ((h_r - <phi>)^2 + var phi).
+// Otherwise the quadrature-point sum is evaluated.
 template <int NQC>
-__device__ __forceinline__ void eq_average(const EqEval &ev, const double *what, const EqEval::Bound &b,
-                                           const double *phi, double &rb, double &Eb) {
+__device__ __forceinline__ void eq_cell_average(const EqEval &ev, const Params &P, const DevData &d,
+                                                const EqEval::Bound &b, int j, double &rb, double &Eb) {
+  if (P.gamma2) {
+    const double t = b.hr - d.phi_m1[j];
+    rb = b.f * t;
+    Eb = b.K * (b.f * b.f) * (t * t + d.phi_var[j]);
+    return;
+  }
   double r, e;
-  b.at(ev, phi[0], r, e);
-  rb = what[0] * r;
-  Eb = what[0] * e;
+  b.at(ev, d.phi_cq[j], r, e);
+  rb = P.what_c[0] * r;
+  Eb = P.what_c[0] * e;
 #pragma unroll
   for (int q = 1; q < NQC; ++q) {
-    b.at(ev, phi[q], r, e);
-    rb += what[q] * r;
-    Eb += what[q] * e;
+    b.at(ev, d.phi_cq[q * d.ld + j], r, e);
+    rb += P.what_c[q] * r;
+    Eb += P.what_c[q] * e;
   }
 }
 
@@ -177,17 +202,16 @@ __device__ __forceinline__ void eq_average(const EqEval &ev, const double *what,
 // equilibrium was found, 1 when it was not (the reference then extrapolates
 // zeros), 2 when the iteration diverged (the reference aborts).
 template <int NQC>
-__device__ int solve_equilibrium(const EqEval &ev, const double *what, const double *phi, double rho_bar,
-                                 double E_bar, double &h_out, double &K_out) {
+__device__ int solve_equilibrium(const EqEval &ev, const Params &P, const DevData &d, int i, double phi_ref,
+                                 double rho_bar, double E_bar, double &h_out, double &K_out) {
   const double gamma = ev.gamma;
-  const double phi_ref = phi[0];
   const double p_g = E_bar * ev.gm1;
   const double h0 = gamma / ev.gm1 * p_g / rho_bar;
   const double K0 = p_g / powd(rho_bar, gamma);
   const double atol0 = 1e-13 * h0, atol1 = 1e-13 * K0;
   auto f = [&](double h, double K, double &f0, double &f1) {
     double rb, Eb;
-    eq_average<NQC>(ev, what, ev.bind(h, K, phi_ref), phi, rb, Eb);
+    eq_cell_average<NQC>(ev, P, d, ev.bind(h, K, phi_ref), i, rb, Eb);
     f0 = rho_bar - rb;
     f1 = E_bar - Eb;
   };
@@ -195,7 +219,6 @@ __device__ int solve_equilibrium(const EqEval &ev, const double *what, const dou
   f(x0, x1, fx0, fx1);
   double dx0 = 2.0 * atol0 + 1.0, dx1 = 2.0 * atol1 + 1.0;
   double hist0[3] = {0, 0, 0}, hist1[3] = {0, 0, 0};
-  int n_hist = 0;
   int iter = 0;
   while (!(fabs(dx0) <= atol0 && fabs(dx1) <= atol1) && iter < 20) {
     double eps0 = 1e-6 * fabs(x0), eps1 = 1e-6 * fabs(x1);
@@ -214,7 +237,6 @@ __device__ int solve_equilibrium(const EqEval &ev, const double *what, const dou
     f(x0, x1, fx0, fx1);
     hist0[0] = hist0[1], hist0[1] = hist0[2], hist0[2] = dx0;
     hist1[0] = hist1[1], hist1[1] = hist1[2], hist1[2] = dx1;
-    ++n_hist;
     if (iter >= 4) {
       bool conv = (hist0[2] <= atol0) && (hist1[2] <= atol1);
       if (!conv) {
@@ -241,9 +263,10 @@ __device__ int solve_equilibrium(const EqEval &ev, const double *what, const dou
 
 __device__ __forceinline__ void set_status(Clock *c, int bits) { atomicOr(&c->status, bits); }
 
-// --------------------------------------------------------------- kernels
-template <class S, int EQ, int SRC>
+// --------------------------------------------------------- reconstruction
+template <class S, int EQ, int SRC, bool MIXED>
 __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Params P, StageArgs a) {
+  using R = std::conditional_t<MIXED, float, double>;
   constexpr int NV = S::NV, ND = S::ND, NF = S::NF, NC = S::NC;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n_cells) return;
@@ -267,21 +290,38 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
   }
   // EulerScaling (model/characteristic_scale.hpp:23-32): {rho, c, c, c, E_int}
   const double cs = sqrt(gamma * (eint * (gamma - 1.0)) / rho);
-  double inv_s2[NV];
-  inv_s2[0] = 1.0 / (rho * rho);
+  R inv_s2[NV];
+  inv_s2[0] = R(1.0 / (rho * rho));
 #pragma unroll
-  for (int v = 1; v < NV - 1; ++v) inv_s2[v] = 1.0 / (cs * cs);
-  inv_s2[NV - 1] = 1.0 / (eint * eint);
+  for (int v = 1; v < NV - 1; ++v) inv_s2[v] = R(1.0 / (cs * cs));
+  inv_s2[NV - 1] = R(1.0 / (eint * eint));
 
   // local equilibrium of this cell from its own average
   double eh = 0.0, eK = 0.0, phi_ref = 0.0;
   bool found = false;
-  double phi_own[S::NQC];
-  if (EQ) {
-#pragma unroll
-    for (int qq = 0; qq < S::NQC; ++qq) phi_own[qq] = d.phi_cq[qq * ld + i];
-    phi_ref = phi_own[0];
-    int st = solve_equilibrium<S::NQC>(ev, P.what_c, phi_own, rho, eint, eh, eK);
+  // closed form for gamma = 2 (mixed form): the cell average of the
+  // equilibrium is rho_bar = T / (2K), E_bar = (T^2 + var phi) / (4K) with
+  // T = h_r - <phi>, so K = (E_bar + sqrt(E_bar^2 - rho_bar^2 var)) / (2 rho_bar^2)
+  // and T = 2 K rho_bar: the exact root the FP64 form's Newton iteration
+  // converges to within its tolerance.
+  bool closed = false;
+  if (EQ && MIXED && P.gamma2) {
+    phi_ref = d.phi_cq[i];
+    const double m1 = d.phi_m1[i], var = d.phi_var[i];
+    const double disc = eint * eint - rho * rho * var;
+    if (disc >= 0.0) {
+      eK = (eint + sqrt(disc)) / (2.0 * rho * rho);
+      eh = 2.0 * eK * rho + m1 - phi_ref;
+      found = eK > 0.0;
+      closed = true;
+      a.eqth[i] = eh;
+      a.eqth[ld + i] = eK;
+      a.eqth[2 * ld + i] = found ? 1.0 : 0.0;
+    }
+  }
+  if (EQ && !closed) {
+    phi_ref = d.phi_cq[i];
+    int st = solve_equilibrium<S::NQC>(ev, P, d, i, phi_ref, rho, eint, eh, eK);
     found = st == 0;
     if (st == 2) set_status(d.clock, kStNewton);
     a.eqth[i] = eh;
@@ -289,16 +329,13 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
     a.eqth[2 * ld + i] = found ? 1.0 : 0.0;
   }
   const EqEval::Bound eqb = ev.bind(eh, eK, phi_ref);
-  // deviation of a stencil cell from this cell's equilibrium
+  // deviation of a stencil cell's average from this cell's equilibrium (FP64)
   auto load_dev = [&](int j, double *out) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) out[v] = q[v * ld + j];
     if (EQ && found) {
-      double phi_j[S::NQC];
-#pragma unroll
-      for (int qq = 0; qq < S::NQC; ++qq) phi_j[qq] = d.phi_cq[qq * ld + j];
       double rb, Eb;
-      eq_average<S::NQC>(ev, P.what_c, eqb, phi_j, rb, Eb);
+      eq_cell_average<S::NQC>(ev, P, d, eqb, j, rb, Eb);
       out[0] -= rb;
       out[NV - 1] -= Eb;
     }
@@ -311,43 +348,69 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
 #pragma unroll
     for (int v = 0; v < NV; ++v) dev0[v] = u0[v];
   }
+  if (MIXED) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.dev0[v * ld + i] = dev0[v];
+  }
+  // dev_j - dev_0 for a stencil cell j.  In the mixed form with gamma = 2 the
+  // equilibrium averages are differenced analytically,
+  //   d rho = (q_j - q_0) - f (<phi>_0 - <phi>_j),
+  //   d E   = (q_j - q_0) - K f^2 ((<phi>_0 - <phi>_j)(2 h_r - <phi>_j - <phi>_0) + var_j - var_0),
+  // so the O(h) equilibrium variation never cancels against the O(h) state
+  // variation in floating point.
+  const bool diff_form = MIXED && EQ && found && P.gamma2;
+  auto row_diff = [&](int j, R *dq) {
+    if (diff_form) {
+      const double m1_0 = d.phi_m1[j0], m1_j = d.phi_m1[j];
+      const double dm = m1_0 - m1_j;
+      double qd[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) qd[v] = q[v * ld + j] - u0[v];
+      qd[0] -= eqb.f * dm;
+      qd[NV - 1] -= eqb.K * (eqb.f * eqb.f) * (dm * (2.0 * eqb.hr - m1_j - m1_0) + (d.phi_var[j] - d.phi_var[j0]));
+#pragma unroll
+      for (int v = 0; v < NV; ++v) dq[v] = R(qd[v]);
+    } else {
+      double dq64[NV];
+      load_dev(j, dq64);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) dq[v] = R(dq64[v] - dev0[v]);
+    }
+  };
 
   // LSQ fits: coefficients 1..C of every stencil, unscaled
-  double b0[S::C0][NV];
+  R b0[S::C0][NV];
 #pragma unroll
   for (int c = 0; c < S::C0; ++c)
 #pragma unroll
-    for (int v = 0; v < NV; ++v) b0[c][v] = 0.0;
+    for (int v = 0; v < NV; ++v) b0[c][v] = R(0);
 #pragma unroll 2
   for (int r = 0; r < S::R0; ++r) {
-    double dq[NV];
-    load_dev(d.l2g[(r + 1) * ld + i], dq);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) dq[v] -= dev0[v];
+    R dq[NV];
+    row_diff(d.l2g[(r + 1) * ld + i], dq);
 #pragma unroll
     for (int c = 0; c < S::C0; ++c) {
-      const double pc = d.pinv[(c * S::R0 + r) * ld + i];
+      const R pc = MIXED ? R(d.pinv32[(c * S::R0 + r) * ld + i]) : R(d.pinv[(c * S::R0 + r) * ld + i]);
 #pragma unroll
       for (int v = 0; v < NV; ++v) b0[c][v] += pc * dq[v];
     }
   }
-  double bb[S::NB][S::CB][NV];
+  R bb[S::NB][S::CB][NV];
 #pragma unroll
   for (int k = 0; k < S::NB; ++k) {
 #pragma unroll
     for (int c = 0; c < S::CB; ++c)
 #pragma unroll
-      for (int v = 0; v < NV; ++v) bb[k][c][v] = 0.0;
+      for (int v = 0; v < NV; ++v) bb[k][c][v] = R(0);
 #pragma unroll
     for (int r = 0; r < S::RB; ++r) {
       const int l = d.bloc[(k * S::RB + r) * ld + i];
-      double dq[NV];
-      load_dev(d.l2g[l * ld + i], dq);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) dq[v] -= dev0[v];
+      R dq[NV];
+      row_diff(d.l2g[l * ld + i], dq);
 #pragma unroll
       for (int c = 0; c < S::CB; ++c) {
-        const double pc = d.pinv[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i];
+        const int pi = (S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i;
+        const R pc = MIXED ? R(d.pinv32[pi]) : R(d.pinv[pi]);
 #pragma unroll
         for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
       }
@@ -355,48 +418,48 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
   }
 
   // CWENO-AO: p_c = (p_opt - sum_k g_k p_k) / g_c   (cweno_ao.cpp:35-53)
-  double pf[NC][NV];
+  R pf[NC][NV];
 #pragma unroll
   for (int c = 0; c < NC; ++c)
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      double x = c < S::C0 ? b0[c][v] : 0.0;
+      R x = c < S::C0 ? b0[c][v] : R(0);
 #pragma unroll
       for (int k = 0; k < S::NB; ++k)
-        if (c < S::CB) x -= P.lw[k + 1] * bb[k][c][v];
-      pf[c][v] = x * P.inv_lw0;
+        if (c < S::CB) x -= R(P.lw[k + 1]) * bb[k][c][v];
+      pf[c][v] = x * R(P.inv_lw0);
     }
   // smoothness indicators in the scaled variables (poly2d_impl.hpp:325-337)
   auto indicator = [&](auto coef, int ncoef) {
-    double m = 0.0;
+    R m = R(0);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      double s = 0.0;
+      R s = R(0);
       for (int c = 0; c < ncoef; ++c) s += coef(c, v) * coef(c, v);
       m = fmax(m, s * inv_s2[v]);
     }
     return m;
   };
-  double alpha[S::NB + 1];
-  auto weight = [&](double IS, double g) {
-    double pw = P.exponent == 4.0 ? (IS * IS) * (IS * IS) : pow(IS, P.exponent);
-    return g / (P.epsilon + pw);
+  R alpha[S::NB + 1];
+  auto weight = [&](R IS, double g) {
+    R pw = P.exponent == 4.0 ? (IS * IS) * (IS * IS) : R(pow(double(IS), P.exponent));
+    return R(g) / (R(P.epsilon) + pw);
   };
   alpha[0] = weight(indicator([&](int c, int v) { return pf[c][v]; }, S::C0), P.lw[0]);
 #pragma unroll
   for (int k = 0; k < S::NB; ++k)
     alpha[k + 1] = weight(indicator([&](int c, int v) { return bb[k][c][v]; }, S::CB), P.lw[k + 1]);
-  double al_tot = 0.0;
+  R al_tot = R(0);
 #pragma unroll
   for (int k = 0; k <= S::NB; ++k) al_tot += alpha[k];
   // eno_hybridize (hybrid_weno.cpp:109-128)
   {
-    const double w0 = alpha[0] / al_tot;
+    const R w0 = alpha[0] / al_tot;
 #pragma unroll
     for (int c = 0; c < NC; ++c)
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        double x = w0 * pf[c][v];
+        R x = w0 * pf[c][v];
 #pragma unroll
         for (int k = 0; k < S::NB; ++k)
           if (c < S::CB) x += (alpha[k + 1] / al_tot) * bb[k][c][v];
@@ -404,23 +467,25 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
       }
   }
 
-  double xc[ND], C[NC];
+  double xc[ND];
+  R C[NC];
 #pragma unroll
   for (int k = 0; k < ND; ++k) xc[k] = d.center[k * ld + i];
   const double il = d.inv_len[i];
 #pragma unroll
-  for (int c = 0; c < NC; ++c) C[c] = d.mom[c * ld + i];
-  auto delta_at = [&](const double *x, double *du) {
-    double X[ND], phi[NC];
+  for (int c = 0; c < NC; ++c) C[c] = R(d.mom[c * ld + i]);
+  // non-constant part of the limited polynomial at x
+  auto poly_at = [&](const double *x, R *pv) {
+    R X[ND], phi[NC];
 #pragma unroll
-    for (int k = 0; k < ND; ++k) X[k] = (x[k] - xc[k]) * il;
+    for (int k = 0; k < ND; ++k) X[k] = R((x[k] - xc[k]) * il);
     basis<ND, NC>(X, C, phi);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      double s = dev0[v];
+      R s = R(0);
 #pragma unroll
       for (int c = 0; c < NC; ++c) s += pf[c][v] * phi[c];
-      du[v] = s;
+      pv[v] = s;
     }
   };
 
@@ -440,24 +505,32 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
       double x[ND];
 #pragma unroll
       for (int k = 0; k < ND; ++k) x[k] = d.fqx[(qq * ND + k) * d.lde + e];
-      double u[NV];
-      delta_at(x, u);
+      R pv[NV];
+      poly_at(x, pv);
+      double r_eq = 0.0, E_eq = 0.0;
       if (EQ && found) {
-        double r, E;
-        eqb.at(ev, d.phi_fq[qq * d.lde + e], r, E);
-        u[0] += r;
-        u[NV - 1] += E;
+        eqb.at(ev, d.phi_fq[qq * d.lde + e], r_eq, E_eq);
         if (SRC) {
           // surface part of the well-balanced source: p_eq n_out
-          const double p_eq = E * ev.gm1;
+          const double p_eq = E_eq * ev.gm1;
           const double w = d.fqw[qq * d.lde + e];
 #pragma unroll
           for (int k = 0; k < ND; ++k) s_acc[1 + k] += w * (p_eq * sgn * d.frame[k * d.lde + e]);
         }
       }
-      double *out = a.fv + ((size_t)((f * S::NQF + qq) * NV)) * ld + i;
+      const size_t slot = (size_t)((f * S::NQF + qq) * NV) * ld + i;
+      if (MIXED) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) out[(size_t)v * ld] = u[v];
+        for (int v = 0; v < NV; ++v) a.fv32[slot + (size_t)v * ld] = float(pv[v]);
+      } else {
+        double u[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) u[v] = dev0[v] + double(pv[v]);
+        u[0] += r_eq;
+        u[NV - 1] += E_eq;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) a.fv[slot + (size_t)v * ld] = u[v];
+      }
     }
   }
 
@@ -472,12 +545,12 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
         x[k] = d.cqx[(qq * ND + k) * ld + i];
         g[k] = d.gphi_cq[(qq * ND + k) * ld + i];
       }
+      R pv[NV];
+      poly_at(x, pv);
       double du[NV];
-      delta_at(x, du);
-      double r = du[0];
-      if (EQ && found) {
-        // du already is the deviation; its density is the source density
-      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) du[v] = dev0[v] + double(pv[v]);
+      const double r = du[0];
       const double w = d.cqw[qq * ld + i];
       double mg = 0.0;
 #pragma unroll
@@ -493,15 +566,16 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
   }
 }
 
-template <int NV, int ND>
-__device__ __forceinline__ void to_face(const double *u, const double *fr, int lde, int e, double *w) {
+// ------------------------------------------------------------- face flux
+template <int NV, int ND, class T>
+__device__ __forceinline__ void to_face(const T *u, const double *fr, int lde, int e, T *w) {
   w[0] = u[0];
   w[NV - 1] = u[NV - 1];
 #pragma unroll
   for (int a = 0; a < ND; ++a) {
-    double s = 0.0;
+    T s = T(0);
 #pragma unroll
-    for (int k = 0; k < ND; ++k) s += u[1 + k] * fr[(a * ND + k) * lde + e];
+    for (int k = 0; k < ND; ++k) s += u[1 + k] * T(fr[(a * ND + k) * lde + e]);
     w[1 + a] = s;
   }
 }
@@ -520,7 +594,32 @@ __device__ __forceinline__ void from_face(double *f, const double *fr, int lde, 
   for (int k = 0; k < ND; ++k) f[1 + k] = m[k];
 }
 
-template <class S, int FLUX>
+template <int NV, int FLUX, class T>
+__device__ __forceinline__ void numerical_flux(const T *uL, const T *uR, T gamma, T *f) {
+  if (FLUX == 0)
+    hllc_flux<NV>(uL, uR, gamma, f);
+  else
+    rusanov_flux<NV>(uL, uR, gamma, f);
+}
+
+// Face state of one side in the MIXED form: FP64 base (cell-average deviation
+// plus the equilibrium at the point) and the FP32 polynomial part.
+template <class S, int EQ>
+__device__ __forceinline__ void mixed_base(const DevData &d, const StageArgs &a, const EqEval &ev, int c, double phi,
+                                           double *base) {
+  const int ld = d.ld;
+#pragma unroll
+  for (int v = 0; v < S::NV; ++v) base[v] = a.dev0[v * ld + c];
+  if (EQ && a.eqth[2 * ld + c] != 0.0) {
+    const EqEval::Bound b = ev.bind(a.eqth[c], a.eqth[ld + c], d.phi_cq[c]);
+    double r, E;
+    b.at(ev, phi, r, E);
+    base[0] += r;
+    base[S::NV - 1] += E;
+  }
+}
+
+template <class S, int FLUX, int EQ, bool MIXED>
 __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params P, StageArgs a) {
   constexpr int NV = S::NV, ND = S::ND;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -529,6 +628,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
   if (!d.factive[e]) return;
   const int lde = d.lde, ld = d.ld;
   const int L = d.fL[e], R = d.fR[e];
+  EqEval ev{P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0)};
   double nf[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) nf[v] = 0.0;
@@ -536,24 +636,87 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
     const int kL = d.fkL[e], kR = d.fkR[e];
 #pragma unroll
     for (int qq = 0; qq < S::NQF; ++qq) {
-      double uL[NV], uR[NV], wL[NV], wR[NV];
-      const double *pL = a.fv + ((size_t)((kL * S::NQF + qq) * NV)) * ld + L;
-      const double *pR = a.fv + ((size_t)((kR * S::NQF + qq) * NV)) * ld + R;
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        uL[v] = pL[(size_t)v * ld];
-        uR[v] = pR[(size_t)v * ld];
-      }
-      to_face<NV, ND>(uL, d.frame, lde, e, wL);
-      to_face<NV, ND>(uR, d.frame, lde, e, wR);
+      const size_t sL = (size_t)((kL * S::NQF + qq) * NV) * ld + L;
+      const size_t sR = (size_t)((kR * S::NQF + qq) * NV) * ld + R;
       double f[NV];
-      if (FLUX == 0)
-        hllc_flux<NV>(wL, wR, P.gamma, f);
-      else
-        rusanov_flux<NV>(wL, wR, P.gamma, f);
-      const double w = d.fqw[qq * lde + e];
+      if (!MIXED) {
+        double uL[NV], uR[NV], wL[NV], wR[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) nf[v] += w * f[v];
+        for (int v = 0; v < NV; ++v) {
+          uL[v] = a.fv[sL + (size_t)v * ld];
+          uR[v] = a.fv[sR + (size_t)v * ld];
+        }
+        to_face<NV, ND>(uL, d.frame, lde, e, wL);
+        to_face<NV, ND>(uR, d.frame, lde, e, wR);
+        numerical_flux<NV, FLUX>(wL, wR, P.gamma, f);
+      } else if (EQ && a.eqth[2 * ld + L] != 0.0 && a.eqth[2 * ld + R] != 0.0) {
+        // perturbation form around the left cell's equilibrium at the point
+        const double phi = d.phi_fq[qq * lde + e];
+        double rwL, EwL, rwR, EwR;
+        ev.bind(a.eqth[L], a.eqth[ld + L], d.phi_cq[L]).at(ev, phi, rwL, EwL);
+        ev.bind(a.eqth[R], a.eqth[ld + R], d.phi_cq[R]).at(ev, phi, rwR, EwR);
+        double cL[NV], cR[NV], gL[NV], gR[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          cL[v] = a.dev0[v * ld + L];
+          cR[v] = a.dev0[v * ld + R];
+        }
+        cR[0] += rwR - rwL;
+        cR[NV - 1] += EwR - EwL;
+        to_face<NV, ND>(cL, d.frame, lde, e, gL);
+        to_face<NV, ND>(cR, d.frame, lde, e, gR);
+        float pL[NV], pR[NV], dL[NV], dR[NV], df[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          pL[v] = a.fv32[sL + (size_t)v * ld];
+          pR[v] = a.fv32[sR + (size_t)v * ld];
+        }
+        to_face<NV, ND>(pL, d.frame, lde, e, dL);
+        to_face<NV, ND>(pR, d.frame, lde, e, dR);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          dL[v] += float(gL[v]);
+          dR[v] += float(gR[v]);
+        }
+        if (FLUX == 0)
+          hllc_flux_dev<NV>(dL, dR, float(rwL), float(EwL), float(P.gamma), df);
+        else
+          rusanov_flux_dev<NV>(dL, dR, float(rwL), float(EwL), float(P.gamma), df);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) f[v] = double(df[v]);
+        f[1] += EwL * ev.gm1;
+      } else {
+        const double phi = EQ ? d.phi_fq[qq * lde + e] : 0.0;
+        double bL[NV], bR[NV], w[NV], wRb[NV];
+        mixed_base<S, EQ>(d, a, ev, L, phi, bL);
+        mixed_base<S, EQ>(d, a, ev, R, phi, bR);
+        to_face<NV, ND>(bL, d.frame, lde, e, w);
+        to_face<NV, ND>(bR, d.frame, lde, e, wRb);
+        float pL[NV], pR[NV], dL[NV], dR[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          pL[v] = a.fv32[sL + (size_t)v * ld];
+          pR[v] = a.fv32[sR + (size_t)v * ld];
+        }
+        to_face<NV, ND>(pL, d.frame, lde, e, dL);
+        to_face<NV, ND>(pR, d.frame, lde, e, dR);
+        float w32[NV], uL32[NV], uR32[NV], f32[NV], fw32[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          w32[v] = float(w[v]);
+          uL32[v] = w32[v] + dL[v];
+          uR32[v] = w32[v] + (float(wRb[v] - w[v]) + dR[v]);
+        }
+        const float g32 = float(P.gamma);
+        numerical_flux<NV, FLUX>(uL32, uR32, g32, f32);
+        euler_flux<NV>(w32, pressure<NV>(w32, g32), fw32);
+        euler_flux<NV>(w, pressure<NV>(w, P.gamma), f);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) f[v] += double(f32[v] - fw32[v]);
+      }
+      const double wq = d.fqw[qq * lde + e];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) nf[v] += wq * f[v];
     }
     from_face<NV, ND>(nf, d.frame, lde, e);
   } else if (P.flux_bc == 1) {
@@ -573,14 +736,12 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
     // of the boundary cell extrapolated to the face; zero velocity, so F = p n.
     const double found = a.eqth[2 * ld + L];
     if (found != 0.0) {
-      EqEval ev{P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0)};
-      const double eh = a.eqth[L], eK = a.eqth[ld + L], phi_ref = d.phi_cq[L];
+      const EqEval::Bound b = ev.bind(a.eqth[L], a.eqth[ld + L], d.phi_cq[L]);
       double pn = 0.0;
-      const EqEval::Bound eqb = ev.bind(eh, eK, phi_ref);
 #pragma unroll
       for (int qq = 0; qq < S::NQF; ++qq) {
         double r, E;
-        eqb.at(ev, d.phi_fq[qq * lde + e], r, E);
+        b.at(ev, d.phi_fq[qq * lde + e], r, E);
         pn += d.fqw[qq * lde + e] * (E * ev.gm1);
       }
 #pragma unroll
@@ -591,6 +752,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
   for (int v = 0; v < NV; ++v) a.nf[v * lde + e] = nf[v];
 }
 
+// ---------------------------------------------------------------- update
 template <int NV>
 __device__ __forceinline__ double cfl_candidate(const double *u, double gamma, double r) {
   double m2 = 0.0;
@@ -663,14 +825,16 @@ __global__ void __launch_bounds__(128) k_update(const DevData d, const Params P,
     } else {
       const int s = a.stage;
       const double dt = d.clock->dt;
-      const double *coef = last ? P.b : P.a[s + 1];
       double un[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         double dudt = 0.0;
-        for (int j = 0; j < s; ++j)
-          if (coef[j] != 0.0) dudt += coef[j] * a.k[j][v * ld + i];
-        if (coef[s] != 0.0) dudt += coef[s] * tend[v];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          if (j > s) break;
+          const double c = a.coef[j];
+          if (c != 0.0) dudt += c * (j == s ? tend[v] : a.k[j][v * ld + i]);
+        }
         un[v] = a.u0[v * ld + i] + dt * dudt;
       }
       if (!last) {
@@ -710,7 +874,7 @@ __global__ void __launch_bounds__(128) k_cfl(const DevData d, const Params P, co
 // ------------------------------------------------------------ launching
 struct LaunchCfg {
   int n_cells, n_edges;
-  bool eq, src;
+  bool eq, src, mixed;
   int flux;
   cudaStream_t stream;
   cudaEvent_t *ev;  // optional: 4 events recorded around the three stage kernels
@@ -726,26 +890,41 @@ using S3o3 = Shape<3, 18, 9, 4, 4, 3, 3, 4>;
 // 3D order 2 (overfit {3,2,...}): central 10 (9x3), one-sided 7 (6x3)
 using S3o2 = Shape<3, 9, 3, 4, 6, 3, 3, 4>;
 
-template <class S>
-void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
+template <class S, bool MIXED>
+void launch_stage_p(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
   const int nb = (c.n_cells + 127) / 128, nbe = (c.n_edges + 127) / 128;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    k_reconstruct<S, 1, 1><<<nb, 128, 0, c.stream>>>(D, P, a);
+    k_reconstruct<S, 1, 1, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
   else if (c.eq)
-    k_reconstruct<S, 1, 0><<<nb, 128, 0, c.stream>>>(D, P, a);
+    k_reconstruct<S, 1, 0, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
   else if (c.src)
-    k_reconstruct<S, 0, 1><<<nb, 128, 0, c.stream>>>(D, P, a);
+    k_reconstruct<S, 0, 1, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
   else
-    k_reconstruct<S, 0, 0><<<nb, 128, 0, c.stream>>>(D, P, a);
+    k_reconstruct<S, 0, 0, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
-  if (c.flux == 0)
-    k_face_flux<S, 0><<<nbe, 128, 0, c.stream>>>(D, P, a);
-  else
-    k_face_flux<S, 1><<<nbe, 128, 0, c.stream>>>(D, P, a);
+  if (c.flux == 0) {
+    if (c.eq)
+      k_face_flux<S, 0, 1, MIXED><<<nbe, 128, 0, c.stream>>>(D, P, a);
+    else
+      k_face_flux<S, 0, 0, MIXED><<<nbe, 128, 0, c.stream>>>(D, P, a);
+  } else {
+    if (c.eq)
+      k_face_flux<S, 1, 1, MIXED><<<nbe, 128, 0, c.stream>>>(D, P, a);
+    else
+      k_face_flux<S, 1, 0, MIXED><<<nbe, 128, 0, c.stream>>>(D, P, a);
+  }
   if (c.ev) cudaEventRecord(c.ev[2], c.stream);
   k_update<S><<<nb, 128, 0, c.stream>>>(D, P, a);
   if (c.ev) cudaEventRecord(c.ev[3], c.stream);
+}
+
+template <class S>
+void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
+  if (c.mixed)
+    launch_stage_p<S, true>(D, P, a, c);
+  else
+    launch_stage_p<S, false>(D, P, a, c);
 }
 
 template <class S>
