@@ -118,7 +118,8 @@ struct zfvm_solver {
   DBuf<uint8_t> flags, bloc, fkL, fkR, factive;
   DBuf<int> l2g, cface, fL, fR, src_map;
   DBuf<double> pinv, center, inv_len, mom, inv_vol, r_eff, fqx, fqw, frame, farea;
-  DBuf<float> pinv32, fv32;
+  DBuf<float> pinv32, fv32, frame32, xfq32, xcq32, mom32, wg32;
+  DBuf<double> gphi_w;
   DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
   DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos, dev0;
   DBuf<Clock> clock;
@@ -469,13 +470,47 @@ int build_solver(zfvm_solver *s) {
     s->phi_fq.upload(h_phi_fq);
     s->srcb.alloc((size_t)nv * ld);
   }
-  if (s->has_eq) s->eqth.alloc((size_t)3 * ld);
+  if (s->has_eq) s->eqth.alloc((size_t)4 * ld);
   s->u0.alloc((size_t)nv * ld);
   s->ux.alloc((size_t)nv * ld);
   s->kbuf.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
   if (s->mixed) {
     std::vector<float> h32(h_pinv.begin(), h_pinv.end());
     s->pinv32.upload(h32);
+    // FP32 copies: face frames, moments, scaled offsets of the quadrature points
+    s->frame32.upload(std::vector<float>(h_frame.begin(), h_frame.end()));
+    s->mom32.upload(std::vector<float>(h_mom.begin(), h_mom.end()));
+    std::vector<float> hxf((size_t)nf * nqf * nd * ld, 0.f), hxc((size_t)nqc * nd * ld, 0.f);
+    for (index_t i = 0; i < n; ++i) {
+      const double il = 1.0 / g.char_length[i];
+      for (int f = 0; f < nf; ++f) {
+        index_t e = g.edge_indices[i * nf + f];
+        for (int q = 0; q < nqf; ++q)
+          for (int k = 0; k < nd; ++k)
+            hxf[((size_t)(f * nqf + q) * nd + k) * ld + i] = (float)((g.face_qx[e * nqf + q][k] - g.cell_centers[i][k]) * il);
+      }
+      for (int q = 0; q < nqc; ++q)
+        for (int k = 0; k < nd; ++k)
+          hxc[((size_t)q * nd + k) * ld + i] = (float)((g.cell_qx[i * nqc + q][k] - g.cell_centers[i][k]) * il);
+    }
+    s->xfq32.upload(hxf);
+    s->xcq32.upload(hxc);
+    if (s->has_src) {
+      std::vector<double> hg((size_t)nd * ld, 0.0);
+      std::vector<float> hwg((size_t)nqc * nd * ld, 0.f);
+      for (index_t i = 0; i < n; ++i)
+        for (int k = 0; k < nd; ++k) {
+          double acc = 0.0;
+          for (int q = 0; q < nqc; ++q) {
+            double wgq = h_cqw[(size_t)q * ld + i] * h_gphi_cq[((size_t)q * nd + k) * ld + i];
+            acc += wgq;
+            hwg[((size_t)q * nd + k) * ld + i] = (float)wgq;
+          }
+          hg[(size_t)k * ld + i] = acc;
+        }
+      s->gphi_w.upload(hg);
+      s->wg32.upload(hwg);
+    }
     s->fv32.alloc((size_t)nf * nqf * nv * ld);
     s->dev0.alloc((size_t)nv * ld);
   } else {
@@ -504,6 +539,12 @@ int build_solver(zfvm_solver *s) {
   D.pinv = s->pinv.p;
   D.pinv32 = s->pinv32.p;
   D.phi_m1 = s->phi_m1.p;
+  D.frame32 = s->frame32.p;
+  D.xfq32 = s->xfq32.p;
+  D.xcq32 = s->xcq32.p;
+  D.mom32 = s->mom32.p;
+  D.gphi_w = s->gphi_w.p;
+  D.wg32 = s->wg32.p;
   D.phi_var = s->phi_var.p;
   D.bloc = s->bloc.p;
   D.center = s->center.p;
@@ -532,7 +573,8 @@ int build_solver(zfvm_solver *s) {
   auto add = [&](size_t nbytes) { bytes += (int64_t)nbytes; };
   add(s->flags.n + s->bloc.n + s->fkL.n + s->fkR.n + s->factive.n);
   add(4 * (s->l2g.n + s->cface.n + s->fL.n + s->fR.n + s->src_map.n));
-  add(4 * (s->pinv32.n + s->fv32.n));
+  add(4 * (s->pinv32.n + s->fv32.n + s->frame32.n + s->xfq32.n + s->xcq32.n + s->mom32.n + s->wg32.n));
+  add(8 * s->gphi_w.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
            s->ux.n + s->kbuf.n + s->fv.n + s->nfb.n + s->srcb.n + s->eqth.n + s->tend.n + s->aos.n));

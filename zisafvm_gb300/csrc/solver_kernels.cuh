@@ -81,6 +81,13 @@ struct DevData {
   const double *cqx;     // [NQC][ND][ld]
   const double *cqw;     // [NQC][ld]
   const double *phi_fq;  // [NQF][lde]
+  // FP32 copies for the mixed form
+  const float *frame32;  // [ND*ND][lde]
+  const float *xfq32;    // [NF*NQF][ND][ld] scaled offsets (x - x_c) / l of the cell's face points
+  const float *xcq32;    // [NQC][ND][ld] scaled offsets of the cell's quadrature points
+  const float *mom32;    // [NC][ld]
+  const double *gphi_w;  // [ND][ld] sum_q w_q grad phi(x_q) over the cell
+  const float *wg32;     // [NQC][ND][ld] w_q grad phi(x_q)
   Clock *clock;
 };
 
@@ -105,7 +112,7 @@ struct StageArgs {
   double *dev0;      // MIXED: cell-average deviation of every cell [NV][ld]
   double *nf;        // face fluxes [NV][lde]
   double *src;       // per-cell source [NV][ld]
-  double *eqth;      // per-cell equilibrium (h, K, found) [3][ld]
+  double *eqth;      // per-cell bound equilibrium (h_r, f, K, found) [4][ld]
   double *u0;        // state at the start of the step
   double *ux;        // next stage state
   double *k[4];      // stage tendencies
@@ -289,12 +296,15 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
     return;
   }
   // EulerScaling (model/characteristic_scale.hpp:23-32): {rho, c, c, c, E_int}
-  const double cs = sqrt(gamma * (eint * (gamma - 1.0)) / rho);
   R inv_s2[NV];
-  inv_s2[0] = R(1.0 / (rho * rho));
+  {
+    const R rr = R(rho), ee = R(eint), g = R(gamma);
+    const R cs = sqrt(g * (ee * (g - R(1))) / rr);
+    inv_s2[0] = R(1) / (rr * rr);
 #pragma unroll
-  for (int v = 1; v < NV - 1; ++v) inv_s2[v] = R(1.0 / (cs * cs));
-  inv_s2[NV - 1] = R(1.0 / (eint * eint));
+    for (int v = 1; v < NV - 1; ++v) inv_s2[v] = R(1) / (cs * cs);
+    inv_s2[NV - 1] = R(1) / (ee * ee);
+  }
 
   // local equilibrium of this cell from its own average
   double eh = 0.0, eK = 0.0, phi_ref = 0.0;
@@ -314,9 +324,6 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
       eh = 2.0 * eK * rho + m1 - phi_ref;
       found = eK > 0.0;
       closed = true;
-      a.eqth[i] = eh;
-      a.eqth[ld + i] = eK;
-      a.eqth[2 * ld + i] = found ? 1.0 : 0.0;
     }
   }
   if (EQ && !closed) {
@@ -324,11 +331,14 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
     int st = solve_equilibrium<S::NQC>(ev, P, d, i, phi_ref, rho, eint, eh, eK);
     found = st == 0;
     if (st == 2) set_status(d.clock, kStNewton);
-    a.eqth[i] = eh;
-    a.eqth[ld + i] = eK;
-    a.eqth[2 * ld + i] = found ? 1.0 : 0.0;
   }
   const EqEval::Bound eqb = ev.bind(eh, eK, phi_ref);
+  if (EQ) {
+    a.eqth[i] = eqb.hr;
+    a.eqth[ld + i] = eqb.f;
+    a.eqth[2 * ld + i] = eqb.K;
+    a.eqth[3 * ld + i] = found ? 1.0 : 0.0;
+  }
   // deviation of a stencil cell's average from this cell's equilibrium (FP64)
   auto load_dev = [&](int j, double *out) {
 #pragma unroll
@@ -469,16 +479,17 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
 
   double xc[ND];
   R C[NC];
+  double il = 0.0;
+  if (!MIXED) {
 #pragma unroll
-  for (int k = 0; k < ND; ++k) xc[k] = d.center[k * ld + i];
-  const double il = d.inv_len[i];
+    for (int k = 0; k < ND; ++k) xc[k] = d.center[k * ld + i];
+    il = d.inv_len[i];
+  }
 #pragma unroll
-  for (int c = 0; c < NC; ++c) C[c] = R(d.mom[c * ld + i]);
-  // non-constant part of the limited polynomial at x
-  auto poly_at = [&](const double *x, R *pv) {
-    R X[ND], phi[NC];
-#pragma unroll
-    for (int k = 0; k < ND; ++k) X[k] = R((x[k] - xc[k]) * il);
+  for (int c = 0; c < NC; ++c) C[c] = MIXED ? R(d.mom32[c * ld + i]) : R(d.mom[c * ld + i]);
+  // non-constant part of the limited polynomial at the scaled offset X
+  auto poly_X = [&](const R *X, R *pv) {
+    R phi[NC];
     basis<ND, NC>(X, C, phi);
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
@@ -487,6 +498,12 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
       for (int c = 0; c < NC; ++c) s += pf[c][v] * phi[c];
       pv[v] = s;
     }
+  };
+  auto poly_at = [&](const double *x, R *pv) {
+    R X[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) X[k] = R((x[k] - xc[k]) * il);
+    poly_X(X, pv);
   };
 
   double s_acc[NV];
@@ -502,11 +519,18 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
     const double sgn = (cf & 1) ? -1.0 : 1.0;
 #pragma unroll
     for (int qq = 0; qq < S::NQF; ++qq) {
-      double x[ND];
-#pragma unroll
-      for (int k = 0; k < ND; ++k) x[k] = d.fqx[(qq * ND + k) * d.lde + e];
       R pv[NV];
-      poly_at(x, pv);
+      if (MIXED) {
+        R X[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) X[k] = R(d.xfq32[((f * S::NQF + qq) * ND + k) * ld + i]);
+        poly_X(X, pv);
+      } else {
+        double x[ND];
+#pragma unroll
+        for (int k = 0; k < ND; ++k) x[k] = d.fqx[(qq * ND + k) * d.lde + e];
+        poly_at(x, pv);
+      }
       double r_eq = 0.0, E_eq = 0.0;
       if (EQ && found) {
         eqb.at(ev, d.phi_fq[qq * d.lde + e], r_eq, E_eq);
@@ -534,7 +558,41 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
     }
   }
 
-  if (SRC) {
+  if (SRC && MIXED) {
+    // volume part, split into the FP64 cell-average deviation times
+    // sum_q w_q grad phi_q and the FP32 polynomial part
+    R acc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) acc[v] = R(0);
+#pragma unroll
+    for (int qq = 0; qq < S::NQC; ++qq) {
+      R X[ND], wg[ND], pv[NV];
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        X[k] = R(d.xcq32[(qq * ND + k) * ld + i]);
+        wg[k] = R(d.wg32[(qq * ND + k) * ld + i]);
+      }
+      poly_X(X, pv);
+      R mg = R(0);
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        acc[1 + k] -= pv[0] * wg[k];
+        mg += pv[1 + k] * wg[k];
+      }
+      acc[NV - 1] -= mg;
+    }
+    double mg0 = 0.0;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      const double G = d.gphi_w[k * ld + i];
+      s_acc[1 + k] += -dev0[0] * G + double(acc[1 + k]);
+      mg0 += dev0[1 + k] * G;
+    }
+    s_acc[NV - 1] += -mg0 + double(acc[NV - 1]);
+    const double iv = d.inv_vol[i];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.src[v * ld + i] = s_acc[v] * iv;
+  } else if (SRC) {
     // volume part: (0, -rho' grad phi, -m . grad phi), rho' = delta (well-balanced)
     // or the full reconstruction (gravity_source_loop.hpp:60-84,121-148)
 #pragma unroll
@@ -594,6 +652,33 @@ __device__ __forceinline__ void from_face(double *f, const double *fr, int lde, 
   for (int k = 0; k < ND; ++k) f[1 + k] = m[k];
 }
 
+template <int NV, int ND>
+__device__ __forceinline__ void to_face32(const float *u, const float *fr, int lde, int e, float *w) {
+  w[0] = u[0];
+  w[NV - 1] = u[NV - 1];
+#pragma unroll
+  for (int a = 0; a < ND; ++a) {
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) s += u[1 + k] * fr[(a * ND + k) * lde + e];
+    w[1 + a] = s;
+  }
+}
+
+template <int NV, int ND>
+__device__ __forceinline__ void from_face32(float *f, const float *fr, int lde, int e) {
+  float m[ND];
+#pragma unroll
+  for (int k = 0; k < ND; ++k) {
+    float s = 0.0f;
+#pragma unroll
+    for (int a = 0; a < ND; ++a) s += f[1 + a] * fr[(a * ND + k) * lde + e];
+    m[k] = s;
+  }
+#pragma unroll
+  for (int k = 0; k < ND; ++k) f[1 + k] = m[k];
+}
+
 template <int NV, int FLUX, class T>
 __device__ __forceinline__ void numerical_flux(const T *uL, const T *uR, T gamma, T *f) {
   if (FLUX == 0)
@@ -601,6 +686,11 @@ __device__ __forceinline__ void numerical_flux(const T *uL, const T *uR, T gamma
   else
     rusanov_flux<NV>(uL, uR, gamma, f);
 }
+
+__device__ __forceinline__ EqEval::Bound eq_bound(const StageArgs &a, int ld, int c) {
+  return EqEval::Bound{a.eqth[c], a.eqth[ld + c], a.eqth[2 * ld + c]};
+}
+__device__ __forceinline__ bool eq_found(const StageArgs &a, int ld, int c) { return a.eqth[3 * ld + c] != 0.0; }
 
 // Face state of one side in the MIXED form: FP64 base (cell-average deviation
 // plus the equilibrium at the point) and the FP32 polynomial part.
@@ -610,10 +700,9 @@ __device__ __forceinline__ void mixed_base(const DevData &d, const StageArgs &a,
   const int ld = d.ld;
 #pragma unroll
   for (int v = 0; v < S::NV; ++v) base[v] = a.dev0[v * ld + c];
-  if (EQ && a.eqth[2 * ld + c] != 0.0) {
-    const EqEval::Bound b = ev.bind(a.eqth[c], a.eqth[ld + c], d.phi_cq[c]);
+  if (EQ && eq_found(a, ld, c)) {
     double r, E;
-    b.at(ev, phi, r, E);
+    eq_bound(a, ld, c).at(ev, phi, r, E);
     base[0] += r;
     base[S::NV - 1] += E;
   }
@@ -634,8 +723,12 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
   for (int v = 0; v < NV; ++v) nf[v] = 0.0;
   if (R >= 0) {
     const int kL = d.fkL[e], kR = d.fkR[e];
+    double nf_rot[NV];  // contributions still in the face frame
+#pragma unroll
+    for (int v = 0; v < NV; ++v) nf_rot[v] = 0.0;
 #pragma unroll
     for (int qq = 0; qq < S::NQF; ++qq) {
+      bool rotated = true;
       const size_t sL = (size_t)((kL * S::NQF + qq) * NV) * ld + L;
       const size_t sR = (size_t)((kR * S::NQF + qq) * NV) * ld + R;
       double f[NV];
@@ -649,76 +742,83 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
         to_face<NV, ND>(uL, d.frame, lde, e, wL);
         to_face<NV, ND>(uR, d.frame, lde, e, wR);
         numerical_flux<NV, FLUX>(wL, wR, P.gamma, f);
-      } else if (EQ && a.eqth[2 * ld + L] != 0.0 && a.eqth[2 * ld + R] != 0.0) {
-        // perturbation form around the left cell's equilibrium at the point
+      } else if (EQ && eq_found(a, ld, L) && eq_found(a, ld, R)) {
+        // perturbation form around the left cell's equilibrium at the point:
+        // F = (0, p_w n, 0) + [F32(w + dL, w + dR) - F32(w)] in the face frame
         const double phi = d.phi_fq[qq * lde + e];
         double rwL, EwL, rwR, EwR;
-        ev.bind(a.eqth[L], a.eqth[ld + L], d.phi_cq[L]).at(ev, phi, rwL, EwL);
-        ev.bind(a.eqth[R], a.eqth[ld + R], d.phi_cq[R]).at(ev, phi, rwR, EwR);
-        double cL[NV], cR[NV], gL[NV], gR[NV];
+        eq_bound(a, ld, L).at(ev, phi, rwL, EwL);
+        eq_bound(a, ld, R).at(ev, phi, rwR, EwR);
+        float cL[NV], cR[NV], dL[NV], dR[NV], df[NV];
+        cL[0] = float(a.dev0[L]);
+        cR[0] = float(a.dev0[R] + (rwR - rwL));
+        cL[NV - 1] = float(a.dev0[(NV - 1) * ld + L]);
+        cR[NV - 1] = float(a.dev0[(NV - 1) * ld + R] + (EwR - EwL));
+#pragma unroll
+        for (int v = 1; v < NV - 1; ++v) {
+          cL[v] = float(a.dev0[v * ld + L]);
+          cR[v] = float(a.dev0[v * ld + R]);
+        }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-          cL[v] = a.dev0[v * ld + L];
-          cR[v] = a.dev0[v * ld + R];
+          cL[v] += a.fv32[sL + (size_t)v * ld];
+          cR[v] += a.fv32[sR + (size_t)v * ld];
         }
-        cR[0] += rwR - rwL;
-        cR[NV - 1] += EwR - EwL;
-        to_face<NV, ND>(cL, d.frame, lde, e, gL);
-        to_face<NV, ND>(cR, d.frame, lde, e, gR);
-        float pL[NV], pR[NV], dL[NV], dR[NV], df[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          pL[v] = a.fv32[sL + (size_t)v * ld];
-          pR[v] = a.fv32[sR + (size_t)v * ld];
-        }
-        to_face<NV, ND>(pL, d.frame, lde, e, dL);
-        to_face<NV, ND>(pR, d.frame, lde, e, dR);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          dL[v] += float(gL[v]);
-          dR[v] += float(gR[v]);
-        }
+        to_face32<NV, ND>(cL, d.frame32, lde, e, dL);
+        to_face32<NV, ND>(cR, d.frame32, lde, e, dR);
         if (FLUX == 0)
           hllc_flux_dev<NV>(dL, dR, float(rwL), float(EwL), float(P.gamma), df);
         else
           rusanov_flux_dev<NV>(dL, dR, float(rwL), float(EwL), float(P.gamma), df);
+        from_face32<NV, ND>(df, d.frame32, lde, e);
+        const double p_w = EwL * ev.gm1;
 #pragma unroll
         for (int v = 0; v < NV; ++v) f[v] = double(df[v]);
-        f[1] += EwL * ev.gm1;
+#pragma unroll
+        for (int k = 0; k < ND; ++k) f[1 + k] += p_w * d.frame[k * lde + e];
+        rotated = false;
+      } else if (!EQ) {
+        // plain FP32 flux of the FP32 face states
+        float uL[NV], uR[NV], wL[NV], wR[NV], f32[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          uL[v] = float(a.dev0[v * ld + L]) + a.fv32[sL + (size_t)v * ld];
+          uR[v] = float(a.dev0[v * ld + R]) + a.fv32[sR + (size_t)v * ld];
+        }
+        to_face32<NV, ND>(uL, d.frame32, lde, e, wL);
+        to_face32<NV, ND>(uR, d.frame32, lde, e, wR);
+        numerical_flux<NV, FLUX>(wL, wR, float(P.gamma), f32);
+        from_face32<NV, ND>(f32, d.frame32, lde, e);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) f[v] = double(f32[v]);
+        rotated = false;
       } else {
-        const double phi = EQ ? d.phi_fq[qq * lde + e] : 0.0;
-        double bL[NV], bR[NV], w[NV], wRb[NV];
+        // a side without equilibrium: FP64 flux of base + polynomial part
+        const double phi = d.phi_fq[qq * lde + e];
+        double bL[NV], bR[NV], wL[NV], wR[NV];
         mixed_base<S, EQ>(d, a, ev, L, phi, bL);
         mixed_base<S, EQ>(d, a, ev, R, phi, bR);
-        to_face<NV, ND>(bL, d.frame, lde, e, w);
-        to_face<NV, ND>(bR, d.frame, lde, e, wRb);
-        float pL[NV], pR[NV], dL[NV], dR[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-          pL[v] = a.fv32[sL + (size_t)v * ld];
-          pR[v] = a.fv32[sR + (size_t)v * ld];
+          bL[v] += double(a.fv32[sL + (size_t)v * ld]);
+          bR[v] += double(a.fv32[sR + (size_t)v * ld]);
         }
-        to_face<NV, ND>(pL, d.frame, lde, e, dL);
-        to_face<NV, ND>(pR, d.frame, lde, e, dR);
-        float w32[NV], uL32[NV], uR32[NV], f32[NV], fw32[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          w32[v] = float(w[v]);
-          uL32[v] = w32[v] + dL[v];
-          uR32[v] = w32[v] + (float(wRb[v] - w[v]) + dR[v]);
-        }
-        const float g32 = float(P.gamma);
-        numerical_flux<NV, FLUX>(uL32, uR32, g32, f32);
-        euler_flux<NV>(w32, pressure<NV>(w32, g32), fw32);
-        euler_flux<NV>(w, pressure<NV>(w, P.gamma), f);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) f[v] += double(f32[v] - fw32[v]);
+        to_face<NV, ND>(bL, d.frame, lde, e, wL);
+        to_face<NV, ND>(bR, d.frame, lde, e, wR);
+        numerical_flux<NV, FLUX>(wL, wR, P.gamma, f);
       }
       const double wq = d.fqw[qq * lde + e];
+      if (rotated) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) nf[v] += wq * f[v];
+        for (int v = 0; v < NV; ++v) nf_rot[v] += wq * f[v];
+      } else {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) nf[v] += wq * f[v];
+      }
     }
-    from_face<NV, ND>(nf, d.frame, lde, e);
+    from_face<NV, ND>(nf_rot, d.frame, lde, e);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) nf[v] += nf_rot[v];
   } else if (P.flux_bc == 1) {
     // FluxBC (boundary/flux_bc.hpp:25-42): physical flux of the cell average
     double u[NV], w[NV], f[NV];
@@ -734,9 +834,8 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
   } else if (P.flux_bc == 2) {
     // EquilibriumFluxBC (boundary/equilibrium_flux_bc.hpp:36-62): the equilibrium
     // of the boundary cell extrapolated to the face; zero velocity, so F = p n.
-    const double found = a.eqth[2 * ld + L];
-    if (found != 0.0) {
-      const EqEval::Bound b = ev.bind(a.eqth[L], a.eqth[ld + L], d.phi_cq[L]);
+    if (eq_found(a, ld, L)) {
+      const EqEval::Bound b = eq_bound(a, ld, L);
       double pn = 0.0;
 #pragma unroll
       for (int qq = 0; qq < S::NQF; ++qq) {
