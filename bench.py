@@ -315,7 +315,7 @@ def main():
     for _ in range(e2e_steps):
         solver.set_state(host)
         solver.advance(n_steps=1)
-        host_out[:], _ = solver.get_state()
+        solver.get_state(out=host_out)
         host, host_out = host_out, host
     e2e_s = time.perf_counter() - t0
     e2e_value = world * cells * stages * e2e_steps / e2e_s

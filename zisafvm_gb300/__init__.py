@@ -341,8 +341,10 @@ class Solver:
         assert a.shape == (self.mesh.n_cells, 5)
         _check(load_library().zfvm_set_state(self._h, _dp(a), t))
 
-    def get_state(self) -> tuple[np.ndarray, float]:
-        a = np.zeros((self.mesh.n_cells, 5))
+    def get_state(self, out: np.ndarray | None = None) -> tuple[np.ndarray, float]:
+        """Copy the state to the host (into `out` when given, e.g. pinned memory)."""
+        a = out if out is not None else np.zeros((self.mesh.n_cells, 5))
+        assert a.shape == (self.mesh.n_cells, 5) and a.dtype == np.float64 and a.flags.c_contiguous
         t = C.c_double()
         _check(load_library().zfvm_get_state(self._h, _dp(a), C.byref(t)))
         return a, t.value

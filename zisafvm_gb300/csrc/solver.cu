@@ -118,7 +118,7 @@ struct zfvm_solver {
   DBuf<uint8_t> flags, bloc, fkL, fkR, factive;
   DBuf<int> l2g, cface, fL, fR, src_map;
   DBuf<double> pinv, center, inv_len, mom, inv_vol, r_eff, fqx, fqw, frame, farea;
-  DBuf<float> pinv32, fv32, frame32, xfq32, xcq32, mom32, wg32;
+  DBuf<float> pinv32, fv32, frame32, xfq32, xcq32, mom32, wg32, g32, mL32, mR32, src32, kbuf32;
   DBuf<double> gphi_w;
   DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
   DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos, dev0;
@@ -155,6 +155,11 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   a.ux = s->ux.p;
   for (int k = 0; k < 4; ++k) a.k[k] = s->kbuf.p ? s->kbuf.p + (size_t)k * s->nv * s->ld : nullptr;
   a.tend_out = tend_out;
+  a.g32 = s->g32.p;
+  a.mL32 = s->mL32.p;
+  a.mR32 = s->mR32.p;
+  a.src32 = s->src32.p;
+  for (int k = 0; k < 4; ++k) a.k32[k] = s->kbuf32.p ? s->kbuf32.p + (size_t)k * s->nv * s->ld : nullptr;
   a.stage = stage;
   const bool last = stage == s->P.n_stages - 1;
   for (int j = 0; j < 4; ++j) a.coef[j] = last ? s->P.b[j] : (stage + 1 < 4 ? s->P.a[stage + 1][j] : 0.0);
@@ -382,7 +387,10 @@ int build_solver(zfvm_solver *s) {
     if (R >= 0)
       h_fact[e] = Lint || Rint;
     else
-      h_fact[e] = Lint && sc.flux_bc != ZFVM_FLUX_BC_NONE;
+      // mixed well-balanced form: a boundary face also carries the cell's
+      // surface source term, so it is visited without a flux boundary
+      h_fact[e] = Lint && (sc.flux_bc != ZFVM_FLUX_BC_NONE ||
+                           (sc.precision == ZFVM_MIXED && sc.equilibrium == ZFVM_EQ_ISENTROPIC));
     for (int q = 0; q < nqf; ++q) {
       h_fqw[(size_t)q * lde + e] = g.face_qw[e * nqf + q];
       for (int k = 0; k < nd; ++k) h_fqx[((size_t)q * nd + k) * lde + e] = g.face_qx[e * nqf + q][k];
@@ -468,12 +476,12 @@ int build_solver(zfvm_solver *s) {
     s->cqx.upload(h_cqx);
     s->cqw.upload(h_cqw);
     s->phi_fq.upload(h_phi_fq);
-    s->srcb.alloc((size_t)nv * ld);
+    if (!s->mixed) s->srcb.alloc((size_t)nv * ld);
   }
   if (s->has_eq) s->eqth.alloc((size_t)4 * ld);
   s->u0.alloc((size_t)nv * ld);
   s->ux.alloc((size_t)nv * ld);
-  s->kbuf.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
+  if (!s->mixed) s->kbuf.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
   if (s->mixed) {
     std::vector<float> h32(h_pinv.begin(), h_pinv.end());
     s->pinv32.upload(h32);
@@ -495,6 +503,12 @@ int build_solver(zfvm_solver *s) {
     }
     s->xfq32.upload(hxf);
     s->xcq32.upload(hxc);
+    s->g32.alloc((size_t)nv * lde);
+    s->mL32.alloc((size_t)nd * lde);
+    s->mR32.alloc((size_t)nd * lde);
+    s->kbuf32.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
+    if (s->has_src) s->src32.alloc((size_t)nv * ld);
+    for (auto *b : {&s->g32, &s->mL32, &s->mR32, &s->kbuf32, &s->src32}) b->zero(s->stream);
     if (s->has_src) {
       std::vector<double> hg((size_t)nd * ld, 0.0);
       std::vector<float> hwg((size_t)nqc * nd * ld, 0.f);
@@ -516,7 +530,7 @@ int build_solver(zfvm_solver *s) {
   } else {
     s->fv.alloc((size_t)nf * nqf * nv * ld);
   }
-  s->nfb.alloc((size_t)nv * lde);
+  if (!s->mixed) s->nfb.alloc((size_t)nv * lde);
   s->tend.alloc((size_t)nv * ld);
   s->aos.alloc((size_t)5 * n);
   s->clock.alloc(1);
@@ -573,7 +587,8 @@ int build_solver(zfvm_solver *s) {
   auto add = [&](size_t nbytes) { bytes += (int64_t)nbytes; };
   add(s->flags.n + s->bloc.n + s->fkL.n + s->fkR.n + s->factive.n);
   add(4 * (s->l2g.n + s->cface.n + s->fL.n + s->fR.n + s->src_map.n));
-  add(4 * (s->pinv32.n + s->fv32.n + s->frame32.n + s->xfq32.n + s->xcq32.n + s->mom32.n + s->wg32.n));
+  add(4 * (s->pinv32.n + s->fv32.n + s->frame32.n + s->xfq32.n + s->xcq32.n + s->mom32.n + s->wg32.n + s->g32.n +
+           s->mL32.n + s->mR32.n + s->src32.n + s->kbuf32.n));
   add(8 * s->gphi_w.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +

@@ -117,6 +117,10 @@ struct StageArgs {
   double *ux;        // next stage state
   double *k[4];      // stage tendencies
   double *tend_out;  // when non-null: write the tendency and do no RK update
+  // MIXED: per-face flux G [NV][lde] and per-side corrections mL, mR [ND][lde]
+  // (tend_L += -G + mL, tend_R += G + mR), FP32 source [NV][ld], FP32 stage
+  // tendencies [NV][ld]
+  float *g32, *mL32, *mR32, *src32, *k32[4];
   double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
   int stage;
 };
@@ -532,7 +536,7 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
         poly_at(x, pv);
       }
       double r_eq = 0.0, E_eq = 0.0;
-      if (EQ && found) {
+      if (EQ && found && !MIXED) {
         eqb.at(ev, d.phi_fq[qq * d.lde + e], r_eq, E_eq);
         if (SRC) {
           // surface part of the well-balanced source: p_eq n_out
@@ -581,6 +585,8 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
       }
       acc[NV - 1] -= mg;
     }
+    // the surface part p_eq n_out cancels face by face against the flux
+    // baseline and is accounted for in k_face_flux
     double mg0 = 0.0;
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
@@ -591,7 +597,7 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
     s_acc[NV - 1] += -mg0 + double(acc[NV - 1]);
     const double iv = d.inv_vol[i];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) a.src[v * ld + i] = s_acc[v] * iv;
+    for (int v = 0; v < NV; ++v) a.src32[v * ld + i] = float(s_acc[v] * iv);
   } else if (SRC) {
     // volume part: (0, -rho' grad phi, -m . grad phi), rho' = delta (well-balanced)
     // or the full reconstruction (gravity_source_loop.hpp:60-84,121-148)
@@ -726,6 +732,11 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
     double nf_rot[NV];  // contributions still in the face frame
 #pragma unroll
     for (int v = 0; v < NV; ++v) nf_rot[v] = 0.0;
+    float g32[NV], mL[ND], mR[ND];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) g32[v] = 0.f;
+#pragma unroll
+    for (int k = 0; k < ND; ++k) mL[k] = mR[k] = 0.f;
 #pragma unroll
     for (int qq = 0; qq < S::NQF; ++qq) {
       bool rotated = true;
@@ -771,12 +782,15 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
         else
           rusanov_flux_dev<NV>(dL, dR, float(rwL), float(EwL), float(P.gamma), df);
         from_face32<NV, ND>(df, d.frame32, lde, e);
-        const double p_w = EwL * ev.gm1;
+        // the baseline p_wL n cancels the left cell's own surface source term
+        // exactly; the right cell keeps (p_wL - p_eqR) n
+        const float wq = float(d.fqw[qq * lde + e]);
+        const float dpn = float((EwL - EwR) * ev.gm1) * wq;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) f[v] = double(df[v]);
+        for (int v = 0; v < NV; ++v) g32[v] += wq * df[v];
 #pragma unroll
-        for (int k = 0; k < ND; ++k) f[1 + k] += p_w * d.frame[k * lde + e];
-        rotated = false;
+        for (int k = 0; k < ND; ++k) mR[k] += dpn * d.frame32[k * lde + e];
+        continue;
       } else if (!EQ) {
         // plain FP32 flux of the FP32 face states
         float uL[NV], uR[NV], wL[NV], wR[NV], f32[NV];
@@ -789,9 +803,10 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
         to_face32<NV, ND>(uR, d.frame32, lde, e, wR);
         numerical_flux<NV, FLUX>(wL, wR, float(P.gamma), f32);
         from_face32<NV, ND>(f32, d.frame32, lde, e);
+        const float wq = float(d.fqw[qq * lde + e]);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) f[v] = double(f32[v]);
-        rotated = false;
+        for (int v = 0; v < NV; ++v) g32[v] += wq * f32[v];
+        continue;
       } else {
         // a side without equilibrium: FP64 flux of base + polynomial part
         const double phi = d.phi_fq[qq * lde + e];
@@ -806,6 +821,19 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
         to_face<NV, ND>(bL, d.frame, lde, e, wL);
         to_face<NV, ND>(bR, d.frame, lde, e, wR);
         numerical_flux<NV, FLUX>(wL, wR, P.gamma, f);
+        // surface source terms of the sides that have an equilibrium
+        double rq, Eq;
+        const float wq32 = float(d.fqw[qq * lde + e]);
+        if (eq_found(a, ld, L)) {
+          eq_bound(a, ld, L).at(ev, phi, rq, Eq);
+#pragma unroll
+          for (int k = 0; k < ND; ++k) mL[k] += float(Eq * ev.gm1) * wq32 * d.frame32[k * lde + e];
+        }
+        if (eq_found(a, ld, R)) {
+          eq_bound(a, ld, R).at(ev, phi, rq, Eq);
+#pragma unroll
+          for (int k = 0; k < ND; ++k) mR[k] -= float(Eq * ev.gm1) * wq32 * d.frame32[k * lde + e];
+        }
       }
       const double wq = d.fqw[qq * lde + e];
       if (rotated) {
@@ -819,6 +847,16 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
     from_face<NV, ND>(nf_rot, d.frame, lde, e);
 #pragma unroll
     for (int v = 0; v < NV; ++v) nf[v] += nf_rot[v];
+    if (MIXED) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) a.g32[v * lde + e] = g32[v] + float(nf[v]);
+#pragma unroll
+      for (int k = 0; k < ND; ++k) {
+        a.mL32[k * lde + e] = mL[k];
+        a.mR32[k * lde + e] = mR[k];
+      }
+      return;
+    }
   } else if (P.flux_bc == 1) {
     // FluxBC (boundary/flux_bc.hpp:25-42): physical flux of the cell average
     double u[NV], w[NV], f[NV];
@@ -831,6 +869,9 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
     const double area = d.farea[e];
 #pragma unroll
     for (int v = 0; v < NV; ++v) nf[v] = area * f[v];
+  } else if (P.flux_bc == 2 && MIXED) {
+    // EquilibriumFluxBC: F = p_eq n on the face equals the cell's own surface
+    // source term there, so the pair contributes nothing
   } else if (P.flux_bc == 2) {
     // EquilibriumFluxBC (boundary/equilibrium_flux_bc.hpp:36-62): the equilibrium
     // of the boundary cell extrapolated to the face; zero velocity, so F = p n.
@@ -846,6 +887,32 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
 #pragma unroll
       for (int k = 0; k < ND; ++k) nf[1 + k] = pn * d.frame[k * lde + e];
     }
+  }
+  if (MIXED) {
+    // boundary face: flux of the cell average (FluxBC); with an equilibrium and
+    // no FluxBC the cell's surface source term on this face remains
+    float mLb[ND];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) mLb[k] = 0.f;
+    if (EQ && P.flux_bc != 2 && eq_found(a, ld, L)) {
+      const EqEval::Bound b = eq_bound(a, ld, L);
+#pragma unroll
+      for (int qq = 0; qq < S::NQF; ++qq) {
+        double r, E;
+        b.at(ev, d.phi_fq[qq * lde + e], r, E);
+        const float pw = float(E * ev.gm1 * d.fqw[qq * lde + e]);
+#pragma unroll
+        for (int k = 0; k < ND; ++k) mLb[k] += pw * d.frame32[k * lde + e];
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.g32[v * lde + e] = float(nf[v]);
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      a.mL32[k * lde + e] = mLb[k];
+      a.mR32[k * lde + e] = 0.f;
+    }
+    return;
   }
 #pragma unroll
   for (int v = 0; v < NV; ++v) a.nf[v * lde + e] = nf[v];
@@ -888,35 +955,64 @@ __device__ __forceinline__ void block_min_to_clock(double cand, Clock *clock) {
   }
 }
 
-template <class S>
+template <class S, bool MIXED>
 __global__ void __launch_bounds__(128) k_update(const DevData d, const Params P, StageArgs a) {
-  constexpr int NV = S::NV, NF = S::NF;
+  constexpr int NV = S::NV, NF = S::NF, ND = S::ND;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool last = a.stage == P.n_stages - 1;
   double cand = INFINITY;
   if (!d.clock->done && i < d.n_cells && (d.flags[i] & kInterior)) {
     const int ld = d.ld, lde = d.lde;
     double tend[NV];
+    if (MIXED) {
+      // deviation-sized terms only: FP32 sums
+      float t32[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) tend[v] = 0.0;
+      for (int v = 0; v < NV; ++v) t32[v] = 0.f;
 #pragma unroll
-    for (int f = 0; f < NF; ++f) {
-      const int cf = d.cface[f * ld + i];
-      if (cf < 0) continue;
-      const int e = cf >> 1;
-      const bool right = cf & 1;
+      for (int f = 0; f < NF; ++f) {
+        const int cf = d.cface[f * ld + i];
+        if (cf < 0) continue;
+        const int e = cf >> 1;
+        const bool right = cf & 1;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const float x = a.g32[v * lde + e];
+          t32[v] += right ? x : -x;
+        }
+        const float *m = right ? a.mR32 : a.mL32;
+#pragma unroll
+        for (int k = 0; k < ND; ++k) t32[1 + k] += m[k * lde + e];
+      }
+      const float iv = float(d.inv_vol[i]);
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const double x = a.nf[v * lde + e];
-        tend[v] += right ? x : -x;
+        t32[v] *= iv;
+        if (a.src32) t32[v] += a.src32[v * ld + i];
+        tend[v] = double(t32[v]);
       }
-    }
-    const double iv = d.inv_vol[i];
+    } else {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) tend[v] *= iv;
-    if (a.src) {
+      for (int v = 0; v < NV; ++v) tend[v] = 0.0;
 #pragma unroll
-      for (int v = 0; v < NV; ++v) tend[v] += a.src[v * ld + i];
+      for (int f = 0; f < NF; ++f) {
+        const int cf = d.cface[f * ld + i];
+        if (cf < 0) continue;
+        const int e = cf >> 1;
+        const bool right = cf & 1;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const double x = a.nf[v * lde + e];
+          tend[v] += right ? x : -x;
+        }
+      }
+      const double iv = d.inv_vol[i];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) tend[v] *= iv;
+      if (a.src) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) tend[v] += a.src[v * ld + i];
+      }
     }
     if (a.tend_out) {
 #pragma unroll
@@ -932,14 +1028,18 @@ __global__ void __launch_bounds__(128) k_update(const DevData d, const Params P,
         for (int j = 0; j < 4; ++j) {
           if (j > s) break;
           const double c = a.coef[j];
-          if (c != 0.0) dudt += c * (j == s ? tend[v] : a.k[j][v * ld + i]);
+          if (c != 0.0)
+            dudt += c * (j == s ? tend[v] : (MIXED ? double(a.k32[j][v * ld + i]) : a.k[j][v * ld + i]));
         }
         un[v] = a.u0[v * ld + i] + dt * dudt;
       }
       if (!last) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-          a.k[s][v * ld + i] = tend[v];
+          if (MIXED)
+            a.k32[s][v * ld + i] = float(tend[v]);
+          else
+            a.k[s][v * ld + i] = tend[v];
           a.ux[v * ld + i] = un[v];
         }
       } else {
@@ -1014,7 +1114,7 @@ void launch_stage_p(const DevData &D, const Params &P, StageArgs &a, const Launc
       k_face_flux<S, 1, 0, MIXED><<<nbe, 128, 0, c.stream>>>(D, P, a);
   }
   if (c.ev) cudaEventRecord(c.ev[2], c.stream);
-  k_update<S><<<nb, 128, 0, c.stream>>>(D, P, a);
+  k_update<S, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
   if (c.ev) cudaEventRecord(c.ev[3], c.stream);
 }
 
