@@ -180,6 +180,27 @@ int zfvm_launches_per_step(const zfvm_solver *s, int32_t *launches);
 /* Bytes of device memory the solver holds. */
 int zfvm_device_bytes(const zfvm_solver *s, int64_t *bytes);
 
+/* ---- batches -------------------------------------------------------------
+ * Many independent solves stepped together: one persistent launch per phase
+ * per RK stage covers every slot (of one kernel configuration), each slot with
+ * its own clock.  No counterpart class in the reference (it runs one solve per
+ * process, or one per MPI rank). */
+typedef struct zfvm_batch zfvm_batch;
+int zfvm_batch_create(int32_t max_slots, zfvm_batch **out);
+int zfvm_batch_destroy(zfvm_batch *b);
+/* Add a solver (its state already set) that runs until n_steps (if > 0) or
+ * t_end (if > 0).  The solver must not be driven by itself while in a batch. */
+int zfvm_batch_add(zfvm_batch *b, zfvm_solver *s, int64_t n_steps, double t_end, int32_t *slot);
+int zfvm_batch_remove(zfvm_batch *b, int32_t slot);
+/* Replay up to max_steps batched steps; returns the number of slots still running. */
+int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_running);
+int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *ms);
+/* Pick the persistent grid sizes of each group's kernels by timing candidates. */
+int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *best_ms);
+int zfvm_batch_slot_status(zfvm_batch *b, int32_t slot, double *t, int64_t *steps, int32_t *done,
+                           int32_t *status);
+int zfvm_batch_slots(const zfvm_batch *b, int32_t *n_active);
+
 const char *zfvm_last_error(void);
 
 #ifdef __cplusplus

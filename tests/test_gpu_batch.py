@@ -1,0 +1,93 @@
+"""Batched solves: every instance gives the same result alone and in the batch."""
+import numpy as np
+import pytest
+
+import zisafvm_gb300 as z
+from problems import polytrope_2d, vortex_2d
+
+pytestmark = pytest.mark.gpu
+
+
+def _single(mesh, scheme, u0, n_steps=0, t_end=0.0):
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t, n = s.advance(n_steps=n_steps, t_end=t_end)
+    u, _ = s.get_state()
+    return u, t, n
+
+
+@pytest.mark.parametrize("precision", [z.FP64, z.MIXED])
+def test_batch_equals_alone(zlib, precision):
+    probs = [polytrope_2d(n_rings=r, amplitude=a, seed=7 + r, precision=precision)
+             for r, a in ((12, 1e-3), (20, 1e-2), (9, 1e-4))]
+    raw, mesh, scheme, u0 = vortex_2d(n=16, halo=3)
+    scheme.precision = precision
+    probs.append((raw, mesh, scheme, u0))
+    b = z.Batch(8)
+    solvers, slots = [], []
+    for k, (raw, mesh, scheme, u0) in enumerate(probs):
+        s = z.Solver(mesh, scheme)
+        s.set_state(u0)
+        solvers.append(s)
+        slots.append(b.add(s, n_steps=6 + 2 * k))
+    for _ in range(10):
+        if b.advance(4) == 0:
+            break
+    for k, (raw, mesh, scheme, u0) in enumerate(probs):
+        st = b.status(slots[k])
+        assert st["done"] and st["steps"] == 6 + 2 * k
+        b.remove(slots[k])
+        u_b, t_b = solvers[k].get_state()
+        u_a, t_a, n_a = _single(mesh, scheme, u0, n_steps=6 + 2 * k)
+        assert n_a == 6 + 2 * k
+        if precision == z.FP64:
+            # same FP64 arithmetic in the single and the batched kernels
+            assert t_b == t_a
+            assert np.array_equal(u_b, u_a), np.abs(u_b - u_a).max()
+        else:
+            # FP32 parts may be rounded differently by the two kernel builds
+            assert abs(t_b - t_a) <= 1e-12 * t_a
+            assert np.abs(u_b - u_a).max() <= 1e-10 * np.abs(u_a).max()
+
+
+def test_batch_t_end(zlib):
+    probs = [polytrope_2d(n_rings=r, amplitude=1e-3, seed=3, precision=z.MIXED) for r in (10, 16)]
+    b = z.Batch(4)
+    solvers, slots = [], []
+    for (raw, mesh, scheme, u0), t_end in zip(probs, (0.01, 0.02)):
+        s = z.Solver(mesh, scheme)
+        s.set_state(u0)
+        solvers.append(s)
+        slots.append(b.add(s, t_end=t_end))
+    while b.advance(8):
+        pass
+    for slot, t_end in zip(slots, (0.01, 0.02)):
+        st = b.status(slot)
+        assert st["done"] and abs(st["t"] - t_end) <= 1e-12 * t_end
+
+
+def test_batch_autotune_keeps_results(zlib):
+    """The persistent grid size the autotuner picks does not change results."""
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=14, amplitude=1e-3, precision=z.MIXED)
+    s_tuned = z.Solver(mesh, scheme)
+    s_tuned.set_state(u0)
+    tuner = z.Batch(2)
+    slot = tuner.add(s_tuned, n_steps=1000)
+    tuner.autotune(2)
+    tuner.remove(slot)
+    u1, t1 = s_tuned.get_state()
+    s_plain = z.Solver(mesh, scheme)
+    s_plain.set_state(u1, t1)
+    s_tuned.set_state(u1, t1)
+    plain = z.Batch(2)
+    a = tuner.add(s_tuned, n_steps=5)
+    b = plain.add(s_plain, n_steps=5)
+    while tuner.advance(4):
+        pass
+    while plain.advance(4):
+        pass
+    tuner.remove(a)
+    plain.remove(b)
+    x, _ = s_tuned.get_state()
+    y, _ = s_plain.get_state()
+    assert np.array_equal(x, y)

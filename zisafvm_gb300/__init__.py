@@ -19,7 +19,7 @@ from pathlib import Path
 import numpy as np
 
 __all__ = [
-    "ZfvmError", "RawMesh", "Mesh", "Solver", "Scheme", "StencilSpec", "library_path", "load_library",
+    "ZfvmError", "RawMesh", "Mesh", "Solver", "Batch", "Scheme", "StencilSpec", "library_path", "load_library",
     "FLUX_HLLC", "FLUX_RUSANOV",
 ]
 
@@ -112,6 +112,15 @@ def load_library() -> C.CDLL:
         "zfvm_launches_per_step": [vp, C.POINTER(i32)],
         "zfvm_kernel_times": [vp, i64, C.POINTER(C.c_float)],
         "zfvm_device_bytes": [vp, C.POINTER(i64)],
+        "zfvm_batch_create": [i32, pp],
+        "zfvm_batch_destroy": [vp],
+        "zfvm_batch_add": [vp, vp, i64, C.c_double, C.POINTER(i32)],
+        "zfvm_batch_remove": [vp, i32],
+        "zfvm_batch_advance": [vp, i32, C.POINTER(i32)],
+        "zfvm_batch_advance_timed": [vp, i32, C.POINTER(C.c_float)],
+        "zfvm_batch_autotune": [vp, i32, C.POINTER(C.c_float)],
+        "zfvm_batch_slot_status": [vp, i32, dp, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)],
+        "zfvm_batch_slots": [vp, C.POINTER(i32)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -387,3 +396,52 @@ class Solver:
         n = C.c_int64()
         _check(load_library().zfvm_device_bytes(self._h, C.byref(n)))
         return n.value
+
+
+class Batch:
+    """Independent solves stepped together (one launch per phase per stage)."""
+
+    def __init__(self, max_slots: int):
+        h = C.c_void_p()
+        _check(load_library().zfvm_batch_create(max_slots, C.byref(h)))
+        self._h = h
+        self._members = {}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and _LIB is not None:
+            _LIB.zfvm_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def add(self, solver: Solver, n_steps: int = 0, t_end: float = 0.0) -> int:
+        slot = C.c_int32()
+        _check(load_library().zfvm_batch_add(self._h, solver._h, n_steps, t_end, C.byref(slot)))
+        self._members[slot.value] = solver
+        return slot.value
+
+    def remove(self, slot: int) -> Solver:
+        _check(load_library().zfvm_batch_remove(self._h, slot))
+        return self._members.pop(slot)
+
+    def advance(self, max_steps: int) -> int:
+        n = C.c_int32()
+        _check(load_library().zfvm_batch_advance(self._h, max_steps, C.byref(n)))
+        return n.value
+
+    def advance_timed(self, n_steps: int) -> float:
+        ms = C.c_float()
+        _check(load_library().zfvm_batch_advance_timed(self._h, n_steps, C.byref(ms)))
+        return float(ms.value)
+
+    def autotune(self, trial_steps: int = 4) -> float:
+        ms = C.c_float()
+        _check(load_library().zfvm_batch_autotune(self._h, trial_steps, C.byref(ms)))
+        return float(ms.value)
+
+    def status(self, slot: int) -> dict:
+        t, st, done, status = C.c_double(), C.c_int64(), C.c_int32(), C.c_int32()
+        _check(load_library().zfvm_batch_slot_status(self._h, slot, C.byref(t), C.byref(st), C.byref(done),
+                                                     C.byref(status)))
+        return {"t": t.value, "steps": st.value, "done": bool(done.value), "status": status.value}

@@ -1,0 +1,388 @@
+// Batch engine: many independent solves stepped together.
+//
+// Solvers are added to slots; slots of one kernel configuration form a group.
+// Every RK stage launches one persistent reconstruction, one face and one
+// update kernel per group; each walks the group's tile list (128 cells or
+// faces per tile, one instance per tile), so meshes of any size share the
+// launches.  Each slot keeps its own device clock: its own CFL time step, step
+// count and end time; a slot that is done stops doing work.  The step loop is
+// captured in a CUDA graph and replayed; adding or removing a slot only
+// rebuilds the small device tables and re-captures the graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "solver_obj.hpp"
+
+using namespace zfvm;
+using namespace zfvm::dev;
+
+namespace {
+
+// mode 0: open a step for every slot; mode 1: close the last step only
+__global__ void k_clock_multi(Clock *const *clocks, const double *cfl, int n, int mode) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  Clock *c = clocks[k];
+  if (c->started) {
+    c->t += c->dt;
+    c->step += 1;
+    c->started = 0;
+  }
+  if (mode == 1 || c->done) return;
+  bool fin = (c->n_steps > 0 && c->step >= c->n_steps) ||
+             (c->t_end > 0.0 && c->t_end - c->t <= 1e-12 * c->t_end) || c->status != 0;
+  if (fin) {
+    c->done = 1;
+    return;
+  }
+  double dt = c->fixed_dt > 0.0 ? c->fixed_dt : cfl[k] * __longlong_as_double((long long)c->cfl_min);
+  if (c->t_end > 0.0) dt = fmin(dt, c->t_end - c->t);
+  c->dt = dt;
+  c->cfl_min = 0x7ff0000000000000ull;
+  c->started = 1;
+}
+
+// number of slots still running
+__global__ void k_count_running(Clock *const *clocks, int n, int *running) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n && !clocks[k]->done) atomicAdd(running, 1);
+}
+
+struct GroupKey {
+  int shape, eq, src, mixed, flux, stages;
+  bool operator<(const GroupKey &o) const {
+    return std::tie(shape, eq, src, mixed, flux, stages) < std::tie(o.shape, o.eq, o.src, o.mixed, o.flux, o.stages);
+  }
+};
+
+struct Group {
+  GroupKey key;
+  std::vector<int> slots;
+  DBuf<BatchInst> inst;
+  DBuf<Tile> cell_tiles, face_tiles;
+  int n_ct = 0, n_ft = 0;
+  int grid[3] = {0, 0, 0};
+  bool tuned = false;
+};
+
+}  // namespace
+
+struct zfvm_batch {
+  int max_slots = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<zfvm_solver *> slots;
+  std::map<GroupKey, std::unique_ptr<Group>> groups;
+  DBuf<Clock *> clock_ptrs;
+  DBuf<double> cfls;
+  DBuf<int> running;
+  int n_clock = 0;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  bool dirty = true;
+  int sms = 0;
+};
+
+namespace {
+
+void launch_group_stage(zfvm_batch *b, Group &g, int stage) {
+  BatchCfg c;
+  c.eq = g.key.eq;
+  c.src = g.key.src;
+  c.mixed = g.key.mixed;
+  c.flux = g.key.flux;
+  c.grid_recon = g.grid[0];
+  c.grid_face = g.grid[1];
+  c.grid_update = g.grid[2];
+  c.stream = b->stream;
+  switch (g.key.shape) {
+    case 0: launch_batch_stage_s2o3(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
+    case 1: launch_batch_stage_s2o2(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
+    case 2: launch_batch_stage_s3o3(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
+    case 3: launch_batch_stage_s3o2(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
+  }
+  CK(cudaGetLastError());
+}
+
+void enqueue_batch_step(zfvm_batch *b) {
+  if (b->n_clock == 0) return;
+  k_clock_multi<<<(b->n_clock + 127) / 128, 128, 0, b->stream>>>(b->clock_ptrs.p, b->cfls.p, b->n_clock, 0);
+  CK(cudaGetLastError());
+  int stages = 0;
+  for (auto &kv : b->groups) stages = std::max(stages, kv.second->key.stages);
+  for (int st = 0; st < stages; ++st)
+    for (auto &kv : b->groups)
+      if (kv.second->n_ct > 0 && st < kv.second->key.stages) launch_group_stage(b, *kv.second, st);
+}
+
+// Rebuild the device tables of every group from the current slots.
+void rebuild(zfvm_batch *b) {
+  for (auto &kv : b->groups) kv.second->slots.clear();
+  std::vector<Clock *> clocks;
+  std::vector<double> cfls;
+  for (int k = 0; k < (int)b->slots.size(); ++k) {
+    zfvm_solver *s = b->slots[k];
+    if (!s) continue;
+    GroupKey key{s->shape_id, s->has_eq, s->has_src, s->mixed, s->scheme.flux == ZFVM_FLUX_HLLC ? 0 : 1,
+                 s->P.n_stages};
+    auto &g = b->groups[key];
+    if (!g) {
+      g = std::make_unique<Group>();
+      g->key = key;
+    }
+    g->slots.push_back(k);
+    clocks.push_back(s->clock.p);
+    cfls.push_back(s->P.cfl);
+  }
+  for (auto &kv : b->groups) {
+    Group &g = *kv.second;
+    std::vector<BatchInst> inst;
+    std::vector<Tile> ct, ft;
+    for (size_t j = 0; j < g.slots.size(); ++j) {
+      zfvm_solver *s = b->slots[g.slots[j]];
+      BatchInst I{};
+      I.d = s->D;
+      I.P = s->P;
+      for (int st = 0; st < 3; ++st) I.a[st] = stage_args(s, std::min(st, s->P.n_stages - 1), nullptr);
+      inst.push_back(I);
+      for (int c = 0; c < s->n_cells; c += 128) ct.push_back(Tile{(int)j, c});
+      for (int e = 0; e < s->n_edges; e += 128) ft.push_back(Tile{(int)j, e});
+    }
+    g.inst.upload(inst);
+    g.cell_tiles.upload(ct);
+    g.face_tiles.upload(ft);
+    g.n_ct = (int)ct.size();
+    g.n_ft = (int)ft.size();
+  }
+  b->clock_ptrs.upload(clocks);
+  b->cfls.upload(cfls);
+  b->n_clock = (int)clocks.size();
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->dirty = false;
+}
+
+void ensure_graph(zfvm_batch *b, int steps) {
+  if (b->dirty) rebuild(b);
+  if (b->graph && b->graph_steps == steps) return;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < steps; ++k) enqueue_batch_step(b);
+  CK(cudaStreamEndCapture(b->stream, &g));
+  CK(cudaGraphInstantiate(&b->graph, g, 0));
+  cudaGraphDestroy(g);
+  b->graph_steps = steps;
+}
+
+int running_count(zfvm_batch *b) {
+  if (b->n_clock == 0) return 0;
+  CK(cudaMemsetAsync(b->running.p, 0, sizeof(int), b->stream));
+  k_count_running<<<(b->n_clock + 127) / 128, 128, 0, b->stream>>>(b->clock_ptrs.p, b->n_clock, b->running.p);
+  int r = 0;
+  CK(cudaMemcpyAsync(&r, b->running.p, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  CK(cudaStreamSynchronize(b->stream));
+  return r;
+}
+
+int fail_cuda(const CudaError &e) { return fail(ZFVM_ECUDA, e.where + ": " + cudaGetErrorString(e.err)); }
+
+}  // namespace
+
+#define BATCH_GUARD_BEGIN try {
+#define BATCH_GUARD_END                                  \
+  }                                                      \
+  catch (const CudaError &e) {                           \
+    return fail_cuda(e);                                 \
+  }                                                      \
+  catch (const std::bad_alloc &) {                       \
+    return fail(ZFVM_ENOMEM, "host allocation failed");  \
+  }
+
+extern "C" int zfvm_batch_create(int32_t max_slots, zfvm_batch **out) {
+  if (!out || max_slots <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  auto b = std::make_unique<zfvm_batch>();
+  BATCH_GUARD_BEGIN
+  b->max_slots = max_slots;
+  b->slots.assign(max_slots, nullptr);
+  CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  b->running.alloc(1);
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, dev));
+  *out = b.release();
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+extern "C" int zfvm_batch_destroy(zfvm_batch *b) {
+  if (!b) return ZFVM_OK;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->stream) {
+    cudaStreamSynchronize(b->stream);
+    cudaStreamDestroy(b->stream);
+  }
+  delete b;
+  return ZFVM_OK;
+}
+
+extern "C" int zfvm_batch_add(zfvm_batch *b, zfvm_solver *s, int64_t n_steps, double t_end, int32_t *slot) {
+  if (!b || !s) return fail(ZFVM_EINVAL, "null argument");
+  if (n_steps <= 0 && !(t_end > 0.0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > 0");
+  BATCH_GUARD_BEGIN
+  int k = -1;
+  for (int j = 0; j < b->max_slots; ++j) {
+    if (b->slots[j] == s) return fail(ZFVM_EINVAL, "solver already in the batch");
+    if (k < 0 && !b->slots[j]) k = j;
+  }
+  if (k < 0) return fail(ZFVM_ENOMEM, "no free batch slot");
+  CK(cudaStreamSynchronize(s->stream));
+  reset_clock_for_run(s, n_steps, t_end, 0.0);
+  CK(cudaStreamSynchronize(s->stream));
+  b->slots[k] = s;
+  b->dirty = true;
+  if (slot) *slot = k;
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+extern "C" int zfvm_batch_remove(zfvm_batch *b, int32_t slot) {
+  if (!b || slot < 0 || slot >= b->max_slots || !b->slots[slot]) return fail(ZFVM_EINVAL, "bad slot");
+  BATCH_GUARD_BEGIN
+  CK(cudaStreamSynchronize(b->stream));
+  zfvm_solver *s = b->slots[slot];
+  // close the slot's last step so its clock reads the final time
+  Clock c = read_clock(s);
+  if (c.started) {
+    c.t += c.dt;
+    c.step += 1;
+    c.started = 0;
+    write_clock(s, c);
+    CK(cudaStreamSynchronize(s->stream));
+  }
+  b->slots[slot] = nullptr;
+  b->dirty = true;
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+extern "C" int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_running) {
+  if (!b || max_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  BATCH_GUARD_BEGIN
+  const int chunk = std::min(max_steps, 8);
+  ensure_graph(b, chunk);
+  int done_steps = 0;
+  while (done_steps < max_steps) {
+    CK(cudaGraphLaunch(b->graph, b->stream));
+    done_steps += chunk;
+  }
+  int r = running_count(b);
+  if (n_running) *n_running = r;
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+extern "C" int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *ms) {
+  if (!b || !ms || n_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  BATCH_GUARD_BEGIN
+  const int chunk = std::min(n_steps, 8);
+  ensure_graph(b, chunk);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaStreamSynchronize(b->stream));
+  CK(cudaEventRecord(e0, b->stream));
+  for (int k = 0; k < n_steps; k += chunk) CK(cudaGraphLaunch(b->graph, b->stream));
+  CK(cudaEventRecord(e1, b->stream));
+  CK(cudaEventSynchronize(e1));
+  CK(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+// Autotuner: time the persistent grid size of each group's kernels
+// (multiples of the SM count up to the occupancy limit, or one block per tile)
+// over `trial_steps` steps and keep the fastest.  The slots' states advance.
+extern "C" int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *best_ms) {
+  if (!b || trial_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  BATCH_GUARD_BEGIN
+  if (b->dirty) rebuild(b);
+  float overall = 0.0f;
+  for (auto &kv : b->groups) {
+    Group &g = *kv.second;
+    if (g.n_ct == 0) continue;
+    BatchCfg c{};
+    c.mixed = g.key.mixed;
+    int occ[3] = {1, 1, 1};
+    switch (g.key.shape) {
+      case 0: batch_occupancy_s2o3(c, occ); break;
+      case 1: batch_occupancy_s2o2(c, occ); break;
+      case 2: batch_occupancy_s3o3(c, occ); break;
+      case 3: batch_occupancy_s3o2(c, occ); break;
+    }
+    std::vector<std::array<int, 3>> cands;
+    cands.push_back({0, 0, 0});  // one block per tile
+    for (int m : {1, 2})
+      cands.push_back({std::max(1, occ[0] * m) * b->sms, std::max(1, occ[1] * m) * b->sms,
+                       std::max(1, occ[2] * m) * b->sms});
+    float best = 1e30f;
+    std::array<int, 3> pick = cands[0];
+    for (auto &cand : cands) {
+      for (int j = 0; j < 3; ++j) g.grid[j] = cand[j];
+      if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+      }
+      float ms = 0;
+      int32_t n = trial_steps;
+      int st = zfvm_batch_advance_timed(b, n, &ms);
+      if (st) return st;
+      if (ms < best) best = ms, pick = cand;
+    }
+    for (int j = 0; j < 3; ++j) g.grid[j] = pick[j];
+    g.tuned = true;
+    overall += best;
+  }
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (best_ms) *best_ms = overall;
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+extern "C" int zfvm_batch_slot_status(zfvm_batch *b, int32_t slot, double *t, int64_t *steps, int32_t *done,
+                                      int32_t *status) {
+  if (!b || slot < 0 || slot >= b->max_slots || !b->slots[slot]) return fail(ZFVM_EINVAL, "bad slot");
+  BATCH_GUARD_BEGIN
+  CK(cudaStreamSynchronize(b->stream));
+  Clock c = read_clock(b->slots[slot]);
+  if (t) *t = c.t + (c.started ? c.dt : 0.0);
+  if (steps) *steps = c.step + (c.started ? 1 : 0);
+  if (done) *done = c.done;
+  if (status) *status = c.status;
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+extern "C" int zfvm_batch_slots(const zfvm_batch *b, int32_t *n_active) {
+  if (!b || !n_active) return fail(ZFVM_EINVAL, "null argument");
+  int n = 0;
+  for (auto *s : b->slots) n += s != nullptr;
+  *n_active = n;
+  return ZFVM_OK;
+}

@@ -70,64 +70,10 @@ __global__ void k_soa_to_aos(const double *soa, double *aos, int n, int ld, int 
 using namespace zfvm;
 using namespace zfvm::dev;
 
-namespace {
+#include "solver_obj.hpp"
 
-struct CudaError {
-  cudaError_t err;
-  std::string where;
-};
-
-#define CK(x)                                                            \
-  do {                                                                   \
-    cudaError_t e_ = (x);                                                \
-    if (e_ != cudaSuccess) throw CudaError{e_, #x};                      \
-  } while (0)
-
-template <class T>
-struct DBuf {
-  T *p = nullptr;
-  size_t n = 0;
-  void alloc(size_t count) {
-    n = count;
-    if (count) CK(cudaMalloc((void **)&p, count * sizeof(T)));
-  }
-  void upload(const std::vector<T> &h) {
-    alloc(h.size());
-    if (n) CK(cudaMemcpy(p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice));
-  }
-  void zero(cudaStream_t s) {
-    if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
-  }
-  ~DBuf() {
-    if (p) cudaFree(p);
-  }
-};
-
-}  // namespace
-
-struct zfvm_solver {
-  zfvm_mesh *mesh = nullptr;
-  zfvm_scheme_desc scheme{};
-  int nd = 2, nv = 4, nf = 3, nqf = 2, nqc = 3, ld = 0, lde = 0;
-  int n_cells = 0, n_edges = 0;
-  int shape_id = -1;
-  cudaStream_t stream = nullptr;
-  Params P{};
-  DevData D{};
-  // device buffers
-  DBuf<uint8_t> flags, bloc, fkL, fkR, factive;
-  DBuf<int> l2g, cface, fL, fR, src_map;
-  DBuf<double> pinv, center, inv_len, mom, inv_vol, r_eff, fqx, fqw, frame, farea;
-  DBuf<float> pinv32, fv32, frame32, xfq32, xcq32, mom32, wg32, g32, mL32, mR32, src32, kbuf32;
-  DBuf<double> gphi_w;
-  DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
-  DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos, dev0;
-  DBuf<Clock> clock;
-  bool has_src = false, has_eq = false, mixed = false;
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
-  int64_t device_bytes = 0;
-};
+using zfvm::CudaError;
+using zfvm::DBuf;
 
 namespace {
 
@@ -141,6 +87,8 @@ bool matches(const ShapeKey &k) {
          k.CB == S::CB && k.nqf == S::NQF && k.nqc == S::NQC;
 }
 
+
+}  // namespace
 
 StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   StageArgs a{};
@@ -165,6 +113,8 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   for (int j = 0; j < 4; ++j) a.coef[j] = last ? s->P.b[j] : (stage + 1 < 4 ? s->P.a[stage + 1][j] : 0.0);
   return a;
 }
+
+namespace {
 
 LaunchCfg launch_cfg(zfvm_solver *s) {
   return LaunchCfg{s->n_cells, s->n_edges,  s->has_eq, s->has_src, s->mixed,
@@ -219,6 +169,8 @@ int status_to_code(int st, std::string &msg) {
   return ZFVM_OK;
 }
 
+}  // namespace
+
 Clock read_clock(zfvm_solver *s) {
   Clock c;
   CK(cudaMemcpyAsync(&c, s->clock.p, sizeof(Clock), cudaMemcpyDeviceToHost, s->stream));
@@ -229,6 +181,8 @@ Clock read_clock(zfvm_solver *s) {
 void write_clock(zfvm_solver *s, const Clock &c) {
   CK(cudaMemcpyAsync(s->clock.p, &c, sizeof(Clock), cudaMemcpyHostToDevice, s->stream));
 }
+
+namespace {
 
 int build_solver(zfvm_solver *s) {
   zfvm_mesh *m = s->mesh;
@@ -601,6 +555,8 @@ int cuda_fail(const CudaError &e) {
   return fail(ZFVM_ECUDA, e.where + ": " + cudaGetErrorString(e.err));
 }
 
+}  // namespace
+
 void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt) {
   Clock c = read_clock(s);
   c.done = 0;
@@ -611,6 +567,8 @@ void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double f
   c.fixed_dt = fixed_dt;
   write_clock(s, c);
 }
+
+namespace {
 
 void build_graph(zfvm_solver *s, int steps) {
   if (s->graph && s->graph_steps == steps) return;

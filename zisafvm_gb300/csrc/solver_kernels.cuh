@@ -276,10 +276,9 @@ __device__ __forceinline__ void set_status(Clock *c, int bits) { atomicOr(&c->st
 
 // --------------------------------------------------------- reconstruction
 template <class S, int EQ, int SRC, bool MIXED>
-__global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Params P, StageArgs a) {
+__device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, const StageArgs &a, const int i) {
   using R = std::conditional_t<MIXED, float, double>;
   constexpr int NV = S::NV, ND = S::ND, NF = S::NF, NC = S::NC;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.n_cells) return;
   if (d.clock->done) return;
   const uint8_t fl = d.flags[i];
@@ -630,6 +629,11 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
   }
 }
 
+template <class S, int EQ, int SRC, bool MIXED>
+__global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Params P, StageArgs a) {
+  recon_cell<S, EQ, SRC, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ------------------------------------------------------------- face flux
 template <int NV, int ND, class T>
 __device__ __forceinline__ void to_face(const T *u, const double *fr, int lde, int e, T *w) {
@@ -715,9 +719,8 @@ __device__ __forceinline__ void mixed_base(const DevData &d, const StageArgs &a,
 }
 
 template <class S, int FLUX, int EQ, bool MIXED>
-__global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params P, StageArgs a) {
+__device__ __forceinline__ void face_one(const DevData &d, const Params &P, const StageArgs &a, const int e) {
   constexpr int NV = S::NV, ND = S::ND;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= d.n_edges) return;
   if (d.clock->done) return;
   if (!d.factive[e]) return;
@@ -918,6 +921,11 @@ __global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params
   for (int v = 0; v < NV; ++v) a.nf[v * lde + e] = nf[v];
 }
 
+template <class S, int FLUX, int EQ, bool MIXED>
+__global__ void __launch_bounds__(128) k_face_flux(const DevData d, const Params P, StageArgs a) {
+  face_one<S, FLUX, EQ, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // ---------------------------------------------------------------- update
 template <int NV>
 __device__ __forceinline__ double cfl_candidate(const double *u, double gamma, double r) {
@@ -955,10 +963,11 @@ __device__ __forceinline__ void block_min_to_clock(double cand, Clock *clock) {
   }
 }
 
+// One cell of the stage update; returns the CFL candidate of the new state at
+// the last stage (+inf otherwise).
 template <class S, bool MIXED>
-__global__ void __launch_bounds__(128) k_update(const DevData d, const Params P, StageArgs a) {
+__device__ __forceinline__ double update_cell(const DevData &d, const Params &P, const StageArgs &a, const int i) {
   constexpr int NV = S::NV, NF = S::NF, ND = S::ND;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool last = a.stage == P.n_stages - 1;
   double cand = INFINITY;
   if (!d.clock->done && i < d.n_cells && (d.flags[i] & kInterior)) {
@@ -1053,7 +1062,13 @@ __global__ void __launch_bounds__(128) k_update(const DevData d, const Params P,
       }
     }
   }
-  if (last && !a.tend_out) block_min_to_clock(cand, d.clock);
+  return cand;
+}
+
+template <class S, bool MIXED>
+__global__ void __launch_bounds__(128) k_update(const DevData d, const Params P, StageArgs a) {
+  const double cand = update_cell<S, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
+  if (a.stage == P.n_stages - 1 && !a.tend_out) block_min_to_clock(cand, d.clock);
 }
 
 template <class S>
@@ -1068,6 +1083,116 @@ __global__ void __launch_bounds__(128) k_cfl(const DevData d, const Params P, co
     cand = cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
   }
   block_min_to_clock(cand, d.clock);
+}
+
+// ------------------------------------------------- multi-instance kernels
+// A batch packs many independent solves (meshes of any size) into one launch
+// per phase: a persistent grid walks a list of 128-item tiles, each tile
+// belonging to one instance, whose argument structs live in device memory.
+// Every instance keeps its own clock (its own CFL time step and end time).
+struct BatchInst {
+  DevData d;
+  Params P;
+  StageArgs a[3];
+};
+
+struct Tile {
+  int slot, begin;
+};
+
+template <class S, int EQ, int SRC, bool MIXED>
+__global__ void __launch_bounds__(128) km_reconstruct(const BatchInst *__restrict__ inst,
+                                                      const Tile *__restrict__ tiles, int n_tiles, int stage) {
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const Tile tl = tiles[t];
+    const BatchInst &I = inst[tl.slot];
+    recon_cell<S, EQ, SRC, MIXED>(I.d, I.P, I.a[stage], tl.begin + threadIdx.x);
+  }
+}
+
+template <class S, int FLUX, int EQ, bool MIXED>
+__global__ void __launch_bounds__(128) km_face_flux(const BatchInst *__restrict__ inst,
+                                                    const Tile *__restrict__ tiles, int n_tiles, int stage) {
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const Tile tl = tiles[t];
+    const BatchInst &I = inst[tl.slot];
+    face_one<S, FLUX, EQ, MIXED>(I.d, I.P, I.a[stage], tl.begin + threadIdx.x);
+  }
+}
+
+template <class S, bool MIXED>
+__global__ void __launch_bounds__(128) km_update(const BatchInst *__restrict__ inst, const Tile *__restrict__ tiles,
+                                                 int n_tiles, int stage) {
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const Tile tl = tiles[t];
+    const BatchInst &I = inst[tl.slot];
+    const double cand = update_cell<S, MIXED>(I.d, I.P, I.a[stage], tl.begin + threadIdx.x);
+    // block-uniform: the whole tile belongs to one instance
+    if (stage == I.P.n_stages - 1) block_min_to_clock(cand, I.d.clock);
+    __syncthreads();
+  }
+}
+
+struct BatchCfg {
+  bool eq, src, mixed;
+  int flux;
+  int grid_recon, grid_face, grid_update;  // persistent grid sizes (autotuned)
+  cudaStream_t stream;
+};
+
+template <class S, bool MIXED>
+void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_ct, const Tile *face_tiles, int n_ft,
+                          int stage, const BatchCfg &c) {
+  const int gr = c.grid_recon > 0 ? c.grid_recon : n_ct, gf = c.grid_face > 0 ? c.grid_face : n_ft,
+            gu = c.grid_update > 0 ? c.grid_update : n_ct;
+  if (c.eq && c.src)
+    km_reconstruct<S, 1, 1, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+  else if (c.eq)
+    km_reconstruct<S, 1, 0, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+  else if (c.src)
+    km_reconstruct<S, 0, 1, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+  else
+    km_reconstruct<S, 0, 0, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+  if (c.flux == 0) {
+    if (c.eq)
+      km_face_flux<S, 0, 1, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+    else
+      km_face_flux<S, 0, 0, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+  } else {
+    if (c.eq)
+      km_face_flux<S, 1, 1, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+    else
+      km_face_flux<S, 1, 0, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+  }
+  km_update<S, MIXED><<<gu, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+}
+
+template <class S>
+void launch_batch_stage_t(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft, int stage,
+                          const BatchCfg &c) {
+  if (c.mixed)
+    launch_batch_stage_p<S, true>(inst, ct, n_ct, ft, n_ft, stage, c);
+  else
+    launch_batch_stage_p<S, false>(inst, ct, n_ct, ft, n_ft, stage, c);
+}
+
+// Occupancy-limited block counts of the three batch kernels (for the autotuner).
+template <class S>
+void batch_occupancy_t(const BatchCfg &c, int *blocks_per_sm) {
+  auto occ = [](const void *k) {
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 128, 0);
+    return b;
+  };
+  if (c.mixed) {
+    blocks_per_sm[0] = occ((const void *)km_reconstruct<S, 1, 1, true>);
+    blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, true>);
+    blocks_per_sm[2] = occ((const void *)km_update<S, true>);
+  } else {
+    blocks_per_sm[0] = occ((const void *)km_reconstruct<S, 1, 1, false>);
+    blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, false>);
+    blocks_per_sm[2] = occ((const void *)km_update<S, false>);
+  }
 }
 
 // ------------------------------------------------------------ launching
@@ -1134,14 +1259,22 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
 
 #define ZFVM_DECLARE_SHAPE(name)                                                                  \
   void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c); \
-  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c);
+  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c); \
+  void launch_batch_stage_##name(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft,  \
+                                 int stage, const BatchCfg &c);                                              \
+  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm);
 #define ZFVM_DEFINE_SHAPE(name, S)                                                                \
   void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) { \
     launch_stage_t<S>(D, P, a, c);                                                                \
   }                                                                                               \
   void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) { \
     launch_cfl_t<S>(D, P, u, c);                                                                  \
-  }
+  }                                                                                               \
+  void launch_batch_stage_##name(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft,  \
+                                 int stage, const BatchCfg &c) {                                             \
+    launch_batch_stage_t<S>(inst, ct, n_ct, ft, n_ft, stage, c);                                             \
+  }                                                                                                          \
+  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm) { batch_occupancy_t<S>(c, blocks_per_sm); }
 
 ZFVM_DECLARE_SHAPE(s2o3)
 ZFVM_DECLARE_SHAPE(s2o2)

@@ -1,0 +1,94 @@
+// Host-side solver object behind the C ABI: device buffers, the kernels'
+// argument structs and the captured step graph.  Shared by the single-solver
+// entry points (solver.cu) and the batch engine (batch.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "mesh_obj.hpp"
+#include "solver_kernels.cuh"
+
+namespace zfvm {
+
+struct CudaError {
+  cudaError_t err;
+  std::string where;
+};
+
+#define CK(x)                                                            \
+  do {                                                                   \
+    cudaError_t e_ = (x);                                                \
+    if (e_ != cudaSuccess) throw CudaError{e_, #x};                      \
+  } while (0)
+
+template <class T>
+struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  DBuf(DBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr, o.n = 0; }
+  DBuf &operator=(DBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p, n = o.n;
+      o.p = nullptr, o.n = 0;
+    }
+    return *this;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    release();
+    n = count;
+    if (count) CK(cudaMalloc((void **)&p, count * sizeof(T)));
+  }
+  void upload(const std::vector<T> &h) {
+    alloc(h.size());
+    if (n) CK(cudaMemcpy(p, h.data(), n * sizeof(T), cudaMemcpyHostToDevice));
+  }
+  void zero(cudaStream_t s) {
+    if (n) CK(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+  }
+  ~DBuf() { release(); }
+};
+
+}  // namespace zfvm
+
+struct zfvm_solver {
+  zfvm_mesh *mesh = nullptr;
+  zfvm_scheme_desc scheme{};
+  int nd = 2, nv = 4, nf = 3, nqf = 2, nqc = 3, ld = 0, lde = 0;
+  int n_cells = 0, n_edges = 0;
+  int shape_id = -1;
+  cudaStream_t stream = nullptr;
+  zfvm::dev::Params P{};
+  zfvm::dev::DevData D{};
+  // device buffers
+  zfvm::DBuf<uint8_t> flags, bloc, fkL, fkR, factive;
+  zfvm::DBuf<int> l2g, cface, fL, fR, src_map;
+  zfvm::DBuf<double> pinv, center, inv_len, mom, inv_vol, r_eff, fqx, fqw, frame, farea;
+  zfvm::DBuf<float> pinv32, fv32, frame32, xfq32, xcq32, mom32, wg32, g32, mL32, mR32, src32, kbuf32;
+  zfvm::DBuf<double> gphi_w;
+  zfvm::DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
+  zfvm::DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos, dev0;
+  zfvm::DBuf<zfvm::dev::Clock> clock;
+  bool has_src = false, has_eq = false, mixed = false;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+  int64_t device_bytes = 0;
+};
+
+
+// helpers shared with the batch engine (solver.cu)
+zfvm::dev::StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out);
+zfvm::dev::Clock read_clock(zfvm_solver *s);
+void write_clock(zfvm_solver *s, const zfvm::dev::Clock &c);
+void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt);
