@@ -153,6 +153,28 @@ int zfvm_get_state(zfvm_solver *s, double *cvars, double *t);
  * Ghost-cell rows are zero. */
 int zfvm_rate_of_change(zfvm_solver *s, double *tendency);
 
+/* Size of the fixed device scratch of zfvm_rate_of_change_noalloc: 16 MiB,
+ * present on every device that loads the library until the process exits. */
+#define ZFVM_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* Same result as zfvm_rate_of_change, for callers that must not allocate device
+ * memory inside their loop: an application whose own pool allocator has
+ * reserved the device memory it may use, or a time-critical loop that cannot
+ * take the device-wide wait of cudaFree (zfvm_rate_of_change allocates and
+ * frees a small buffer on every call).  This call allocates nothing: its stage
+ * scratch is a fixed array of ZFVM_NOALLOC_SCRATCH_BYTES inside the library.
+ * This entry point has no counterpart in the reference.
+ *  - Limit: about 40 000 cells for third-order triangles and 20 000 for
+ *    third-order tetrahedra; a larger solver fails with ZFVM_EINVAL and a
+ *    message giving the bytes it needs.
+ *  - The first call on a device looks up the array's device address; make that
+ *    first call before any stream capture on that device.
+ *  - Every call on a device shares the one array.  Calls return only when their
+ *    work is done, so calls from one thread never overlap; calls from several
+ *    threads must be serialised by the caller, or they race on the GPU.
+ *  - The solver's device must be current, as for the other entry points. */
+int zfvm_rate_of_change_noalloc(zfvm_solver *s, double *tendency);
+
 /* CFL time step of the current state (LocalCFL, local_cfl_condition_impl.hpp:24-40). */
 int zfvm_cfl_dt(zfvm_solver *s, double *dt);
 

@@ -153,6 +153,8 @@ void enqueue_step(zfvm_solver *s) {
   }
 }
 
+}  // namespace
+
 int status_to_code(int st, std::string &msg) {
   if (st & kStNewton) {
     msg = "local equilibrium solve is not converging";
@@ -168,8 +170,6 @@ int status_to_code(int st, std::string &msg) {
   }
   return ZFVM_OK;
 }
-
-}  // namespace
 
 Clock read_clock(zfvm_solver *s) {
   Clock c;

@@ -92,3 +92,5 @@ zfvm::dev::StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out);
 zfvm::dev::Clock read_clock(zfvm_solver *s);
 void write_clock(zfvm_solver *s, const zfvm::dev::Clock &c);
 void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt);
+// ZFVM_* status and message for the device status bits of a Clock
+int status_to_code(int st, std::string &msg);
