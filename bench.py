@@ -1,21 +1,28 @@
 """Benchmark: cell-stage updates/s of the rate-of-change + SSP-RK step loop.
 
-Default workload: the well-balanced 2D polytrope (gamma = 2, K = 1,
+Default workload (C2): the well-balanced 2D polytrope (gamma = 2, K = 1,
 phi = r^2 / 2 on the unit disk, ~200k jittered Delaunay triangles, CWENO-AO
-order 3, HLLC, SSP3, CFL 0.45), seeded synthetic data.  One "step" is one SSP3
-time step over the whole mesh: 3 cell-stage updates per cell.
+order 3, HLLC, SSP3, CFL 0.45, perturbation 1e-4), seeded synthetic data.  One
+"step" is one SSP3 time step over the whole mesh: 3 cell-stage updates per cell.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c2|c1|c3|c2-small] [--precision fp64|mixed]
+                  [--workload c2|c1|c3|c3o2|c4|...] [--precision mixed|fp64]
 
-value    whole-job cell-stage updates/s, state resident in HBM, CUDA events on
-         the solver stream around K graph-replayed steps (max over ranks).
+value    whole-job cell-stage updates/s of the --precision form (default: the
+         mixed FP32/FP64 form), state resident in HBM, CUDA events on the
+         solver stream around K graph-replayed steps (max over ranks).  With
+         the mixed form the plain FP64 form is timed the same way on the same
+         mesh ("fp64"), and the mixed form's error against it and its
+         well-balanced residual are reported.
+c4       256 solves of uneven size batched into one persistent launch per
+         phase per RK stage (autotuned grids), against the FP64 form run one
+         solve at a time on the same instances.
 e2e      the same metric through the public API with host buffers: every step
          copies the state from pinned host memory to the device, advances one
          CFL step and reads the new state back.
 roofline dominant kernel (the reconstruction kernel): algorithmic bytes per
          launch / its event-timed launch duration, against the measured HBM
-         copy bandwidth; FP64 issue rate reported beside it.
+         copy bandwidth; the FP64 pipe bounds these kernels first.
 Multi-GPU: replicas only -- every rank solves its own copy (no data exchange).
 """
 from __future__ import annotations
@@ -44,8 +51,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=160)
     ap.add_argument("--warmup", type=int, default=16)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c2-small", "c1-small"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--workload", default="c2",
+                    choices=["c2", "c1", "c3", "c3o2", "c4", "c2-small", "c1-small", "c3-small", "c4-small"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
+                    help="form whose throughput is `value`; with mixed the FP64 form is timed beside it")
     ap.add_argument("--profile", action="store_true",
                     help="timed loop only (no CPU baseline, no e2e loop): the command profiled with ncu")
     return ap.parse_args()
@@ -76,6 +85,13 @@ def workload(name: str, precision: str):
     elif name == "c1-small":
         raw, mesh, scheme, u0 = vortex_2d(n=48, halo=3)
         desc = {"workload": "C1 periodic isentropic vortex (small)", "cells": mesh.info["n_interior_cells"]}
+    elif name == "c3o2":
+        raw, mesh, scheme, u0 = vortex_tube_3d(n=70, order=2)
+        desc = {"workload": "C3 tetrahedral vortex tube, order 2", "cells": mesh.n_cells,
+                "scheme": "CWENO-AO o2, HLLC, SSP3, CFL 0.3"}
+    elif name == "c3-small":
+        raw, mesh, scheme, u0 = vortex_tube_3d(n=24, order=3)
+        desc = {"workload": "C3 tetrahedral vortex tube (small)", "cells": mesh.n_cells}
     else:
         raw, mesh, scheme, u0 = vortex_tube_3d(n=70, order=3)
         desc = {"workload": "C3 tetrahedral vortex tube", "cells": mesh.n_cells,
@@ -84,13 +100,19 @@ def workload(name: str, precision: str):
     return raw, mesh, scheme, u0, desc
 
 
-def algorithmic_bytes_per_cell_stage(mesh, scheme, wdt=8) -> int:
+def algorithmic_bytes_per_cell_stage(mesh, scheme, mixed: bool = False) -> int:
     """Compulsory unique HBM traffic of one cell through one stage of the
-    reconstruction kernel (per cell, from the array sizes the kernel reads and
-    writes): stage state (nv words), pseudo-inverse, stencil indices, one-sided
-    local indices, geometry (centre, 1/length, moments), face ids, the face-point
-    values it writes and, with well-balancing, potentials at its quadrature
-    points and the equilibrium it stores."""
+    reconstruction kernel, from the array sizes the kernel reads and writes.
+
+    FP64 form: stage state (nv words), pseudo-inverse (8-byte words), stencil
+    indices, one-sided local indices, geometry (centre, 1/length, moments), face
+    ids, face quadrature points (shared by two cells), the face-point values it
+    writes and, with well-balancing, the potential and weights at its quadrature
+    points and the equilibrium it stores; with gravity the source it writes.
+    Mixed form: the pseudo-inverse, moments and scaled quadrature offsets are
+    FP32 per cell, the face-point values are written in FP32 beside the FP64
+    cell-average deviation, and the gamma = 2 equilibrium needs <phi> and
+    var(phi) per cell instead of the quadrature-point arrays."""
     nd = mesh.info["n_dims"]
     nv = nd + 2
     nf = nd + 1
@@ -103,16 +125,27 @@ def algorithmic_bytes_per_cell_stage(mesh, scheme, wdt=8) -> int:
     MAXL = R0 + 1 + NB * RB
     NC = max(C0, CB)
     b = nv * 8                      # own state (neighbour states hit L2: SFC order)
-    b += NP * wdt                   # pseudo-inverse
     b += MAXL * 4 + NB * RB         # l2g + one-sided local indices
-    b += (nd + 1 + NC) * 8 + nf * 4  # centre, 1/length, moments, face ids
-    b += nf * nqf * nd * 8 / 2      # face quadrature points (shared by two cells)
-    b += nf * nqf * nv * 8          # face-point values written
-    if scheme.equilibrium:
-        b += nqc * 8 * 2 + nqc * nd * 8 * 2 + 3 * 8   # phi, weights, x, grad phi, equilibrium out
-        b += nf * nqf * 8 / 2                          # phi at face points
-    if scheme.gravity:
-        b += nv * 8                                    # source written
+    b += nf * 4                     # face ids
+    if not mixed:
+        b += NP * 8                     # pseudo-inverse
+        b += (nd + 1 + NC) * 8          # centre, 1/length, moments
+        b += nf * nqf * nd * 8 / 2      # face quadrature points (shared by two cells)
+        b += nf * nqf * nv * 8          # face-point values written
+        if scheme.equilibrium:
+            b += nqc * 8 * 2 + nqc * nd * 8 * 2 + 3 * 8   # phi, weights, x, grad phi, equilibrium out
+            b += nf * nqf * 8 / 2                          # phi at face points
+        if scheme.gravity:
+            b += nv * 8                                    # source written
+    else:
+        b += NP * 4                     # pseudo-inverse (FP32)
+        b += NC * 4                     # moments (FP32)
+        b += nf * nqf * nd * 4          # scaled face-point offsets (FP32, per cell)
+        b += nf * nqf * nv * 4 + nv * 8  # face-point values (FP32) + deviation (FP64) written
+        if scheme.equilibrium:
+            b += 3 * 8 + 4 * 8          # phi at the reference point, <phi>, var(phi); equilibrium out
+        if scheme.gravity:
+            b += nqc * nd * 4 * 2 + nd * 8 + 8 + nv * 4   # offsets, w grad phi, sum, 1/vol, source out
     return int(b)
 
 
@@ -199,24 +232,28 @@ def cpu_baseline(raw, mesh, scheme, u0, desc, budget_s=20.0):
                                       f"with the oracle's OpenMP loops on {threads} threads"}
 
 
+def reference_sample(workload_name: str):
+    """A bounded sample of the workload for the CPU arm: the same scheme on a
+    smaller mesh of the same family."""
+    from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+    if workload_name.startswith("c1"):
+        raw, mesh, scheme, u0 = vortex_2d(n=48, halo=3)
+        return raw, mesh, scheme, u0, mesh.info["n_interior_cells"], "C1 periodic isentropic vortex"
+    if workload_name.startswith("c3"):
+        raw, mesh, scheme, u0 = vortex_tube_3d(n=12, order=2 if workload_name == "c3o2" else 3)
+        return raw, mesh, scheme, u0, mesh.n_cells, "C3 tetrahedral vortex tube"
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=60, amplitude=1e-4)
+    name = "C4 polytrope ensemble" if workload_name.startswith("c4") else "C2 well-balanced polytrope disk"
+    return raw, mesh, scheme, u0, mesh.n_cells, name
+
+
 def run_reference(args, rank, world):
     """The reference's CPU implementation of the path (its oracle restatement;
     the reference cannot be built here) timed on the host cores."""
     if rank != 0:
         return
-    import zisafvm_gb300 as z  # set-up only (host code)
     from oracle import pyoracle
-    from problems import polytrope_2d, vortex_2d
-    # bounded per-step sample of the same workload: the same scheme on a smaller
-    # mesh of the same family, one SSP3 step per timed step
-    if args.workload.startswith("c1"):
-        raw, mesh, scheme, u0 = vortex_2d(n=48, halo=3)
-        cells = mesh.info["n_interior_cells"]
-        wl = "C1 periodic isentropic vortex"
-    else:
-        raw, mesh, scheme, u0 = polytrope_2d(n_rings=60, amplitude=1e-4)
-        cells = mesh.n_cells
-        wl = "C2 well-balanced polytrope disk"
+    raw, mesh, scheme, u0, cells, wl = reference_sample(args.workload)
     threads = os.cpu_count() or 1
     o = pyoracle.Oracle(raw, mesh.stencils(), scheme.oracle_vector(), quad=mesh.quad, threads=threads)
     dt = o.cfl_dt(u0)
@@ -228,17 +265,309 @@ def run_reference(args, rank, world):
         u = o.step(u, dt)
     el = time.perf_counter() - t0
     value = cells * 3 * args.steps / el
-    line = {"metric": "cell-stage updates/s", "value": value, "unit": "cell-stage updates/s", "n_gpus": world,
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "impl": "reference",
             "config": {"workload": wl, "cells_per_step_sample": cells, "precision": "fp64"},
-            "cpu_baseline": {"value": value, "unit": "cell-stage updates/s", "cores": threads, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"each step: one SSP3 step of a {cells}-cell mesh of the same workload "
                                        f"family, oracle OpenMP loops on {threads} threads"},
-            "e2e": {"value": value, "unit": "cell-stage updates/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+METRIC = "cell-stage updates/s, FP64 vs mixed-batched at \u22641e-6 L1 error; p50/p99 latency"
+UNIT = "cell-stage updates/s"
+
+
+def roofline_block(mesh, scheme, kt: dict, mixed: bool, workload_name: str, n_cells_launch: int):
+    """HBM roofline of the reconstruction kernel (the dominant launch): the
+    algorithmic bytes of one launch over its event-timed duration."""
+    b_cell = algorithmic_bytes_per_cell_stage(mesh, scheme, mixed)
+    bytes_launch = b_cell * n_cells_launch
+    achieved = bytes_launch / (kt["reconstruct"] * 1e-3) / 1e9
+    hbm, peak_kind = measured_peaks()
+    traffic = profiles_traffic("k_reconstruct", workload_name, "mixed" if mixed else "fp64")
+    return {"bound": "hbm", "kernel": "k_reconstruct", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_cell_stage": b_cell,
+            "bytes_per_launch": bytes_launch, "traffic": traffic, "kernel_ms": kt,
+            "fp64_pipe_note": "the FP64 pipe (1.25 TFLOP/s measured) bounds these kernels before HBM does"}
+
+
+def pinned(shape):
+    import numpy as np
+    try:
+        import torch
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        return np.empty(shape)
+
+
+def e2e_single(solver, mesh, u0, steps, pg):
+    """Public-API loop with host buffers: upload the state from pinned memory,
+    advance one CFL step, read the new state back."""
+    host, host_out = pinned((mesh.n_cells, 5)), pinned((mesh.n_cells, 5))
+    solver.set_state(u0)
+    solver.advance(n_steps=1)
+    state, _ = solver.get_state()
+    host[:] = state
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        solver.set_state(host)
+        solver.advance(n_steps=1)
+        solver.get_state(out=host_out)
+        host, host_out = host_out, host
+    return time.perf_counter() - t0
+
+
+def max_over_ranks(pg, x: float) -> float:
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def run_single_mesh(args, rank, world, local, pg):
+    import dataclasses
+
+    import numpy as np
+    import zisafvm_gb300 as z
+    raw, mesh, scheme, u0, desc = workload(args.workload, args.precision)
+    mixed = args.precision == "mixed"
+    solver = z.Solver(mesh, scheme)
+    solver.set_state(u0)
+    cells = desc["cells"]
+    stages = scheme.rk_stages
+
+    # warm-up, then K graph-replayed steps timed with CUDA events
+    if args.warmup:
+        solver.advance_timed(args.warmup)
+    if pg:
+        pg.barrier()
+    with ClockSampler(local) as clk:
+        ms = solver.advance_timed(args.steps)
+    ms = max_over_ranks(pg, ms)
+    value = world * cells * stages * args.steps / (ms * 1e-3)
+
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms / args.steps,
+                              "config": desc, "profile_run": True}), flush=True)
+        return
+
+    kt = solver.kernel_times(min(args.steps, 32))
+    roof = roofline_block(mesh, scheme, kt, mixed, args.workload, mesh.n_cells)
+    e2e_steps = max(4, min(args.steps, 64))
+    e2e_s = max_over_ranks(pg, e2e_single(solver, mesh, u0, e2e_steps, pg))
+    e2e_value = world * cells * stages * e2e_steps / e2e_s
+    io_bytes = mesh.n_cells * 5 * 8
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
+        "data": "synthetic (seeded mesh and initial data)",
+        "config": {**desc, "precision": args.precision, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 for c2/c3 (state, operators and face data > 129 MB)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+                "path": "Solver.set_state / advance(1) / get_state with pinned host buffers"},
+        "roofline": roof,
+        "gpu_launches": solver.launches_per_step() * args.steps,
+        "clocks": clk.summary(),
+    }
+    if mixed:
+        # the plain FP64 form on the same mesh and data, timed the same way
+        s64 = z.Solver(mesh, dataclasses.replace(scheme, precision=z.FP64))
+        s64.set_state(u0)
+        if args.warmup:
+            s64.advance_timed(args.warmup)
+        ms64 = max_over_ranks(pg, s64.advance_timed(args.steps))
+        v64 = world * cells * stages * args.steps / (ms64 * 1e-3)
+        kt64 = s64.kernel_times(min(args.steps, 32))
+        line["fp64"] = {"value": v64, "ms_per_step": ms64 / args.steps,
+                        "roofline": roofline_block(mesh, dataclasses.replace(scheme, precision=z.FP64), kt64,
+                                                   False, args.workload, mesh.n_cells)}
+        line["mixed_over_fp64"] = value / v64
+        # error of the mixed form against the FP64 form after the same steps
+        from metrics import perturbation_rel_l1, state_rel_l1
+        s64.set_state(u0)
+        s32 = z.Solver(mesh, scheme)
+        s32.set_state(u0)
+        n_cmp = min(args.steps, 100)
+        s64.advance(n_steps=n_cmp)
+        s32.advance(n_steps=n_cmp)
+        u64, _ = s64.get_state()
+        u32, _ = s32.get_state()
+        mask = raw.ghost == 0 if raw.ghost is not None else None
+        line["error_vs_fp64"] = {"steps": n_cmp, "state_rel_l1": state_rel_l1(u32, u64, mask),
+                                 "perturbation_rel_l1": perturbation_rel_l1(u32, u64, u0, mask)}
+        if scheme.equilibrium:
+            line["well_balanced"] = well_balanced_residual(z, mesh, scheme, n_cmp)
+    if rank == 0:
+        try:
+            line["cpu_baseline"] = cpu_baseline(raw, mesh, scheme, u0, desc)
+        except Exception as exc:  # the baseline must not hide the GPU number
+            line["cpu_baseline"] = {"error": str(exc)}
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+
+
+def well_balanced_residual(z, mesh, scheme, steps: int) -> dict:
+    """max |du/dt| of the unperturbed equilibrium and its relative drift after
+    `steps` steps (rho and E), in the given form."""
+    import numpy as np
+    u_eq = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=0.0)
+    s_eq = z.Solver(mesh, scheme)
+    s_eq.set_state(u_eq)
+    res = float(np.abs(s_eq.rate_of_change()).max())
+    s_eq.advance(n_steps=steps)
+    u_end, _ = s_eq.get_state()
+    cols = [0, 4]  # rho and E (the momenta of the equilibrium are zero)
+    drift = float((np.abs(u_end - u_eq)[:, cols].max(axis=0) / np.abs(u_eq)[:, cols].max(axis=0)).max())
+    return {"max_abs_dudt": res, "rel_drift": drift, "steps": steps}
+
+
+def run_ensemble(args, rank, world, local, pg):
+    """C4: 256 independent well-balanced polytrope solves of uneven size in one
+    batch (mixed form, one persistent launch per phase per RK stage, grids
+    picked by the autotuner), against the plain FP64 form run one solve at a
+    time on the same instances."""
+    import dataclasses
+
+    import numpy as np
+    import zisafvm_gb300 as z
+    from metrics import perturbation_rel_l1, state_rel_l1
+    from problems import ensemble_c4
+    n_inst = 256 if args.workload == "c4" else 16
+    t_setup = time.perf_counter()
+    inst = ensemble_c4(n_inst, n_max=200000 if args.workload == "c4" else 40000, seed=2024 + 7919 * rank)
+    t_setup = time.perf_counter() - t_setup
+    total_cells = sum(m.n_cells for _, m, _, _ in inst)
+    stages = 3
+    batch = z.Batch(n_inst)
+    solvers = []
+    for raw, mesh, scheme, u0 in inst:
+        s = z.Solver(mesh, scheme)
+        s.set_state(u0)
+        batch.add(s, n_steps=1 << 40)
+        solvers.append(s)
+    t_tune = time.perf_counter()
+    batch.autotune(trial_steps=4)
+    t_tune = time.perf_counter() - t_tune
+    if args.warmup:
+        batch.advance_timed(args.warmup)
+    if pg:
+        pg.barrier()
+    with ClockSampler(local) as clk:
+        ms = batch.advance_timed(args.steps)
+    ms = max_over_ranks(pg, ms)
+    value = world * total_cells * stages * args.steps / (ms * 1e-3)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms / args.steps,
+                              "config": {"workload": "C4", "instances": n_inst}, "profile_run": True}), flush=True)
+        return
+    kt = batch.kernel_times(min(args.steps, 16))
+    roof = roofline_block(inst[0][1], inst[0][2], kt, True, args.workload, total_cells)
+    roof["kernel"] = "km_reconstruct"
+
+    # end to end: every step uploads all states from pinned host memory, advances
+    # the batch one step and reads every state back
+    hosts = [pinned((m.n_cells, 5)) for _, m, _, _ in inst]
+    for h, s in zip(hosts, solvers):
+        s.get_state(out=h)
+    e2e_steps = max(3, min(args.steps, 16))
+    if pg:
+        pg.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for h, s in zip(hosts, solvers):
+            s.set_state(h)
+        batch.advance(1)
+        for h, s in zip(hosts, solvers):
+            s.get_state(out=h)
+    e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_value = world * total_cells * stages * e2e_steps / e2e_s
+    io_bytes = total_cells * 5 * 8
+    launches = 1 + stages * 3   # clock + three persistent kernels per stage, one group
+    batch.close()
+    del solvers
+
+    # plain FP64 form, one solve at a time, same steps per instance
+    k64 = max(3, min(args.steps, 24))
+    ms64 = 0.0
+    for raw, mesh, scheme, u0 in inst:
+        s64 = z.Solver(mesh, dataclasses.replace(scheme, precision=z.FP64))
+        s64.set_state(u0)
+        s64.advance_timed(3)
+        ms64 += s64.advance_timed(k64)
+        s64.close()
+    ms64 = max_over_ranks(pg, ms64)
+    v64 = world * total_cells * stages * k64 / (ms64 * 1e-3)
+
+    # accuracy of the mixed batched form against FP64 on a sample of instances
+    errs = []
+    sample = [inst[j] for j in np.linspace(0, n_inst - 1, 6).astype(int)]
+    n_cmp = 50
+    b2 = z.Batch(len(sample))
+    pairs = []
+    for raw, mesh, scheme, u0 in sample:
+        s32 = z.Solver(mesh, scheme)
+        s32.set_state(u0)
+        b2.add(s32, n_steps=n_cmp)
+        s64 = z.Solver(mesh, dataclasses.replace(scheme, precision=z.FP64))
+        s64.set_state(u0)
+        s64.advance(n_steps=n_cmp)
+        pairs.append((s32, s64, raw, u0))
+    while b2.advance(8):
+        pass
+    for s32, s64, raw, u0 in pairs:
+        u32, _ = s32.get_state()
+        u64, _ = s64.get_state()
+        errs.append((state_rel_l1(u32, u64, None), perturbation_rel_l1(u32, u64, u0, None)))
+    b2.close()
+    wb = well_balanced_residual(z, sample[0][1], sample[0][2], n_cmp)
+
+    sizes = sorted(m.n_cells for _, m, _, _ in inst)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded meshes and data)",
+        "config": {"workload": f"C4 batched ensemble of {n_inst} well-balanced polytrope disks",
+                   "instances": n_inst, "cells": total_cells, "cells_min": sizes[0], "cells_median": sizes[len(sizes) // 2],
+                   "cells_max": sizes[-1], "precision": "mixed", "batched": True,
+                   "scheme": "CWENO-AO o3, HLLC, SSP3, CFL 0.45, isentropic well-balancing",
+                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2",
+                   "setup_s": t_setup, "autotune_s": t_tune},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+                "path": "set_state of every slot / Batch.advance(1) / get_state of every slot, pinned buffers"},
+        "roofline": roof,
+        "gpu_launches": launches * args.steps,
+        "clocks": clk.summary(),
+        "fp64": {"value": v64, "ms_per_step": ms64 / k64, "form": "plain FP64, one solve at a time",
+                 "steps_per_instance": k64},
+        "mixed_batched_over_fp64": value / v64,
+        "error_vs_fp64": {"instances": len(sample), "steps": n_cmp,
+                          "state_rel_l1_max": max(e[0] for e in errs),
+                          "perturbation_rel_l1_max": max(e[1] for e in errs)},
+        "well_balanced": wb,
+    }
+    if rank == 0:
+        raw, mesh, scheme, u0 = inst[len(inst) // 2]
+        try:
+            line["cpu_baseline"] = cpu_baseline(raw, mesh, scheme, u0,
+                                                {"cells": mesh.n_cells, "workload": "C4 ensemble instance"})
+        except Exception as exc:
+            line["cpu_baseline"] = {"error": str(exc)}
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
 
 
 def main():
@@ -254,121 +583,10 @@ def main():
         pg = dist
     if args.impl == "reference":
         run_reference(args, rank, world)
-        if pg:
-            pg.barrier()
-        return
-
-    import numpy as np
-    import zisafvm_gb300 as z
-    raw, mesh, scheme, u0, desc = workload(args.workload, args.precision)
-    solver = z.Solver(mesh, scheme)
-    solver.set_state(u0)
-    cells = desc["cells"]
-    stages = scheme.rk_stages
-
-    # warm-up, then K graph-replayed steps timed with CUDA events
-    if args.warmup:
-        solver.advance_timed(args.warmup)
-    if pg:
-        pg.barrier()
-    with ClockSampler(local) as clk:
-        ms = solver.advance_timed(args.steps)
-    if pg:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * cells * stages * args.steps / (ms * 1e-3)
-
-    if args.profile:
-        if rank == 0:
-            print(json.dumps({"metric": "cell-stage updates/s", "value": value, "ms_per_step": ms / args.steps,
-                              "config": desc, "profile_run": True}), flush=True)
-        return
-
-    # per-kernel event timing of the same loop (not graph-replayed)
-    kt = solver.kernel_times(min(args.steps, 32))
-    wdt = 8
-    b_cell = algorithmic_bytes_per_cell_stage(mesh, scheme, wdt)
-    n_recon = mesh.n_cells
-    bytes_launch = b_cell * n_recon
-    achieved = bytes_launch / (kt["reconstruct"] * 1e-3) / 1e9
-    hbm, peak_kind = measured_peaks()
-    traffic = profiles_traffic("k_reconstruct", args.workload, args.precision)
-
-    # end to end through the public API with host buffers
-    try:
-        import torch
-        host = torch.empty((mesh.n_cells, 5), dtype=torch.float64, pin_memory=True).numpy()
-        host_out = torch.empty((mesh.n_cells, 5), dtype=torch.float64, pin_memory=True).numpy()
-    except Exception:
-        host = np.empty((mesh.n_cells, 5))
-        host_out = np.empty((mesh.n_cells, 5))
-    solver.set_state(u0)
-    solver.advance(n_steps=1)
-    state, _ = solver.get_state()
-    host[:] = state
-    e2e_steps = max(4, min(args.steps, 64))
-    if pg:
-        pg.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        solver.set_state(host)
-        solver.advance(n_steps=1)
-        solver.get_state(out=host_out)
-        host, host_out = host_out, host
-    e2e_s = time.perf_counter() - t0
-    e2e_value = world * cells * stages * e2e_steps / e2e_s
-    io_bytes = mesh.n_cells * 5 * 8
-
-    line = {
-        "metric": "cell-stage updates/s", "value": value, "unit": "cell-stage updates/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
-        "data": "synthetic (seeded mesh and initial data)",
-        "config": {**desc, "precision": args.precision, "parallelism": f"replicas x{world}",
-                   "l2": "working set of the step loop > L2 for c2/c3; state stays resident across steps"},
-        "e2e": {"value": e2e_value, "unit": "cell-stage updates/s", "h2d_bytes_per_step": io_bytes,
-                "d2h_bytes_per_step": io_bytes},
-        "roofline": {"bound": "hbm", "kernel": "k_reconstruct", "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "peak_kind": peak_kind,
-                     "bytes_per_cell_stage": b_cell, "traffic": traffic,
-                     "kernel_ms": kt},
-        "gpu_launches": solver.launches_per_step() * args.steps,
-        "clocks": clk.summary(),
-    }
-    if args.precision == "mixed":
-        # error of the mixed form against the FP64 form after the same steps
-        import dataclasses
-        from metrics import perturbation_rel_l1, state_rel_l1
-        s64 = z.Solver(mesh, dataclasses.replace(scheme, precision=z.FP64))
-        s64.set_state(u0)
-        s32 = z.Solver(mesh, scheme)
-        s32.set_state(u0)
-        n_cmp = min(args.steps, 100)
-        s64.advance(n_steps=n_cmp)
-        s32.advance(n_steps=n_cmp)
-        u64, _ = s64.get_state()
-        u32, _ = s32.get_state()
-        mask = raw.ghost == 0 if raw.ghost is not None else None
-        line["error_vs_fp64"] = {"steps": n_cmp, "state_rel_l1": state_rel_l1(u32, u64, mask),
-                                 "perturbation_rel_l1": perturbation_rel_l1(u32, u64, u0, mask)}
-        if scheme.equilibrium:
-            eq_raw, eq_mesh, eq_scheme, eq_u0, _ = workload(args.workload, args.precision)
-            u_eq = eq_mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=0.0)
-            s_eq = z.Solver(eq_mesh, eq_scheme)
-            s_eq.set_state(u_eq)
-            res = float(np.abs(s_eq.rate_of_change()).max())
-            s_eq.advance(n_steps=n_cmp)
-            u_end, _ = s_eq.get_state()
-            drift = float((np.abs(u_end - u_eq).max(axis=0) / np.abs(u_eq).max(axis=0))[[0, 4]].max())
-            line["well_balanced"] = {"max_abs_dudt": res, "rel_drift": drift, "steps": n_cmp}
-    if rank == 0:
-        try:
-            line["cpu_baseline"] = cpu_baseline(raw, mesh, scheme, u0, desc)
-        except Exception as exc:  # the baseline must not hide the GPU number
-            line["cpu_baseline"] = {"error": str(exc)}
-        print(json.dumps(line), flush=True)
+    elif args.workload.startswith("c4"):
+        run_ensemble(args, rank, world, local, pg)
+    else:
+        run_single_mesh(args, rank, world, local, pg)
     if pg:
         pg.barrier()
 

@@ -219,6 +219,9 @@ int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_running);
 int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *ms);
 /* Pick the persistent grid sizes of each group's kernels by timing candidates. */
 int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *best_ms);
+/* Average per-launch device time (ms) of the three batched stage kernels
+ * {reconstruct, face flux, update} over `n_steps` steps (events, no graph). */
+int zfvm_batch_kernel_times(zfvm_batch *b, int32_t n_steps, float *ms);
 int zfvm_batch_slot_status(zfvm_batch *b, int32_t slot, double *t, int64_t *steps, int32_t *done,
                            int32_t *status);
 int zfvm_batch_slots(const zfvm_batch *b, int32_t *n_active);

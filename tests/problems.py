@@ -47,3 +47,29 @@ def vortex_tube_3d(n: int = 70, order: int = 3, seed: int = 1):
                       exponent=4.0, rk_stages=3, cfl_number=0.3, flux_bc=z.FLUX_BC_CONSTANT)
     u0 = mesh.initial_conditions("vortex", gamma=1.4, beta=5.0, x0=0.5, y0=0.5, length=0.1, v_inf=1.0, u_inf=1.0)
     return raw, mesh, scheme, u0
+
+
+def ensemble_c4(n_instances: int = 256, n_min: int = 5000, n_max: int = 200000, seed: int = 2024,
+                precision: int = z.MIXED):
+    """C4: independent well-balanced polytrope solves on seeded jittered disk
+    meshes with log-uniform sizes in [n_min, n_max] triangles, perturbation
+    amplitudes log-uniform in [1e-6, 1e-2], centres at r ~ U[0.1, 0.7] and a
+    random angle, width 0.05; CWENO-AO order 3, HLLC, SSP3."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_instances):
+        n_cells = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        rings = max(4, int(round(np.sqrt(n_cells / (2.0 * np.pi)))))
+        amp = float(np.exp(rng.uniform(np.log(1e-6), np.log(1e-2))))
+        r0, ang = float(rng.uniform(0.1, 0.7)), float(rng.uniform(0.0, 2.0 * np.pi))
+        raw = z.RawMesh.generate("disk", n=rings, radius=1.0, jitter=0.2, seed=seed + 17 * k + 1)
+        mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2), quad=(3, 3, 2))
+        scheme = z.Scheme(flux=z.FLUX_HLLC, gamma=2.0, linear_weights=[100.0, 1.0, 1.0, 1.0], epsilon=1e-6,
+                          exponent=4.0, rk_stages=3, cfl_number=0.45, equilibrium=z.EQ_ISENTROPIC,
+                          gravity=z.GRAVITY_HARMONIC_RADIAL, gravity_strength=1.0,
+                          flux_bc=z.FLUX_BC_ISENTROPIC, precision=precision)
+        u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amp,
+                                     width=0.05, x0=r0 * np.cos(ang), y0=r0 * np.sin(ang))
+        out.append((raw, mesh, scheme, u0))
+    return out

@@ -119,6 +119,7 @@ def load_library() -> C.CDLL:
         "zfvm_batch_advance": [vp, i32, C.POINTER(i32)],
         "zfvm_batch_advance_timed": [vp, i32, C.POINTER(C.c_float)],
         "zfvm_batch_autotune": [vp, i32, C.POINTER(C.c_float)],
+        "zfvm_batch_kernel_times": [vp, i32, C.POINTER(C.c_float)],
         "zfvm_batch_slot_status": [vp, i32, dp, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)],
         "zfvm_batch_slots": [vp, C.POINTER(i32)],
     }
@@ -439,6 +440,11 @@ class Batch:
         ms = C.c_float()
         _check(load_library().zfvm_batch_autotune(self._h, trial_steps, C.byref(ms)))
         return float(ms.value)
+
+    def kernel_times(self, n_steps: int) -> dict:
+        ms = (C.c_float * 3)()
+        _check(load_library().zfvm_batch_kernel_times(self._h, n_steps, ms))
+        return {"reconstruct": ms[0], "face_flux": ms[1], "update": ms[2]}
 
     def status(self, slot: int) -> dict:
         t, st, done, status = C.c_double(), C.c_int64(), C.c_int32(), C.c_int32()

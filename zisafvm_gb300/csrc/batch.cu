@@ -91,8 +91,9 @@ struct zfvm_batch {
 
 namespace {
 
-void launch_group_stage(zfvm_batch *b, Group &g, int stage) {
+void launch_group_stage(zfvm_batch *b, Group &g, int stage, cudaEvent_t *ev = nullptr) {
   BatchCfg c;
+  c.ev = ev;
   c.eq = g.key.eq;
   c.src = g.key.src;
   c.mixed = g.key.mixed;
@@ -361,6 +362,45 @@ extern "C" int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *be
     b->graph = nullptr;
   }
   if (best_ms) *best_ms = overall;
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+// Average device time (ms) of one launch of each of the three stage kernels
+// {reconstruct, face flux, update} over `n_steps` steps (no graph; events
+// around every launch on the batch stream).  The slots' states advance.
+extern "C" int zfvm_batch_kernel_times(zfvm_batch *b, int32_t n_steps, float *ms) {
+  if (!b || !ms || n_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  BATCH_GUARD_BEGIN
+  if (b->dirty) rebuild(b);
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  cudaEvent_t ev[4];
+  for (auto &e : ev) CK(cudaEventCreate(&e));
+  double acc[3] = {0.0, 0.0, 0.0};
+  int n = 0;
+  int stages = 0;
+  for (auto &kv : b->groups) stages = std::max(stages, kv.second->key.stages);
+  for (int k = 0; k < n_steps && b->n_clock > 0; ++k) {
+    k_clock_multi<<<(b->n_clock + 127) / 128, 128, 0, b->stream>>>(b->clock_ptrs.p, b->cfls.p, b->n_clock, 0);
+    CK(cudaGetLastError());
+    for (int st = 0; st < stages; ++st)
+      for (auto &kv : b->groups) {
+        if (kv.second->n_ct == 0 || st >= kv.second->key.stages) continue;
+        launch_group_stage(b, *kv.second, st, ev);
+        CK(cudaEventSynchronize(ev[3]));
+        for (int j = 0; j < 3; ++j) {
+          float t = 0.f;
+          CK(cudaEventElapsedTime(&t, ev[j], ev[j + 1]));
+          acc[j] += t;
+        }
+        ++n;
+      }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  for (int j = 0; j < 3; ++j) ms[j] = n ? float(acc[j] / n) : 0.f;
   return ZFVM_OK;
   BATCH_GUARD_END
 }

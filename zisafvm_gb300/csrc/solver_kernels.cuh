@@ -1138,6 +1138,7 @@ struct BatchCfg {
   int flux;
   int grid_recon, grid_face, grid_update;  // persistent grid sizes (autotuned)
   cudaStream_t stream;
+  cudaEvent_t *ev = nullptr;  // optional: 4 events recorded around the three stage kernels
 };
 
 template <class S, bool MIXED>
@@ -1145,6 +1146,7 @@ void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_c
                           int stage, const BatchCfg &c) {
   const int gr = c.grid_recon > 0 ? c.grid_recon : n_ct, gf = c.grid_face > 0 ? c.grid_face : n_ft,
             gu = c.grid_update > 0 ? c.grid_update : n_ct;
+  if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
     km_reconstruct<S, 1, 1, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
   else if (c.eq)
@@ -1153,6 +1155,7 @@ void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_c
     km_reconstruct<S, 0, 1, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
   else
     km_reconstruct<S, 0, 0, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+  if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
       km_face_flux<S, 0, 1, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
@@ -1164,7 +1167,9 @@ void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_c
     else
       km_face_flux<S, 1, 0, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
   }
+  if (c.ev) cudaEventRecord(c.ev[2], c.stream);
   km_update<S, MIXED><<<gu, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+  if (c.ev) cudaEventRecord(c.ev[3], c.stream);
 }
 
 template <class S>
