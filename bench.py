@@ -52,7 +52,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=16)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c1", "c3", "c3o2", "c4", "c2-small", "c1-small", "c3-small", "c4-small"])
+                    choices=["c2", "c1", "c3", "c3o2", "c4", "c5", "c2-small", "c1-small", "c3-small", "c4-small",
+                             "c5-small"])
+    ap.add_argument("--load", type=float, default=0.7, help="c5: offered load as a fraction of throughput")
+    ap.add_argument("--budget-gb", type=float, default=24.0, help="c5: device memory budget of the server")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
                     help="form whose throughput is `value`; with mixed the FP64 form is timed beside it")
     ap.add_argument("--profile", action="store_true",
@@ -243,7 +246,8 @@ def reference_sample(workload_name: str):
         raw, mesh, scheme, u0 = vortex_tube_3d(n=12, order=2 if workload_name == "c3o2" else 3)
         return raw, mesh, scheme, u0, mesh.n_cells, "C3 tetrahedral vortex tube"
     raw, mesh, scheme, u0 = polytrope_2d(n_rings=60, amplitude=1e-4)
-    name = "C4 polytrope ensemble" if workload_name.startswith("c4") else "C2 well-balanced polytrope disk"
+    name = {"c4": "C4 polytrope ensemble", "c5": "C5 serving request (polytrope disk)"}.get(
+        workload_name[:2], "C2 well-balanced polytrope disk")
     return raw, mesh, scheme, u0, mesh.n_cells, name
 
 
@@ -329,6 +333,15 @@ def max_over_ranks(pg, x: float) -> float:
     import torch
     t = torch.tensor([x], dtype=torch.float64)
     pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, x: float) -> float:
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
     return float(t.item())
 
 
@@ -570,6 +583,148 @@ def run_ensemble(args, rank, world, local, pg):
         pg.barrier()
 
 
+def serving_requests(n_req: int, seed: int, small: bool):
+    """C5 request stream: 70% 2D triangle meshes (2k-500k cells, log-uniform;
+    a gamma = 2 well-balanced polytrope disk or a gamma = 1.4 periodic vortex),
+    30% 3D tetrahedral meshes (50k-2M cells; gamma = 1.4 vortex tube), seeded
+    perturbation amplitudes 1e-6-1e-2, end times U[0.05, 0.5].  Meshes come
+    from a seeded pool (built before the arrivals start; set-up is reported
+    apart from latency)."""
+    import numpy as np
+    import zisafvm_gb300 as z
+    from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+    rng = np.random.default_rng(seed)
+    lo2, hi2, lo3, hi3 = (2000, 60000, 20000, 120000) if small else (2000, 500000, 50000, 2000000)
+    def logu(lo, hi):
+        return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+    pool = {"disk": [], "square": [], "cube": []}
+    for _ in range(3):
+        pool["disk"].append(polytrope_2d(n_rings=max(8, int(round(np.sqrt(logu(lo2, hi2) / (2 * np.pi))))),
+                                         amplitude=1e-4, seed=int(rng.integers(1 << 30))))
+        pool["square"].append(vortex_2d(n=max(12, int(round(np.sqrt(logu(lo2, hi2) / 2)))), halo=3,
+                                        flux=z.FLUX_HLLC))
+        pool["cube"].append(vortex_tube_3d(n=max(6, int(round((logu(lo3, hi3) / 6) ** (1 / 3)))), order=3))
+    reqs = []
+    for _ in range(n_req):
+        u = rng.uniform()
+        kind = "cube" if u < 0.3 else ("disk" if u < 0.65 else "square")
+        raw, mesh, scheme, _ = pool[kind][int(rng.integers(3))]
+        amp = float(np.exp(rng.uniform(np.log(1e-6), np.log(1e-2))))
+        t_end = float(rng.uniform(0.05, 0.5))
+        if kind == "disk":
+            r0, ang = float(rng.uniform(0.1, 0.7)), float(rng.uniform(0, 2 * np.pi))
+            u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amp,
+                                         width=0.05, x0=r0 * np.cos(ang), y0=r0 * np.sin(ang))
+        else:
+            # vortex strength scaled by the amplitude draw: beta in [0.5, 5]
+            beta = 0.5 + 4.5 * (np.log10(amp) + 6.0) / 4.0
+            x0, y0 = float(rng.uniform(0.3, 0.7)), float(rng.uniform(0.3, 0.7))
+            u0 = mesh.initial_conditions("vortex", gamma=1.4, beta=beta, x0=x0, y0=y0, length=0.1)
+        reqs.append({"kind": kind, "mesh": mesh, "scheme": scheme, "u0": u0, "t_end": t_end, "amp": amp})
+    return pool, reqs
+
+
+def serve_stream(z, reqs, arrivals, precision, budget, max_slots, steps_per_round):
+    """Submit every request at its arrival time from a client thread, wait for
+    all, and return per-request latencies and the server statistics."""
+    import dataclasses
+    srv = z.Server(hbm_budget_bytes=budget, max_slots=max_slots, steps_per_round=steps_per_round)
+    ids = [None] * len(reqs)
+    t_start = time.perf_counter()
+
+    def client():
+        for k, r in enumerate(reqs):
+            delay = t_start + arrivals[k] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            sc = dataclasses.replace(r["scheme"], precision=precision)
+            ids[k] = srv.submit(r["mesh"], sc, r["u0"], t_end=r["t_end"])
+
+    th = threading.Thread(target=client)
+    th.start()
+    th.join()
+    out = [srv.wait(rid) for rid in ids]
+    makespan = time.perf_counter() - t_start
+    st = srv.stats()
+    srv.close()
+    return out, st, makespan
+
+
+def percentile(xs, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(xs), q)) if xs else None
+
+
+def run_serving(args, rank, world, local, pg):
+    """C5: Poisson arrivals of uneven 2D / 3D solves, admitted by device
+    footprint and batched continuously; mixed form (value) next to the plain
+    FP64 form serving the same stream."""
+    import numpy as np
+    import zisafvm_gb300 as z
+    small = args.workload == "c5-small"
+    n_req = 12 if small else 32
+    t0 = time.perf_counter()
+    pool, reqs = serving_requests(n_req, seed=77 + 7919 * rank, small=small)
+    setup_s = time.perf_counter() - t0
+    # expected work per request from the CFL step of its initial state
+    work = []
+    for r in reqs:
+        s = z.Solver(r["mesh"], r["scheme"])
+        s.set_state(r["u0"])
+        dt = s.cfl_dt()
+        s.close()
+        steps = int(np.ceil(r["t_end"] / dt))
+        work.append(r["mesh"].n_cells * 3 * steps)
+    # offered load: args.load of the mixed form's sustained throughput (~7e8 /s)
+    rate = args.load * 7.0e8 / float(np.mean(work))
+    rng = np.random.default_rng(1234 + rank)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n_req))
+    arrivals -= arrivals[0]
+    budget = int(args.budget_gb * (1 << 30))
+    if pg:
+        pg.barrier()
+    with ClockSampler(local) as clk:
+        res, st, makespan = serve_stream(z, reqs, arrivals, z.MIXED, budget, 64, 8)
+    lat = [r[3]["total"] for r in res]
+    queued = [r[3]["queued"] for r in res]
+    work_all = sum_over_ranks(pg, float(st["cell_stage_updates"]))
+    value = work_all / max_over_ranks(pg, makespan)
+    res64, st64, makespan64 = serve_stream(z, reqs, arrivals, z.FP64, budget, 64, 8)
+    lat64 = [r[3]["total"] for r in res64]
+    # result of each request: mixed against FP64 (perturbation-level agreement)
+    from metrics import state_rel_l1
+    errs = [state_rel_l1(a[0], b[0], None) for a, b in zip(res, res64)]
+    # e2e here is the serving path itself: host states in, host states out
+    io_in = sum(r["mesh"].n_cells * 5 * 8 for r in reqs)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": None, "warmup": 0,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic (seeded meshes, data and arrivals)",
+        "config": {"workload": "C5 serving loop" + (" (small)" if small else ""), "requests": n_req,
+                   "mix": {k: sum(r["kind"] == k for r in reqs) for k in ("disk", "square", "cube")},
+                   "cells_per_request": [int(r["mesh"].n_cells) for r in reqs],
+                   "t_end": [round(r["t_end"], 4) for r in reqs],
+                   "arrival_rate_per_s": rate, "offered_load": args.load, "budget_bytes": budget,
+                   "max_slots": 64, "steps_per_round": 8, "mesh_setup_s": setup_s,
+                   "parallelism": f"replicas x{world}"},
+        "latency_ms": {"p50": percentile(lat, 50), "p99": percentile(lat, 99), "mean": float(np.mean(lat)),
+                       "queued_p50": percentile(queued, 50), "queued_p99": percentile(queued, 99)},
+        "server": {"completed": st["completed"], "failed": st["failed"], "bytes_peak": st["bytes_peak"],
+                   "busy_s": st["busy_s"], "makespan_s": makespan, "rounds": st["rounds"]},
+        "fp64": {"value": st64["cell_stage_updates"] / makespan64,
+                 "latency_ms": {"p50": percentile(lat64, 50), "p99": percentile(lat64, 99)},
+                 "makespan_s": makespan64, "completed": st64["completed"], "failed": st64["failed"]},
+        "error_vs_fp64": {"state_rel_l1_max": max(errs) if errs else None},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": io_in, "d2h_bytes_per_step": io_in,
+                "path": "Server.submit / wait with host states (bytes per stream, not per step)"},
+        "roofline": None,
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -585,6 +740,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload.startswith("c4"):
         run_ensemble(args, rank, world, local, pg)
+    elif args.workload.startswith("c5"):
+        run_serving(args, rank, world, local, pg)
     else:
         run_single_mesh(args, rank, world, local, pg)
     if pg:

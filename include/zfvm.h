@@ -226,6 +226,46 @@ int zfvm_batch_slot_status(zfvm_batch *b, int32_t slot, double *t, int64_t *step
                            int32_t *status);
 int zfvm_batch_slots(const zfvm_batch *b, int32_t *n_active);
 
+/* ---- serving --------------------------------------------------------------
+ * A request loop with continuous batching: solves submitted from any thread
+ * wait in a queue, are admitted in arrival order while their device footprint
+ * (zfvm_solver_footprint) fits the memory budget and a slot is free (smaller
+ * requests may overtake one that does not fit, at most 8 times), join the
+ * solves already running in one batch, keep their state on the device and
+ * return their final state when done.  One worker thread owns the device work.
+ * No counterpart in the reference (one solve per process). */
+typedef struct zfvm_server zfvm_server;
+typedef struct {
+  int64_t hbm_budget_bytes;  /* device bytes the solves may hold (<= 0: 80% of the free memory) */
+  int32_t max_slots;         /* concurrent solves                                              */
+  int32_t steps_per_round;   /* batched steps between admission and retirement                 */
+} zfvm_server_desc;
+typedef struct {
+  int64_t submitted, completed, failed, queued, running;
+  int64_t bytes_in_use, bytes_peak, budget_bytes;
+  int64_t cell_stage_updates;  /* work of the completed solves                  */
+  int64_t rounds;
+  double busy_s;               /* worker time spent stepping running solves      */
+} zfvm_server_stats;
+/* Device bytes zfvm_solver_create will allocate for this mesh and scheme. */
+int zfvm_solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc *scheme, int64_t *bytes);
+int zfvm_server_create(const zfvm_server_desc *desc, zfvm_server **out);
+/* Stops the worker; unfinished requests fail.  No thread may be waiting on the server. */
+int zfvm_server_destroy(zfvm_server *srv);
+/* Queue a solve of `mesh` (kept alive by the caller until the request is
+ * waited for) from cvars (n_cells x 5, copied) at time t0 until n_steps steps
+ * (if > 0) or time t_end (if > t0).  ZFVM_ENOMEM if its footprint exceeds the budget. */
+int zfvm_server_submit(zfvm_server *srv, zfvm_mesh *mesh, const zfvm_scheme_desc *scheme, const double *cvars,
+                       double t0, int64_t n_steps, double t_end, int64_t *id);
+/* phase: 0 queued, 1 running, 2 done, 3 failed */
+int zfvm_server_poll(zfvm_server *srv, int64_t id, int32_t *phase);
+/* Wait (timeout_s < 0: no limit) for a request, copy its final state, time and
+ * steps, and release it.  times_ms = {queued, running, submit to result}.  A
+ * failed solve returns its error status. */
+int zfvm_server_wait(zfvm_server *srv, int64_t id, double timeout_s, double *cvars, double *t, int64_t *steps,
+                     double *times_ms);
+int zfvm_server_get_stats(zfvm_server *srv, zfvm_server_stats *stats);
+
 const char *zfvm_last_error(void);
 
 #ifdef __cplusplus

@@ -31,3 +31,18 @@ def test_error_reporting_without_compute(zlib):
     lib = z.load_library()
     assert lib.zfvm_mesh_create(None, None) == 1
     assert b"null" in lib.zfvm_last_error()
+
+
+def test_solver_footprint_without_device(zlib):
+    """The admission estimate is host arithmetic: available without a GPU."""
+    z = zlib
+    from problems import polytrope_2d
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=12)
+    f64 = z.solver_footprint(mesh, scheme)
+    scheme.precision = z.MIXED
+    f32 = z.solver_footprint(mesh, scheme)
+    raw2, mesh2, scheme2, _ = polytrope_2d(n_rings=24)
+    f64_big = z.solver_footprint(mesh2, scheme2)
+    assert 0 < f32 < f64 < f64_big
+    per_cell = f64_big / mesh2.n_cells
+    assert 500 < per_cell < 5000

@@ -61,6 +61,16 @@ class _MeshInfo(C.Structure):
                 ("max_circum_radius", C.c_double), ("total_volume", C.c_double)]
 
 
+class _ServerDesc(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_slots", C.c_int32), ("steps_per_round", C.c_int32)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "queued", "running", "bytes_in_use",
+                                          "bytes_peak", "budget_bytes", "cell_stage_updates", "rounds")] + \
+               [("busy_s", C.c_double)]
+
+
 class _SchemeDesc(C.Structure):
     _fields_ = [("flux", C.c_int32), ("gamma", C.c_double), ("specific_gas_constant", C.c_double),
                 ("linear_weights", C.c_double * MAX_STENCILS), ("epsilon", C.c_double),
@@ -122,6 +132,13 @@ def load_library() -> C.CDLL:
         "zfvm_batch_kernel_times": [vp, i32, C.POINTER(C.c_float)],
         "zfvm_batch_slot_status": [vp, i32, dp, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)],
         "zfvm_batch_slots": [vp, C.POINTER(i32)],
+        "zfvm_solver_footprint": [vp, vp, C.POINTER(i64)],
+        "zfvm_server_create": [vp, pp],
+        "zfvm_server_destroy": [vp],
+        "zfvm_server_submit": [vp, vp, vp, dp, C.c_double, i64, C.c_double, C.POINTER(i64)],
+        "zfvm_server_poll": [vp, i64, C.POINTER(i32)],
+        "zfvm_server_wait": [vp, i64, C.c_double, dp, dp, C.POINTER(i64), dp],
+        "zfvm_server_get_stats": [vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -451,3 +468,74 @@ class Batch:
         _check(load_library().zfvm_batch_slot_status(self._h, slot, C.byref(t), C.byref(st), C.byref(done),
                                                      C.byref(status)))
         return {"t": t.value, "steps": st.value, "done": bool(done.value), "status": status.value}
+
+
+def solver_footprint(mesh: "Mesh", scheme: "Scheme") -> int:
+    """Device bytes a Solver of this mesh and scheme allocates (host-side count)."""
+    desc = scheme.desc()
+    n = C.c_int64()
+    _check(load_library().zfvm_solver_footprint(mesh._h, C.byref(desc), C.byref(n)))
+    return n.value
+
+
+class Server:
+    """Request loop with continuous batching (see zfvm_server_* in zfvm.h).
+
+    submit() queues a solve and returns its id at once; wait() blocks until it
+    is done and returns (final state, final time, steps, times in ms
+    {queued, running, total}).  Meshes must stay alive until their requests
+    have been waited for; this object keeps a reference for that."""
+
+    QUEUED, RUNNING, DONE, FAILED = 0, 1, 2, 3
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_slots: int = 64, steps_per_round: int = 8):
+        d = _ServerDesc(hbm_budget_bytes, max_slots, steps_per_round)
+        h = C.c_void_p()
+        _check(load_library().zfvm_server_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self._meshes = {}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and _LIB is not None:
+            _LIB.zfvm_server_destroy(self._h)
+            self._h = None
+            self._meshes.clear()
+
+    def __del__(self):
+        self.close()
+
+    def submit(self, mesh: "Mesh", scheme: "Scheme", cvars: np.ndarray, t0: float = 0.0, n_steps: int = 0,
+               t_end: float = 0.0) -> int:
+        a = np.ascontiguousarray(cvars, dtype=np.float64)
+        assert a.shape == (mesh.n_cells, 5)
+        desc = scheme.desc()
+        rid = C.c_int64()
+        _check(load_library().zfvm_server_submit(self._h, mesh._h, C.byref(desc), _dp(a), t0, n_steps, t_end,
+                                                 C.byref(rid)))
+        self._meshes[rid.value] = mesh
+        return rid.value
+
+    def poll(self, rid: int) -> int:
+        ph = C.c_int32()
+        _check(load_library().zfvm_server_poll(self._h, rid, C.byref(ph)))
+        return ph.value
+
+    def wait(self, rid: int, timeout_s: float = -1.0):
+        mesh = self._meshes[rid]
+        out = np.empty((mesh.n_cells, 5))
+        t, st = C.c_double(), C.c_int64()
+        times = (C.c_double * 3)()
+        try:
+            _check(load_library().zfvm_server_wait(self._h, rid, timeout_s, _dp(out), C.byref(t), C.byref(st),
+                                                   C.cast(times, C.POINTER(C.c_double))))
+        except ZfvmError as e:
+            if e.code != 5:  # a timeout keeps the request
+                self._meshes.pop(rid, None)
+            raise
+        self._meshes.pop(rid, None)
+        return out, t.value, st.value, {"queued": times[0], "running": times[1], "total": times[2]}
+
+    def stats(self) -> dict:
+        s = _ServerStats()
+        _check(load_library().zfvm_server_get_stats(self._h, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in _ServerStats._fields_}

@@ -28,7 +28,7 @@ NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fope
              "--expt-relaxed-constexpr"]
 
 HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp"]
-CUDA_SOURCES = ["solver.cu", "batch.cu", "noalloc.cu", "inst_s2o3.cu", "inst_s2o2.cu", "inst_s3o3.cu", "inst_s3o2.cu"]
+CUDA_SOURCES = ["solver.cu", "batch.cu", "server.cu", "noalloc.cu", "inst_s2o3.cu", "inst_s2o2.cu", "inst_s3o3.cu", "inst_s3o2.cu"]
 
 
 def _headers() -> list[Path]:

@@ -815,3 +815,55 @@ extern "C" int zfvm_kernel_times(zfvm_solver *s, int64_t n_steps, float *ms) {
   return ZFVM_OK;
   SOLVER_GUARD_END
 }
+
+// Device bytes zfvm_solver_create would allocate for this mesh and scheme: the
+// same buffers and sizes as build_solver, so a caller (or the server's
+// admission control) can decide before allocating.
+int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
+  const Grid &g = m->grid;
+  const auto &sp = m->sparams;
+  const int64_t nd = g.n_dims, nv = nd + 2, nf = nd + 1, nqf = g.n_face_qp, nqc = g.n_cell_qp;
+  const int64_t ld = (g.n_cells + 31) / 32 * 32, lde = (g.n_edges + 31) / 32 * 32, n = g.n_cells;
+  const int ns = (int)sp.orders.size();
+  if (ns < 2) return -1;
+  const int64_t R0 = (int64_t)required_stencil_size(sp.orders[0] - 1, sp.overfit[0], (int)nd) - 1;
+  const int64_t C0 = poly_dof(sp.orders[0] - 1, (int)nd) - 1;
+  const int64_t NB = ns - 1;
+  const int64_t RB = (int64_t)required_stencil_size(sp.orders[1] - 1, sp.overfit[1], (int)nd) - 1;
+  const int64_t CB = poly_dof(sp.orders[1] - 1, (int)nd) - 1;
+  const int64_t NC = std::max(C0, CB), NP = R0 * C0 + NB * RB * CB, MAXL = R0 + 1 + NB * RB;
+  const bool mixed = sc.precision == ZFVM_MIXED, has_eq = sc.equilibrium == ZFVM_EQ_ISENTROPIC,
+             has_src = sc.gravity != ZFVM_GRAVITY_NONE;
+  const int64_t kst = std::max(1, sc.rk_stages - 1);
+  int64_t b = 0;
+  // flags, bloc, fkL, fkR, factive
+  b += ld + NB * RB * ld + 3 * lde;
+  // l2g, cface, fL, fR, src_map
+  b += 4 * (MAXL * ld + nf * ld + 2 * lde + ld);
+  // geometry, faces, state and tendency
+  b += 8 * (nd * ld + ld + NC * ld + ld + ld);                       // center, inv_len, mom, inv_vol, r_eff
+  b += 8 * (nqf * nd * lde + nqf * lde + nd * nd * lde + lde);       // fqx, fqw, frame, farea
+  b += 8 * (2 * nv * ld + nv * ld + 5 * n);                          // u0, ux, tend, aos
+  if (has_src) {
+    b += 8 * (nqc * ld + 2 * ld + 2 * nqc * nd * ld + nqc * ld + nqf * lde);  // phi_cq, m1, var, gphi, cqx, cqw, phi_fq
+    if (!mixed) b += 8 * nv * ld;                                               // srcb
+  }
+  if (has_eq) b += 8 * 4 * ld;                                                  // eqth
+  if (mixed) {
+    b += 4 * (NP * ld + nd * nd * lde + NC * ld + nf * nqf * nd * ld + nqc * nd * ld);  // pinv32 frame32 mom32 xfq32 xcq32
+    b += 4 * (nv * lde + 2 * nd * lde + kst * nv * ld + nf * nqf * nv * ld);          // g32 mL32 mR32 kbuf32 fv32
+    b += 8 * nv * ld;                                                                   // dev0
+    if (has_src) b += 4 * nv * ld + 8 * nd * ld + 4 * nqc * nd * ld;                   // src32 gphi_w wg32
+  } else {
+    b += 8 * (NP * ld + kst * nv * ld + nf * nqf * nv * ld + nv * lde);  // pinv kbuf fv nfb
+  }
+  return b;
+}
+
+extern "C" int zfvm_solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc *sc, int64_t *bytes) {
+  if (!m || !sc || !bytes) return fail(ZFVM_EINVAL, "null argument");
+  const int64_t b = solver_footprint(m, *sc);
+  if (b < 0) return fail(ZFVM_EINVAL, "the mesh has fewer than two stencils");
+  *bytes = b;
+  return ZFVM_OK;
+}

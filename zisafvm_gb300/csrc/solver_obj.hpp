@@ -94,3 +94,5 @@ void write_clock(zfvm_solver *s, const zfvm::dev::Clock &c);
 void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt);
 // ZFVM_* status and message for the device status bits of a Clock
 int status_to_code(int st, std::string &msg);
+// device bytes zfvm_solver_create allocates for this mesh and scheme (-1: no stencils)
+int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc);
