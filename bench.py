@@ -586,13 +586,15 @@ def run_ensemble(args, rank, world, local, pg):
 def serving_requests(n_req: int, seed: int, small: bool):
     """C5 request stream: 70% 2D triangle meshes (2k-500k cells, log-uniform;
     a gamma = 2 well-balanced polytrope disk or a gamma = 1.4 periodic vortex),
-    30% 3D tetrahedral meshes (50k-2M cells; gamma = 1.4 vortex tube), seeded
-    perturbation amplitudes 1e-6-1e-2, end times U[0.05, 0.5].  Meshes come
-    from a seeded pool (built before the arrivals start; set-up is reported
-    apart from latency)."""
+    30% 3D tetrahedral meshes (50k-2M cells; gamma = 2 well-balanced
+    polytrope on the unit cube), seeded perturbation amplitudes 1e-6-1e-2, end
+    times U[0.05, 0.5].  Meshes come from a seeded pool (built before the
+    arrivals start; set-up is reported apart from latency).  The 3D vortex
+    tube of the C3 benchmark is not used here: with the constant flux
+    boundary its inflow faces amplify perturbations over hundreds of steps."""
     import numpy as np
     import zisafvm_gb300 as z
-    from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+    from problems import polytrope_2d, polytrope_3d, vortex_2d
     rng = np.random.default_rng(seed)
     lo2, hi2, lo3, hi3 = (2000, 60000, 20000, 120000) if small else (2000, 500000, 50000, 2000000)
     def logu(lo, hi):
@@ -603,7 +605,8 @@ def serving_requests(n_req: int, seed: int, small: bool):
                                          amplitude=1e-4, seed=int(rng.integers(1 << 30))))
         pool["square"].append(vortex_2d(n=max(12, int(round(np.sqrt(logu(lo2, hi2) / 2)))), halo=3,
                                         flux=z.FLUX_HLLC))
-        pool["cube"].append(vortex_tube_3d(n=max(6, int(round((logu(lo3, hi3) / 6) ** (1 / 3)))), order=3))
+        pool["cube"].append(polytrope_3d(n=max(6, int(round((logu(lo3, hi3) / 6) ** (1 / 3)))),
+                                         seed=int(rng.integers(1 << 30))))
     reqs = []
     for _ in range(n_req):
         u = rng.uniform()
@@ -615,6 +618,10 @@ def serving_requests(n_req: int, seed: int, small: bool):
             r0, ang = float(rng.uniform(0.1, 0.7)), float(rng.uniform(0, 2 * np.pi))
             u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amp,
                                          width=0.05, x0=r0 * np.cos(ang), y0=r0 * np.sin(ang))
+        elif kind == "cube":
+            x0, y0 = float(rng.uniform(0.2, 0.8)), float(rng.uniform(0.2, 0.8))
+            u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amp,
+                                         width=0.05, x0=x0, y0=y0)
         else:
             # vortex strength scaled by the amplitude draw: beta in [0.5, 5]
             beta = 0.5 + 4.5 * (np.log10(amp) + 6.0) / 4.0
@@ -694,6 +701,8 @@ def run_serving(args, rank, world, local, pg):
     # result of each request: mixed against FP64 (perturbation-level agreement)
     from metrics import state_rel_l1
     errs = [state_rel_l1(a[0], b[0], None) for a, b in zip(res, res64)]
+    err_by_kind = {k: max([e for e, r in zip(errs, reqs) if r["kind"] == k], default=None)
+                   for k in ("disk", "square", "cube")}
     # e2e here is the serving path itself: host states in, host states out
     io_in = sum(r["mesh"].n_cells * 5 * 8 for r in reqs)
     line = {
@@ -710,11 +719,12 @@ def run_serving(args, rank, world, local, pg):
         "latency_ms": {"p50": percentile(lat, 50), "p99": percentile(lat, 99), "mean": float(np.mean(lat)),
                        "queued_p50": percentile(queued, 50), "queued_p99": percentile(queued, 99)},
         "server": {"completed": st["completed"], "failed": st["failed"], "bytes_peak": st["bytes_peak"],
-                   "busy_s": st["busy_s"], "makespan_s": makespan, "rounds": st["rounds"]},
+                   "busy_s": st["busy_s"], "makespan_s": makespan, "rounds": st["rounds"],
+                   "throughput_while_busy": st["cell_stage_updates"] / max(st["busy_s"], 1e-9)},
         "fp64": {"value": st64["cell_stage_updates"] / makespan64,
                  "latency_ms": {"p50": percentile(lat64, 50), "p99": percentile(lat64, 99)},
                  "makespan_s": makespan64, "completed": st64["completed"], "failed": st64["failed"]},
-        "error_vs_fp64": {"state_rel_l1_max": max(errs) if errs else None},
+        "error_vs_fp64": {"state_rel_l1_max": max(errs) if errs else None, "by_kind": err_by_kind},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": io_in, "d2h_bytes_per_step": io_in,
                 "path": "Server.submit / wait with host states (bytes per stream, not per step)"},
         "roofline": None,

@@ -49,6 +49,24 @@ def vortex_tube_3d(n: int = 70, order: int = 3, seed: int = 1):
     return raw, mesh, scheme, u0
 
 
+def polytrope_3d(n: int = 40, amplitude: float = 1e-4, seed: int = 3, precision: int = z.FP64, order: int = 3):
+    """gamma = 2 isentropic polytrope on the unit cube of n^3 x 6 jittered
+    tetrahedra, phi = r^2 / 2 about the origin (the cube is one octant of the
+    star: rho = 1 - r^2 / 4 falls from 1 to 1/4 at the far corner), plus a
+    Gaussian pressure tube along z of width 0.05 through (0.5, 0.4); CWENO-AO,
+    HLLC, SSP3, CFL 0.3, isentropic well-balancing and flux boundary."""
+    raw = z.RawMesh.generate("cube", n=n, jitter=0.1, seed=seed)
+    quad = (2, 2, 2) if order == 3 else (2, 2, 1)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(order, 3), quad=quad)
+    scheme = z.Scheme(flux=z.FLUX_HLLC, gamma=2.0, linear_weights=[100.0, 1.0, 1.0, 1.0, 1.0], epsilon=1e-6,
+                      exponent=4.0, rk_stages=3, cfl_number=0.3, equilibrium=z.EQ_ISENTROPIC,
+                      gravity=z.GRAVITY_HARMONIC_RADIAL, gravity_strength=1.0, flux_bc=z.FLUX_BC_ISENTROPIC,
+                      precision=precision)
+    u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amplitude,
+                                 width=0.05, x0=0.5, y0=0.4)
+    return raw, mesh, scheme, u0
+
+
 def ensemble_c4(n_instances: int = 256, n_min: int = 5000, n_max: int = 200000, seed: int = 2024,
                 precision: int = z.MIXED):
     """C4: independent well-balanced polytrope solves on seeded jittered disk

@@ -9,7 +9,7 @@ import pytest
 
 import zisafvm_gb300 as z
 from metrics import perturbation_rel_l1, rel_errors, state_rel_l1
-from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+from problems import polytrope_2d, polytrope_3d, vortex_2d, vortex_tube_3d
 
 pytestmark = pytest.mark.gpu
 
@@ -58,7 +58,7 @@ def test_mixed_well_balanced(zlib):
     assert res < TOL_WB
     s.advance(n_steps=30)
     u, _ = s.get_state()
-    drift = (np.abs(u - u0).max(axis=0) / np.abs(u0).max(axis=0))[[0, 4]].max()
+    drift = (np.abs(u - u0)[:, [0, 4]].max(axis=0) / np.abs(u0)[:, [0, 4]].max(axis=0)).max()
     print(f"mixed WB drift after 30 steps = {drift:.3e}")
     assert drift < TOL_WB
 
@@ -87,3 +87,24 @@ def test_mixed_tets(zlib):
     u32, _ = s32.get_state()
     l1, linf = rel_errors(u32, u64)
     assert l1 < TOL_MIXED, (l1, linf)
+
+
+def test_mixed_polytrope_3d(zlib):
+    """Tetrahedral well-balanced polytrope: residual at rest and the
+    perturbation against the FP64 form."""
+    raw, mesh, scheme, u0 = polytrope_3d(n=8, amplitude=0.0, precision=z.MIXED)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    assert np.abs(s.rate_of_change()).max() < TOL_WB
+    s.advance(n_steps=20)
+    u, _ = s.get_state()
+    drift = (np.abs(u - u0)[:, [0, 4]].max(axis=0) / np.abs(u0)[:, [0, 4]].max(axis=0)).max()
+    assert drift < TOL_WB
+    raw, mesh, scheme, u0 = polytrope_3d(n=8, amplitude=1e-3)
+    s64, s32 = _pair(mesh, scheme, u0)
+    s64.advance(n_steps=20)
+    s32.advance(n_steps=20)
+    u64, _ = s64.get_state()
+    u32, _ = s32.get_state()
+    assert state_rel_l1(u32, u64) < TOL_MIXED
+    assert perturbation_rel_l1(u32, u64, u0) < 1e-4

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from metrics import rel_errors
-from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+from problems import polytrope_2d, polytrope_3d, vortex_2d, vortex_tube_3d
 
 pytestmark = pytest.mark.gpu
 
@@ -145,6 +145,29 @@ def test_tets_rhs(zlib, olib, order):
             continue
         err = np.abs(t_gpu[:, v] - t_ref[:, v]).max() / scale[v]
         assert err < TOL_RHS * 10, (v, err)
+
+
+def test_polytrope_3d_rhs_steps_and_balance(zlib, olib):
+    """Well-balanced gamma = 2 polytrope on tetrahedra: right-hand side and
+    steps against the oracle, and the unperturbed equilibrium at rest."""
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_3d(n=5, amplitude=1e-2)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t_gpu = s.rate_of_change()
+    o = _oracle(olib, raw, mesh, scheme)
+    t_ref = o.rate_of_change(u0)
+    scale = np.abs(t_ref).max()
+    assert np.abs(t_gpu - t_ref).max() <= 1e-10 * scale
+    s.advance(n_steps=4)
+    u_gpu, t1 = s.get_state()
+    u_ref, t_ref1, _ = o.run(u0, n_steps=4)
+    d_gpu, d_ref = u_gpu - u0, u_ref - u0
+    assert np.abs(d_gpu - d_ref).max() <= 1e-9 * np.abs(d_ref).max()
+    assert abs(t1 - t_ref1) < 1e-12 * t_ref1
+    u_eq = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=0.0)
+    s.set_state(u_eq)
+    assert np.abs(s.rate_of_change()).max() < 1e-10
 
 
 def test_error_status_nonphysical(zlib):
