@@ -89,3 +89,21 @@ def _first_qp(tri):
     # the degree-2 rule: barycentric (2/3, 1/6, 1/6)
     t = np.asarray(tri, float)
     return list(2.0 / 3.0 * t[0] + 1.0 / 6.0 * t[1] + 1.0 / 6.0 * t[2])
+
+
+def test_pseudo_inverse_matches_ldlt_solve(zlib, olib):
+    """The product solves the stencil least-squares problems with a precomputed
+    pseudo-inverse (host Householder QR); the reference solves the normal
+    equations with an LDLT factorisation per call (reconstruction/
+    lsq_solver.cpp:40-85).  The oracle's LDLT restatement and the product's
+    pseudo-inverses give the same right-hand side to round-off."""
+    from problems import polytrope_2d, vortex_2d
+    for raw, mesh, scheme, u0 in (vortex_2d(n=12, halo=3), polytrope_2d(n_rings=10, amplitude=1e-2)):
+        o = olib.Oracle(raw, mesh.stencils(), scheme.oracle_vector(), quad=mesh.quad, threads=1)
+        t_ldlt = o.rate_of_change(u0)
+        o.use_pinv(mesh)
+        t_pinv = o.rate_of_change(u0)
+        scale = np.abs(t_ldlt).max(axis=0)
+        for v in range(5):
+            if scale[v] > 0:
+                assert np.abs(t_pinv[:, v] - t_ldlt[:, v]).max() <= 1e-12 * scale[v], v
