@@ -285,15 +285,16 @@ METRIC = "cell-stage updates/s, FP64 vs mixed-batched at \u22641e-6 L1 error; p5
 UNIT = "cell-stage updates/s"
 
 
-def roofline_block(mesh, scheme, kt: dict, mixed: bool, workload_name: str, n_cells_launch: int):
+def roofline_block(mesh, scheme, kt: dict, mixed: bool, workload_name: str, n_cells_launch: int,
+                   kernel: str = "k_reconstruct"):
     """HBM roofline of the reconstruction kernel (the dominant launch): the
     algorithmic bytes of one launch over its event-timed duration."""
     b_cell = algorithmic_bytes_per_cell_stage(mesh, scheme, mixed)
     bytes_launch = b_cell * n_cells_launch
     achieved = bytes_launch / (kt["reconstruct"] * 1e-3) / 1e9
     hbm, peak_kind = measured_peaks()
-    traffic = profiles_traffic("k_reconstruct", workload_name, "mixed" if mixed else "fp64")
-    return {"bound": "hbm", "kernel": "k_reconstruct", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+    traffic = profiles_traffic(kernel, workload_name, "mixed" if mixed else "fp64")
+    return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_cell_stage": b_cell,
             "bytes_per_launch": bytes_launch, "traffic": traffic, "kernel_ms": kt,
             "fp64_pipe_note": "the FP64 pipe (1.25 TFLOP/s measured) bounds these kernels before HBM does"}
@@ -487,8 +488,7 @@ def run_ensemble(args, rank, world, local, pg):
                               "config": {"workload": "C4", "instances": n_inst}, "profile_run": True}), flush=True)
         return
     kt = batch.kernel_times(min(args.steps, 16))
-    roof = roofline_block(inst[0][1], inst[0][2], kt, True, args.workload, total_cells)
-    roof["kernel"] = "km_reconstruct"
+    roof = roofline_block(inst[0][1], inst[0][2], kt, True, args.workload, total_cells, kernel="km_reconstruct")
 
     # end to end: every step uploads all states from pinned host memory, advances
     # the batch one step and reads every state back
