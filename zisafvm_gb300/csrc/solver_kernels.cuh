@@ -88,6 +88,8 @@ struct DevData {
   const float *mom32;    // [NC][ld]
   const double *gphi_w;  // [ND][ld] sum_q w_q grad phi(x_q) over the cell
   const float *wg32;     // [NQC][ND][ld] w_q grad phi(x_q)
+  const float2 *m1s;     // [ld] phi_m1 as an FP32 (hi, lo) pair
+  const float2 *vars;    // [ld] phi_var as an FP32 (hi, lo) pair
   Clock *clock;
 };
 
@@ -121,6 +123,10 @@ struct StageArgs {
   // (tend_L += -G + mL, tend_R += G + mR), FP32 source [NV][ld], FP32 stage
   // tendencies [NV][ld]
   float *g32, *mL32, *mR32, *src32, *k32[4];
+  // MIXED: the stage state as FP32 (hi, lo) pairs [NV][ld] (hi + lo carries 48
+  // bits of the FP64 value), and the pairs the update writes with its state
+  const float2 *qs;
+  float2 *qs_next;
   double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
   int stage;
 };
@@ -274,6 +280,43 @@ __device__ int solve_equilibrium(const EqEval &ev, const Params &P, const DevDat
 
 __device__ __forceinline__ void set_status(Clock *c, int bits) { atomicOr(&c->status, bits); }
 
+// ------------------------------------------------- FP32 pair ("double-float")
+// Unevaluated sums hi + lo of two FP32 numbers, with the error-free
+// transformations of Knuth (two-sum, TAOCP vol. 2, 4.2.2) and Dekker (two-product,
+// 1971; here with a fused multiply-add).  About 48 significant bits on the
+// FP32 pipe, which on this GPU issues 64 times faster than the FP64 pipe.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return DF{s, e};
+}
+__device__ __forceinline__ DF df_fast(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  DF s = df_two_sum(x.hi, y.hi);
+  return df_fast(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
+}
+__device__ __forceinline__ DF df_sub(DF x, DF y) { return df_add(x, DF{-y.hi, -y.lo}); }
+__device__ __forceinline__ DF df_mul(DF x, DF y) {
+  const float p = __fmul_rn(x.hi, y.hi);
+  float e = __fmaf_rn(x.hi, y.hi, -p);
+  e = __fmaf_rn(x.hi, y.lo, e);
+  e = __fmaf_rn(x.lo, y.hi, e);
+  return df_fast(p, e);
+}
+__device__ __forceinline__ DF df_of(float2 v) { return DF{v.x, v.y}; }
+// FP64 value as an FP32 pair (FP64 pipe: used once per cell, not per stencil row)
+__device__ __forceinline__ DF df_split(double x) {
+  const float hi = __double2float_rn(x);
+  return DF{hi, __double2float_rn(x - (double)hi)};
+}
+
 // --------------------------------------------------------- reconstruction
 template <class S, int EQ, int SRC, bool MIXED>
 __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, const StageArgs &a, const int i) {
@@ -369,20 +412,46 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   // equilibrium averages are differenced analytically,
   //   d rho = (q_j - q_0) - f (<phi>_0 - <phi>_j),
   //   d E   = (q_j - q_0) - K f^2 ((<phi>_0 - <phi>_j)(2 h_r - <phi>_j - <phi>_0) + var_j - var_0),
-  // so the O(h) equilibrium variation never cancels against the O(h) state
-  // variation in floating point.
+  // so the O(h) equilibrium variation cancels against the O(h) state variation
+  // in 48-bit FP32-pair arithmetic, never in plain FP32.
   const bool diff_form = MIXED && EQ && found && P.gamma2;
-  auto row_diff = [&](int j, R *dq) {
+  // Mixed form: the stencil rows come from the FP32 (hi, lo) pairs of the
+  // state, <phi> and var(phi); the differences and the analytic equilibrium
+  // differences are formed in FP32-pair arithmetic and rounded once to FP32.
+  DF own_q[NV], own_m1{0.f, 0.f}, own_var{0.f, 0.f}, df_f{0.f, 0.f}, df_kf2{0.f, 0.f}, df_2t{0.f, 0.f};
+  if (MIXED && (!EQ || diff_form)) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) own_q[v] = df_of(a.qs[v * ld + j0]);
     if (diff_form) {
-      const double m1_0 = d.phi_m1[j0], m1_j = d.phi_m1[j];
-      const double dm = m1_0 - m1_j;
-      double qd[NV];
+      own_m1 = df_of(d.m1s[j0]);
+      own_var = df_of(d.vars[j0]);
+      df_f = df_split(eqb.f);
+      df_kf2 = df_split(eqb.K * (eqb.f * eqb.f));
+      df_2t = df_split(2.0 * (eqb.hr - d.phi_m1[j0]));
+    }
+  }
+  auto row_diff = [&](int j, R *dq) {
+    if (MIXED && !EQ) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) qd[v] = q[v * ld + j] - u0[v];
-      qd[0] -= eqb.f * dm;
-      qd[NV - 1] -= eqb.K * (eqb.f * eqb.f) * (dm * (2.0 * eqb.hr - m1_j - m1_0) + (d.phi_var[j] - d.phi_var[j0]));
+      for (int v = 0; v < NV; ++v) {
+        const float2 x = a.qs[v * ld + j];
+        dq[v] = R(__fadd_rn(__fsub_rn(x.x, own_q[v].hi), __fsub_rn(x.y, own_q[v].lo)));
+      }
+    } else if (MIXED && diff_form) {
+      // rho_eq(j) - rho_eq(0) = f dm,
+      // E_eq(j) - E_eq(0) = K f^2 (dm (2 (h_r - <phi>_0) + dm) + var_j - var_0),
+      // dm = <phi>_0 - <phi>_j
+      const DF dm = df_sub(own_m1, df_of(d.m1s[j]));
 #pragma unroll
-      for (int v = 0; v < NV; ++v) dq[v] = R(qd[v]);
+      for (int v = 1; v < NV - 1; ++v) {
+        const float2 x = a.qs[v * ld + j];
+        dq[v] = R(__fadd_rn(__fsub_rn(x.x, own_q[v].hi), __fsub_rn(x.y, own_q[v].lo)));
+      }
+      const DF drho = df_sub(df_sub(df_of(a.qs[j]), own_q[0]), df_mul(df_f, dm));
+      dq[0] = R(__fadd_rn(drho.hi, drho.lo));
+      const DF t = df_add(df_mul(dm, df_add(df_2t, dm)), df_sub(df_of(d.vars[j]), own_var));
+      const DF dE = df_sub(df_sub(df_of(a.qs[(NV - 1) * ld + j]), own_q[NV - 1]), df_mul(df_kf2, t));
+      dq[NV - 1] = R(__fadd_rn(dE.hi, dE.lo));
     } else {
       double dq64[NV];
       load_dev(j, dq64);
@@ -1041,6 +1110,13 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
             dudt += c * (j == s ? tend[v] : (MIXED ? double(a.k32[j][v * ld + i]) : a.k[j][v * ld + i]));
         }
         un[v] = a.u0[v * ld + i] + dt * dudt;
+      }
+      if (MIXED) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const DF x = df_split(un[v]);
+          a.qs_next[v * ld + i] = make_float2(x.hi, x.lo);
+        }
       }
       if (!last) {
 #pragma unroll

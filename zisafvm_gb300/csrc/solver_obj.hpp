@@ -79,6 +79,7 @@ struct zfvm_solver {
   zfvm::DBuf<double> gphi_w;
   zfvm::DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
   zfvm::DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos, dev0;
+  zfvm::DBuf<float2> qsplit, m1s, vars;  // mixed: FP32 (hi, lo) pairs of u0, ux; <phi>, var(phi)
   zfvm::DBuf<zfvm::dev::Clock> clock;
   bool has_src = false, has_eq = false, mixed = false;
   cudaGraphExec_t graph = nullptr;
