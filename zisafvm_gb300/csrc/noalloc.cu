@@ -76,7 +76,8 @@ struct Layout {
   size_t zero_bytes = 0;
   // written by the kernels before they are read in the same call
   double *fv = nullptr, *dev0 = nullptr, *src = nullptr, *eqth = nullptr, *aos = nullptr;
-  float *fv32 = nullptr, *src32 = nullptr;
+  float *fv32 = nullptr, *src32 = nullptr, *dev032 = nullptr;
+  float2 *eq32 = nullptr;
   size_t bytes = 0;
 };
 
@@ -97,6 +98,8 @@ Layout plan(const zfvm_solver *s, unsigned char *base) {
   if (s->mixed) {
     L.fv32 = c.take<float>(fpts);
     L.dev0 = c.take<double>(nv * ld);
+    L.dev032 = c.take<float>(nv * ld);
+    if (s->has_eq) L.eq32 = c.take<float2>(3 * ld);
     if (s->has_src) L.src32 = c.take<float>(nv * ld);
   } else {
     L.fv = c.take<double>(fpts);
@@ -151,6 +154,8 @@ extern "C" int zfvm_rate_of_change_noalloc(zfvm_solver *s, double *tendency) {
     a.fv = L.fv;
     a.fv32 = L.fv32;
     a.dev0 = L.dev0;
+    a.dev032 = L.dev032;
+    a.eq32 = L.eq32;
     a.nf = L.nf;
     a.src = L.src;
     a.eqth = L.eqth;

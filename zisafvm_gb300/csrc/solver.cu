@@ -107,6 +107,8 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   a.fv = s->fv.p;
   a.fv32 = s->fv32.p;
   a.dev0 = s->dev0.p;
+  a.dev032 = s->dev032.p;
+  a.eq32 = s->eq32.p;
   a.nf = s->nfb.p;
   a.src = s->has_src ? s->srcb.p : nullptr;
   a.eqth = s->has_eq ? s->eqth.p : nullptr;
@@ -510,7 +512,17 @@ int build_solver(zfvm_solver *s) {
       };
       s->m1s.upload(pairs(h_phi_m1));
       s->vars.upload(pairs(h_phi_var));
+      s->eq32.alloc((size_t)3 * ld);
+      s->eq32.zero(s->stream);
+      std::vector<float2> hp((size_t)nqf * lde, make_float2(0.f, 0.f));
+      for (size_t k = 0; k < hp.size(); ++k) {
+        const float hi = (float)h_phi_fq[k];
+        hp[k] = make_float2(hi, (float)(h_phi_fq[k] - (double)hi));
+      }
+      s->phi_fq2.upload(hp);
     }
+    s->dev032.alloc((size_t)nv * ld);
+    s->dev032.zero(s->stream);
   } else {
     s->fv.alloc((size_t)nf * nqf * nv * ld);
   }
@@ -545,6 +557,7 @@ int build_solver(zfvm_solver *s) {
   D.wg32 = s->wg32.p;
   D.m1s = s->m1s.p;
   D.vars = s->vars.p;
+  D.phi_fq2 = s->phi_fq2.p;
   D.phi_var = s->phi_var.p;
   D.bloc = s->bloc.p;
   D.center = s->center.p;
@@ -575,7 +588,8 @@ int build_solver(zfvm_solver *s) {
   add(4 * (s->l2g.n + s->cface.n + s->fL.n + s->fR.n + s->src_map.n));
   add(4 * (s->pinv32.n + s->fv32.n + s->frame32.n + s->xfq32.n + s->xcq32.n + s->mom32.n + s->wg32.n + s->g32.n +
            s->mL32.n + s->mR32.n + s->src32.n + s->kbuf32.n));
-  add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n));
+  add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n + s->eq32.n + s->phi_fq2.n));
+  add(4 * s->dev032.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
            s->ux.n + s->kbuf.n + s->fv.n + s->nfb.n + s->srcb.n + s->eqth.n + s->tend.n + s->aos.n));
@@ -889,8 +903,8 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
     b += 4 * (NP * ld + nd * nd * lde + NC * ld + nf * nqf * nd * ld + nqc * nd * ld);  // pinv32 frame32 mom32 xfq32 xcq32
     b += 4 * (nv * lde + 2 * nd * lde + kst * nv * ld + nf * nqf * nv * ld);          // g32 mL32 mR32 kbuf32 fv32
     b += 8 * nv * ld;                                                                   // dev0
-    b += 8 * 2 * nv * ld;                                                               // qsplit
-    if (has_eq) b += 8 * 2 * ld;                                                        // m1s vars
+    b += 8 * 2 * nv * ld + 4 * nv * ld;                                                 // qsplit dev032
+    if (has_eq) b += 8 * 2 * ld + 8 * 3 * ld + 8 * nqf * lde;                           // m1s vars eq32 phi_fq2
     if (has_src) b += 4 * nv * ld + 8 * nd * ld + 4 * nqc * nd * ld;                   // src32 gphi_w wg32
   } else {
     b += 8 * (NP * ld + kst * nv * ld + nf * nqf * nv * ld + nv * lde);  // pinv kbuf fv nfb

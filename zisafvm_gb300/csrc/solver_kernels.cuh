@@ -90,6 +90,7 @@ struct DevData {
   const float *wg32;     // [NQC][ND][ld] w_q grad phi(x_q)
   const float2 *m1s;     // [ld] phi_m1 as an FP32 (hi, lo) pair
   const float2 *vars;    // [ld] phi_var as an FP32 (hi, lo) pair
+  const float2 *phi_fq2; // [NQF][lde] phi at the face points as FP32 (hi, lo) pairs
   Clock *clock;
 };
 
@@ -127,6 +128,10 @@ struct StageArgs {
   // bits of the FP64 value), and the pairs the update writes with its state
   const float2 *qs;
   float2 *qs_next;
+  // MIXED: FP32 copy of dev0 [NV][ld]; with gamma = 2 the bound equilibrium
+  // (h_r, f, K) as FP32 (hi, lo) pairs [3][ld]
+  float *dev032;
+  float2 *eq32;
   double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
   int stage;
 };
@@ -406,7 +411,16 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   }
   if (MIXED) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) a.dev0[v * ld + i] = dev0[v];
+    for (int v = 0; v < NV; ++v) {
+      a.dev0[v * ld + i] = dev0[v];
+      a.dev032[v * ld + i] = float(dev0[v]);
+    }
+    if (EQ && P.gamma2) {
+      const DF hr = df_split(eqb.hr), f = df_split(eqb.f), K = df_split(eqb.K);
+      a.eq32[i] = make_float2(hr.hi, hr.lo);
+      a.eq32[ld + i] = make_float2(f.hi, f.lo);
+      a.eq32[2 * ld + i] = make_float2(K.hi, K.lo);
+    }
   }
   // dev_j - dev_0 for a stencil cell j.  In the mixed form with gamma = 2 the
   // equilibrium averages are differenced analytically,
@@ -828,20 +842,39 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
       } else if (EQ && eq_found(a, ld, L) && eq_found(a, ld, R)) {
         // perturbation form around the left cell's equilibrium at the point:
         // F = (0, p_w n, 0) + [F32(w + dL, w + dR) - F32(w)] in the face frame
-        const double phi = d.phi_fq[qq * lde + e];
-        double rwL, EwL, rwR, EwR;
-        eq_bound(a, ld, L).at(ev, phi, rwL, EwL);
-        eq_bound(a, ld, R).at(ev, phi, rwR, EwR);
-        float cL[NV], cR[NV], dL[NV], dR[NV], df[NV];
-        cL[0] = float(a.dev0[L]);
-        cR[0] = float(a.dev0[R] + (rwR - rwL));
-        cL[NV - 1] = float(a.dev0[(NV - 1) * ld + L]);
-        cR[NV - 1] = float(a.dev0[(NV - 1) * ld + R] + (EwR - EwL));
-#pragma unroll
-        for (int v = 1; v < NV - 1; ++v) {
-          cL[v] = float(a.dev0[v * ld + L]);
-          cR[v] = float(a.dev0[v * ld + R]);
+        // base w = the left equilibrium at the point; the right side carries
+        // the difference of the two equilibria there
+        float rwL, EwL, drho, dE;
+        if (P.gamma2) {
+          // gamma = 2: rho = f (h_r - phi), E = K rho^2, in FP32-pair arithmetic
+          const DF phi = df_of(d.phi_fq2[qq * lde + e]);
+          const DF rL = df_mul(df_of(a.eq32[ld + L]), df_sub(df_of(a.eq32[L]), phi));
+          const DF rR = df_mul(df_of(a.eq32[ld + R]), df_sub(df_of(a.eq32[R]), phi));
+          const DF EL = df_mul(df_of(a.eq32[2 * ld + L]), df_mul(rL, rL));
+          const DF ER = df_mul(df_of(a.eq32[2 * ld + R]), df_mul(rR, rR));
+          const DF dr = df_sub(rR, rL), dEE = df_sub(ER, EL);
+          rwL = rL.hi;
+          EwL = EL.hi;
+          drho = __fadd_rn(dr.hi, dr.lo);
+          dE = __fadd_rn(dEE.hi, dEE.lo);
+        } else {
+          const double phi = d.phi_fq[qq * lde + e];
+          double rwL64, EwL64, rwR64, EwR64;
+          eq_bound(a, ld, L).at(ev, phi, rwL64, EwL64);
+          eq_bound(a, ld, R).at(ev, phi, rwR64, EwR64);
+          rwL = float(rwL64);
+          EwL = float(EwL64);
+          drho = float(rwR64 - rwL64);
+          dE = float(EwR64 - EwL64);
         }
+        float cL[NV], cR[NV], dL[NV], dR[NV], df[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          cL[v] = a.dev032[v * ld + L];
+          cR[v] = a.dev032[v * ld + R];
+        }
+        cR[0] += drho;
+        cR[NV - 1] += dE;
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           cL[v] += a.fv32[sL + (size_t)v * ld];
@@ -849,15 +882,16 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         }
         to_face32<NV, ND>(cL, d.frame32, lde, e, dL);
         to_face32<NV, ND>(cR, d.frame32, lde, e, dR);
+        const float gamma32 = float(P.gamma);
         if (FLUX == 0)
-          hllc_flux_dev<NV>(dL, dR, float(rwL), float(EwL), float(P.gamma), df);
+          hllc_flux_dev<NV>(dL, dR, rwL, EwL, gamma32, df);
         else
-          rusanov_flux_dev<NV>(dL, dR, float(rwL), float(EwL), float(P.gamma), df);
+          rusanov_flux_dev<NV>(dL, dR, rwL, EwL, gamma32, df);
         from_face32<NV, ND>(df, d.frame32, lde, e);
         // the baseline p_wL n cancels the left cell's own surface source term
         // exactly; the right cell keeps (p_wL - p_eqR) n
         const float wq = float(d.fqw[qq * lde + e]);
-        const float dpn = float((EwL - EwR) * ev.gm1) * wq;
+        const float dpn = -dE * (gamma32 - 1.f) * wq;
 #pragma unroll
         for (int v = 0; v < NV; ++v) g32[v] += wq * df[v];
 #pragma unroll
@@ -868,8 +902,8 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         float uL[NV], uR[NV], wL[NV], wR[NV], f32[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-          uL[v] = float(a.dev0[v * ld + L]) + a.fv32[sL + (size_t)v * ld];
-          uR[v] = float(a.dev0[v * ld + R]) + a.fv32[sR + (size_t)v * ld];
+          uL[v] = a.dev032[v * ld + L] + a.fv32[sL + (size_t)v * ld];
+          uR[v] = a.dev032[v * ld + R] + a.fv32[sR + (size_t)v * ld];
         }
         to_face32<NV, ND>(uL, d.frame32, lde, e, wL);
         to_face32<NV, ND>(uR, d.frame32, lde, e, wR);
