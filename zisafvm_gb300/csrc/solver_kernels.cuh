@@ -717,6 +717,21 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
   recon_cell<S, EQ, SRC, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// The 2D mixed reconstruction is latency-bound: this build of it is held to
+// 128 registers so four blocks of 128 threads fit on an SM.
+template <class S, int EQ, int SRC, bool MIXED>
+__global__ void __launch_bounds__(128, 4) k_reconstruct4(const DevData d, const Params P, StageArgs a) {
+  recon_cell<S, EQ, SRC, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <class S, int EQ, int SRC, bool MIXED>
+constexpr auto recon_kernel() {
+  if constexpr (MIXED && S::ND == 2)
+    return &k_reconstruct4<S, EQ, SRC, MIXED>;
+  else
+    return &k_reconstruct<S, EQ, SRC, MIXED>;
+}
+
 // ------------------------------------------------------------- face flux
 template <int NV, int ND, class T>
 __device__ __forceinline__ void to_face(const T *u, const double *fr, int lde, int e, T *w) {
@@ -1220,6 +1235,24 @@ __global__ void __launch_bounds__(128) km_reconstruct(const BatchInst *__restric
   }
 }
 
+template <class S, int EQ, int SRC, bool MIXED>
+__global__ void __launch_bounds__(128, 4) km_reconstruct4(const BatchInst *__restrict__ inst,
+                                                          const Tile *__restrict__ tiles, int n_tiles, int stage) {
+  for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    const Tile tl = tiles[t];
+    const BatchInst &I = inst[tl.slot];
+    recon_cell<S, EQ, SRC, MIXED>(I.d, I.P, I.a[stage], tl.begin + threadIdx.x);
+  }
+}
+
+template <class S, int EQ, int SRC, bool MIXED>
+constexpr auto batch_recon_kernel() {
+  if constexpr (MIXED && S::ND == 2)
+    return &km_reconstruct4<S, EQ, SRC, MIXED>;
+  else
+    return &km_reconstruct<S, EQ, SRC, MIXED>;
+}
+
 template <class S, int FLUX, int EQ, bool MIXED>
 __global__ void __launch_bounds__(128) km_face_flux(const BatchInst *__restrict__ inst,
                                                     const Tile *__restrict__ tiles, int n_tiles, int stage) {
@@ -1258,13 +1291,13 @@ void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_c
             gu = c.grid_update > 0 ? c.grid_update : n_ct;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    km_reconstruct<S, 1, 1, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 1, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
   else if (c.eq)
-    km_reconstruct<S, 1, 0, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 0, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
   else if (c.src)
-    km_reconstruct<S, 0, 1, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 1, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
   else
-    km_reconstruct<S, 0, 0, MIXED><<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 0, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
@@ -1300,11 +1333,11 @@ void batch_occupancy_t(const BatchCfg &c, int *blocks_per_sm) {
     return b;
   };
   if (c.mixed) {
-    blocks_per_sm[0] = occ((const void *)km_reconstruct<S, 1, 1, true>);
+    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, true>());
     blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, true>);
     blocks_per_sm[2] = occ((const void *)km_update<S, true>);
   } else {
-    blocks_per_sm[0] = occ((const void *)km_reconstruct<S, 1, 1, false>);
+    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, false>());
     blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, false>);
     blocks_per_sm[2] = occ((const void *)km_update<S, false>);
   }
@@ -1334,13 +1367,13 @@ void launch_stage_p(const DevData &D, const Params &P, StageArgs &a, const Launc
   const int nb = (c.n_cells + 127) / 128, nbe = (c.n_edges + 127) / 128;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    k_reconstruct<S, 1, 1, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 1, 1, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
   else if (c.eq)
-    k_reconstruct<S, 1, 0, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 1, 0, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
   else if (c.src)
-    k_reconstruct<S, 0, 1, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 0, 1, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
   else
-    k_reconstruct<S, 0, 0, MIXED><<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 0, 0, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
