@@ -422,6 +422,8 @@ def run_single_mesh(args, rank, world, local, pg):
                                  "perturbation_rel_l1": perturbation_rel_l1(u32, u64, u0, mask)}
         if scheme.equilibrium:
             line["well_balanced"] = well_balanced_residual(z, mesh, scheme, n_cmp)
+        if args.workload == "c2":
+            line["run_to_t_end"] = run_to_t_end(z, mesh, scheme, u0, 0.5)
     if rank == 0:
         try:
             line["cpu_baseline"] = cpu_baseline(raw, mesh, scheme, u0, desc)
@@ -430,6 +432,29 @@ def run_single_mesh(args, rank, world, local, pg):
         print(json.dumps(line), flush=True)
     if pg:
         pg.barrier()
+
+
+def run_to_t_end(z, mesh, scheme, u0, t_end: float) -> dict:
+    """The C2 run as specified: both forms from the same data to t_end with CFL
+    time steps (device-resident clock, graph replay), wall time of each, and
+    the mixed form's error against the FP64 form at t_end."""
+    import dataclasses
+    from metrics import perturbation_rel_l1, state_rel_l1
+    out = {"t_end": t_end}
+    states = {}
+    for name, prec in (("mixed", z.MIXED), ("fp64", z.FP64)):
+        s = z.Solver(mesh, dataclasses.replace(scheme, precision=prec))
+        s.set_state(u0)
+        t0 = time.perf_counter()
+        t, n = s.advance(t_end=t_end)
+        wall = time.perf_counter() - t0
+        states[name], _ = s.get_state()
+        out[name] = {"t": t, "steps": n, "wall_s": wall,
+                     "cell_stage_updates_per_s": mesh.n_cells * scheme.rk_stages * n / wall}
+        s.close()
+    out["error_vs_fp64"] = {"state_rel_l1": state_rel_l1(states["mixed"], states["fp64"]),
+                            "perturbation_rel_l1": perturbation_rel_l1(states["mixed"], states["fp64"], u0)}
+    return out
 
 
 def well_balanced_residual(z, mesh, scheme, steps: int) -> dict:

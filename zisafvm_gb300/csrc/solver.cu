@@ -123,7 +123,10 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   for (int k = 0; k < 4; ++k) a.k32[k] = s->kbuf32.p ? s->kbuf32.p + (size_t)k * s->nv * s->ld : nullptr;
   a.stage = stage;
   const bool last = stage == s->P.n_stages - 1;
-  for (int j = 0; j < 4; ++j) a.coef[j] = last ? s->P.b[j] : (stage + 1 < 4 ? s->P.a[stage + 1][j] : 0.0);
+  for (int j = 0; j < 4; ++j) {
+    a.coef[j] = last ? s->P.b[j] : (stage + 1 < 4 ? s->P.a[stage + 1][j] : 0.0);
+    a.coef32[j] = (float)a.coef[j];
+  }
   if (s->qsplit.p) {
     const size_t half = (size_t)s->nv * s->ld;
     a.qs = s->qsplit.p + (stage == 0 ? 0 : half);

@@ -133,6 +133,7 @@ struct StageArgs {
   float *dev032;
   float2 *eq32;
   double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
+  float coef32[4];   // the same row rounded to FP32 (mixed form)
   int stage;
 };
 
@@ -1056,6 +1057,18 @@ __device__ __forceinline__ double cfl_candidate(const double *u, double gamma, d
   return r / (sqrt(v2) + c);
 }
 
+// The same quantity with one reciprocal instead of four divisions (mixed form):
+// r / (|m| / rho + sqrt(gamma p / rho)), p = (gamma - 1) (E - |m|^2 / (2 rho)).
+template <int NV>
+__device__ __forceinline__ double cfl_candidate_1rcp(const double *u, double gamma, double r) {
+  double m2 = 0.0;
+#pragma unroll
+  for (int k = 1; k < NV - 1; ++k) m2 += u[k] * u[k];
+  const double ir = 1.0 / u[0];
+  const double p = (u[NV - 1] - 0.5 * m2 * ir) * (gamma - 1.0);
+  return r / (sqrt(m2) * ir + sqrt(gamma * p * ir));
+}
+
 __device__ __forceinline__ void block_min_to_clock(double cand, Clock *clock) {
   // positive doubles order like their bit patterns; NaN bits sort above +inf
   unsigned long long bits = __double_as_longlong(cand);
@@ -1091,9 +1104,9 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
   if (!d.clock->done && i < d.n_cells && (d.flags[i] & kInterior)) {
     const int ld = d.ld, lde = d.lde;
     double tend[NV];
+    float t32[NV];  // mixed form: the tendency in FP32
     if (MIXED) {
       // deviation-sized terms only: FP32 sums
-      float t32[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) t32[v] = 0.f;
 #pragma unroll
@@ -1150,15 +1163,27 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
       double un[NV];
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        double dudt = 0.0;
+        if (MIXED) {
+          // FP32 stage tendencies combined in FP32; the cell average itself
+          // accumulates in FP64
+          float dudt = 0.f;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          if (j > s) break;
-          const double c = a.coef[j];
-          if (c != 0.0)
-            dudt += c * (j == s ? tend[v] : (MIXED ? double(a.k32[j][v * ld + i]) : a.k[j][v * ld + i]));
+          for (int j = 0; j < 4; ++j) {
+            if (j > s) break;
+            const float c = a.coef32[j];
+            if (c != 0.f) dudt += c * (j == s ? t32[v] : a.k32[j][v * ld + i]);
+          }
+          un[v] = a.u0[v * ld + i] + dt * double(dudt);
+        } else {
+          double dudt = 0.0;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            if (j > s) break;
+            const double c = a.coef[j];
+            if (c != 0.0) dudt += c * (j == s ? tend[v] : a.k[j][v * ld + i]);
+          }
+          un[v] = a.u0[v * ld + i] + dt * dudt;
         }
-        un[v] = a.u0[v * ld + i] + dt * dudt;
       }
       if (MIXED) {
 #pragma unroll
@@ -1171,7 +1196,7 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           if (MIXED)
-            a.k32[s][v * ld + i] = float(tend[v]);
+            a.k32[s][v * ld + i] = t32[v];
           else
             a.k[s][v * ld + i] = tend[v];
           a.ux[v * ld + i] = un[v];
@@ -1179,7 +1204,7 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
       } else {
 #pragma unroll
         for (int v = 0; v < NV; ++v) a.u0[v * ld + i] = un[v];
-        cand = cfl_candidate<NV>(un, P.gamma, d.r_eff[i]);
+        cand = MIXED ? cfl_candidate_1rcp<NV>(un, P.gamma, d.r_eff[i]) : cfl_candidate<NV>(un, P.gamma, d.r_eff[i]);
         bool finite = true;
 #pragma unroll
         for (int v = 0; v < NV; ++v) finite = finite && isfinite(un[v]);
