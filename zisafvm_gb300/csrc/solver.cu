@@ -63,15 +63,15 @@ __global__ void k_soa_to_aos(const double *soa, double *aos, int n, int ld, int 
   for (int v = 0; v < 5; ++v) aos[i * 5 + v] = r[v];
 }
 
-// FP64 state -> the state pairs of the gather records (mixed form), for a
-// state set from the host
-template <int NV>
-__global__ void k_split(const double *soa, float4 *rec, int n, int ld) {
+// FP64 state -> FP32 (hi, lo) pairs (mixed form), for a state set from the host
+__global__ void k_split(const double *soa, float2 *pairs, int n, int ld, int nv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  DF q[NV];
-  for (int v = 0; v < NV; ++v) q[v] = df_split(soa[(size_t)v * ld + i]);
-  rec_store_state<NV>(rec + (size_t)i * RecLayout<NV>::W, q);
+  for (int v = 0; v < nv; ++v) {
+    const double x = soa[(size_t)v * ld + i];
+    const float hi = __double2float_rn(x);
+    pairs[(size_t)v * ld + i] = make_float2(hi, __double2float_rn(x - (double)hi));
+  }
 }
 
 }  // namespace dev
@@ -127,10 +127,10 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
     a.coef[j] = last ? s->P.b[j] : (stage + 1 < 4 ? s->P.a[stage + 1][j] : 0.0);
     a.coef32[j] = (float)a.coef[j];
   }
-  if (s->recs.p) {
-    const size_t half = (size_t)s->ld * ((s->nv + 3) / 2);
-    a.rec = s->recs.p + (stage == 0 ? 0 : half);
-    a.rec_next = s->recs.p + (last ? 0 : half);
+  if (s->qsplit.p) {
+    const size_t half = (size_t)s->nv * s->ld;
+    a.qs = s->qsplit.p + (stage == 0 ? 0 : half);
+    a.qs_next = s->qsplit.p + (last ? 0 : half);
   }
   return a;
 }
@@ -502,26 +502,19 @@ int build_solver(zfvm_solver *s) {
     }
     s->fv32.alloc((size_t)nf * nqf * nv * ld);
     s->dev0.alloc((size_t)nv * ld);
-    {
-      // gather records of u0 and ux: state pairs zero until set, <phi> and
-      // var(phi) pairs (pairs nv and nv + 1) fixed
-      const int W = (nv + 3) / 2;
-      std::vector<float> rec((size_t)2 * ld * W * 4, 0.f);
-      if (s->has_eq)
-        for (int half = 0; half < 2; ++half)
-          for (index_t i = 0; i < n; ++i)
-            for (int k = 0; k < 2; ++k) {
-              const double x = k == 0 ? h_phi_m1[i] : h_phi_var[i];
-              const int pr = nv + k;
-              const size_t at = (((size_t)half * ld + i) * W + pr / 2) * 4 + (pr % 2) * 2;
-              rec[at] = (float)x;
-              rec[at + 1] = (float)(x - (double)rec[at]);
-            }
-      std::vector<float4> rec4((size_t)2 * ld * W);
-      std::memcpy(rec4.data(), rec.data(), rec.size() * sizeof(float));
-      s->recs.upload(rec4);
-    }
+    s->qsplit.alloc((size_t)2 * nv * ld);
+    s->qsplit.zero(s->stream);
     if (s->has_eq) {
+      auto pairs = [&](const std::vector<double> &x) {
+        std::vector<float2> out(ld, make_float2(0.f, 0.f));
+        for (index_t i = 0; i < n; ++i) {
+          const float hi = (float)x[i];
+          out[i] = make_float2(hi, (float)(x[i] - (double)hi));
+        }
+        return out;
+      };
+      s->m1s.upload(pairs(h_phi_m1));
+      s->vars.upload(pairs(h_phi_var));
       s->eq32.alloc((size_t)3 * ld);
       s->eq32.zero(s->stream);
       std::vector<float2> hp((size_t)nqf * lde, make_float2(0.f, 0.f));
@@ -565,6 +558,8 @@ int build_solver(zfvm_solver *s) {
   D.mom32 = s->mom32.p;
   D.gphi_w = s->gphi_w.p;
   D.wg32 = s->wg32.p;
+  D.m1s = s->m1s.p;
+  D.vars = s->vars.p;
   D.phi_fq2 = s->phi_fq2.p;
   D.phi_var = s->phi_var.p;
   D.bloc = s->bloc.p;
@@ -596,7 +591,7 @@ int build_solver(zfvm_solver *s) {
   add(4 * (s->l2g.n + s->cface.n + s->fL.n + s->fR.n + s->src_map.n));
   add(4 * (s->pinv32.n + s->fv32.n + s->frame32.n + s->xfq32.n + s->xcq32.n + s->mom32.n + s->wg32.n + s->g32.n +
            s->mL32.n + s->mR32.n + s->src32.n + s->kbuf32.n));
-  add(8 * (s->gphi_w.n + s->eq32.n + s->phi_fq2.n) + 16 * s->recs.n);
+  add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n + s->eq32.n + s->phi_fq2.n));
   add(4 * s->dev032.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
@@ -687,11 +682,8 @@ extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
   CK(cudaMemcpyAsync(s->aos.p, cvars, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
   k_aos_to_soa<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->aos.p, s->u0.p, (int)n, s->ld, s->nv);
   CK(cudaGetLastError());
-  if (s->recs.p) {
-    if (s->nv == 4)
-      k_split<4><<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->recs.p, (int)n, s->ld);
-    else
-      k_split<5><<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->recs.p, (int)n, s->ld);
+  if (s->qsplit.p) {
+    k_split<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->qsplit.p, (int)n, s->ld, s->nv);
     CK(cudaGetLastError());
   }
   Clock c{};
@@ -914,8 +906,8 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
     b += 4 * (NP * ld + nd * nd * lde + NC * ld + nf * nqf * nd * ld + nqc * nd * ld);  // pinv32 frame32 mom32 xfq32 xcq32
     b += 4 * (nv * lde + 2 * nd * lde + kst * nv * ld + nf * nqf * nv * ld);          // g32 mL32 mR32 kbuf32 fv32
     b += 8 * nv * ld;                                                                   // dev0
-    b += 16 * 2 * ld * ((nv + 3) / 2) + 4 * nv * ld;                                    // recs dev032
-    if (has_eq) b += 8 * 3 * ld + 8 * nqf * lde;                                        // eq32 phi_fq2
+    b += 8 * 2 * nv * ld + 4 * nv * ld;                                                 // qsplit dev032
+    if (has_eq) b += 8 * 2 * ld + 8 * 3 * ld + 8 * nqf * lde;                           // m1s vars eq32 phi_fq2
     if (has_src) b += 4 * nv * ld + 8 * nd * ld + 4 * nqc * nd * ld;                   // src32 gphi_w wg32
   } else {
     b += 8 * (NP * ld + kst * nv * ld + nf * nqf * nv * ld + nv * lde);  // pinv kbuf fv nfb

@@ -88,6 +88,8 @@ struct DevData {
   const float *mom32;    // [NC][ld]
   const double *gphi_w;  // [ND][ld] sum_q w_q grad phi(x_q) over the cell
   const float *wg32;     // [NQC][ND][ld] w_q grad phi(x_q)
+  const float2 *m1s;     // [ld] phi_m1 as an FP32 (hi, lo) pair
+  const float2 *vars;    // [ld] phi_var as an FP32 (hi, lo) pair
   const float2 *phi_fq2; // [NQF][lde] phi at the face points as FP32 (hi, lo) pairs
   Clock *clock;
 };
@@ -122,10 +124,10 @@ struct StageArgs {
   // (tend_L += -G + mL, tend_R += G + mR), FP32 source [NV][ld], FP32 stage
   // tendencies [NV][ld]
   float *g32, *mL32, *mR32, *src32, *k32[4];
-  // MIXED: per-cell gather records of the stage state (RecLayout) and the
-  // records the update writes with its state
-  const float4 *rec;
-  float4 *rec_next;
+  // MIXED: the stage state as FP32 (hi, lo) pairs [NV][ld] (hi + lo carries 48
+  // bits of the FP64 value), and the pairs the update writes with its state
+  const float2 *qs;
+  float2 *qs_next;
   // MIXED: FP32 copy of dev0 [NV][ld]; with gamma = 2 the bound equilibrium
   // (h_r, f, K) as FP32 (hi, lo) pairs [3][ld]
   float *dev032;
@@ -321,32 +323,6 @@ __device__ __forceinline__ DF df_split(double x) {
   return DF{hi, __double2float_rn(x - (double)hi)};
 }
 
-// Mixed form gather record of one cell: everything a stencil row reads from a
-// neighbour, as FP32 (hi, lo) pairs packed in float4s -- the NV conserved
-// variables, then <phi> and var(phi) -- so a row costs W 128-bit loads from
-// one 48-byte (2D) or 64-byte (3D) record instead of NV + 2 scattered loads.
-// Pair p sits in float4 p / 2, half p % 2.
-template <int NV>
-struct RecLayout {
-  static constexpr int W = (NV + 3) / 2;   // float4s per cell
-  static constexpr int WQ = (NV + 1) / 2;  // float4s holding the state pairs
-};
-__device__ __forceinline__ DF rec_pair(const float4 *r, int p) {
-  const float4 &x = r[p >> 1];
-  return (p & 1) ? DF{x.z, x.w} : DF{x.x, x.y};
-}
-// write the NV state pairs of one cell, leaving <phi>, var(phi) in place
-template <int NV>
-__device__ __forceinline__ void rec_store_state(float4 *rec, const DF *q) {
-#pragma unroll
-  for (int p = 0; p < NV; p += 2) {
-    if (p + 1 < NV)
-      rec[p >> 1] = make_float4(q[p].hi, q[p].lo, q[p + 1].hi, q[p + 1].lo);
-    else
-      *reinterpret_cast<float2 *>(&rec[p >> 1]) = make_float2(q[p].hi, q[p].lo);
-  }
-}
-
 // --------------------------------------------------------- reconstruction
 template <class S, int EQ, int SRC, bool MIXED>
 __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, const StageArgs &a, const int i) {
@@ -457,17 +433,13 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   // Mixed form: the stencil rows come from the FP32 (hi, lo) pairs of the
   // state, <phi> and var(phi); the differences and the analytic equilibrium
   // differences are formed in FP32-pair arithmetic and rounded once to FP32.
-  using RL = RecLayout<NV>;
   DF own_q[NV], own_m1{0.f, 0.f}, own_var{0.f, 0.f}, df_f{0.f, 0.f}, df_kf2{0.f, 0.f}, df_2t{0.f, 0.f};
   if (MIXED && (!EQ || diff_form)) {
-    float4 r[RL::W];
 #pragma unroll
-    for (int w = 0; w < RL::W; ++w) r[w] = (EQ || w < RL::WQ) ? a.rec[(size_t)j0 * RL::W + w] : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) own_q[v] = rec_pair(r, v);
+    for (int v = 0; v < NV; ++v) own_q[v] = df_of(a.qs[v * ld + j0]);
     if (diff_form) {
-      own_m1 = rec_pair(r, NV);
-      own_var = rec_pair(r, NV + 1);
+      own_m1 = df_of(d.m1s[j0]);
+      own_var = df_of(d.vars[j0]);
       df_f = df_split(eqb.f);
       df_kf2 = df_split(eqb.K * (eqb.f * eqb.f));
       df_2t = df_split(2.0 * (eqb.hr - d.phi_m1[j0]));
@@ -475,31 +447,25 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   }
   auto row_diff = [&](int j, R *dq) {
     if (MIXED && !EQ) {
-      float4 r[RL::WQ];
-#pragma unroll
-      for (int w = 0; w < RL::WQ; ++w) r[w] = a.rec[(size_t)j * RL::W + w];
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const DF x = rec_pair(r, v);
-        dq[v] = R(__fadd_rn(__fsub_rn(x.hi, own_q[v].hi), __fsub_rn(x.lo, own_q[v].lo)));
+        const float2 x = a.qs[v * ld + j];
+        dq[v] = R(__fadd_rn(__fsub_rn(x.x, own_q[v].hi), __fsub_rn(x.y, own_q[v].lo)));
       }
     } else if (MIXED && diff_form) {
       // rho_eq(j) - rho_eq(0) = f dm,
       // E_eq(j) - E_eq(0) = K f^2 (dm (2 (h_r - <phi>_0) + dm) + var_j - var_0),
       // dm = <phi>_0 - <phi>_j
-      float4 r[RL::W];
-#pragma unroll
-      for (int w = 0; w < RL::W; ++w) r[w] = a.rec[(size_t)j * RL::W + w];
-      const DF dm = df_sub(own_m1, rec_pair(r, NV));
+      const DF dm = df_sub(own_m1, df_of(d.m1s[j]));
 #pragma unroll
       for (int v = 1; v < NV - 1; ++v) {
-        const DF x = rec_pair(r, v);
-        dq[v] = R(__fadd_rn(__fsub_rn(x.hi, own_q[v].hi), __fsub_rn(x.lo, own_q[v].lo)));
+        const float2 x = a.qs[v * ld + j];
+        dq[v] = R(__fadd_rn(__fsub_rn(x.x, own_q[v].hi), __fsub_rn(x.y, own_q[v].lo)));
       }
-      const DF drho = df_sub(df_sub(rec_pair(r, 0), own_q[0]), df_mul(df_f, dm));
+      const DF drho = df_sub(df_sub(df_of(a.qs[j]), own_q[0]), df_mul(df_f, dm));
       dq[0] = R(__fadd_rn(drho.hi, drho.lo));
-      const DF t = df_add(df_mul(dm, df_add(df_2t, dm)), df_sub(rec_pair(r, NV + 1), own_var));
-      const DF dE = df_sub(df_sub(rec_pair(r, NV - 1), own_q[NV - 1]), df_mul(df_kf2, t));
+      const DF t = df_add(df_mul(dm, df_add(df_2t, dm)), df_sub(df_of(d.vars[j]), own_var));
+      const DF dE = df_sub(df_sub(df_of(a.qs[(NV - 1) * ld + j]), own_q[NV - 1]), df_mul(df_kf2, t));
       dq[NV - 1] = R(__fadd_rn(dE.hi, dE.lo));
     } else {
       double dq64[NV];
@@ -1220,10 +1186,11 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
         }
       }
       if (MIXED) {
-        DF x[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) x[v] = df_split(un[v]);
-        rec_store_state<NV>(a.rec_next + (size_t)i * RecLayout<NV>::W, x);
+        for (int v = 0; v < NV; ++v) {
+          const DF x = df_split(un[v]);
+          a.qs_next[v * ld + i] = make_float2(x.hi, x.lo);
+        }
       }
       if (!last) {
 #pragma unroll

@@ -79,7 +79,7 @@ struct zfvm_solver {
   zfvm::DBuf<double> gphi_w;
   zfvm::DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
   zfvm::DBuf<double> u0, ux, kbuf, fv, nfb, srcb, eqth, tend, aos, dev0;
-  zfvm::DBuf<float4> recs;               // mixed: gather records of u0 and ux (RecLayout)
+  zfvm::DBuf<float2> qsplit, m1s, vars;  // mixed: FP32 (hi, lo) pairs of u0, ux; <phi>, var(phi)
   zfvm::DBuf<float2> eq32, phi_fq2;       // mixed + equilibrium: (h_r, f, K) pairs; phi at face points
   zfvm::DBuf<float> dev032;               // mixed: FP32 copy of the cell deviation
   zfvm::DBuf<zfvm::dev::Clock> clock;
