@@ -317,6 +317,14 @@ __device__ __forceinline__ DF df_mul(DF x, DF y) {
   return df_fast(p, e);
 }
 __device__ __forceinline__ DF df_of(float2 v) { return DF{v.x, v.y}; }
+// x - y for two pairs whose hi parts lie within a factor of two of each other
+// (neighbouring cell averages, or a difference and the equilibrium variation
+// it nearly cancels): the hi difference is then exact (Sterbenz's lemma), so
+// the result needs no renormalisation.  Outside that range the hi difference
+// is rounded once, a relative error of 2^-24 of a difference that is then
+// large -- the precision the result is rounded to anyway.
+__device__ __forceinline__ DF df_sub_close(DF x, DF y) { return DF{__fsub_rn(x.hi, y.hi), __fsub_rn(x.lo, y.lo)}; }
+__device__ __forceinline__ float df_round(DF x) { return __fadd_rn(x.hi, x.lo); }
 // FP64 value as an FP32 pair (FP64 pipe: used once per cell, not per stencil row)
 __device__ __forceinline__ DF df_split(double x) {
   const float hi = __double2float_rn(x);
@@ -456,17 +464,21 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       // rho_eq(j) - rho_eq(0) = f dm,
       // E_eq(j) - E_eq(0) = K f^2 (dm (2 (h_r - <phi>_0) + dm) + var_j - var_0),
       // dm = <phi>_0 - <phi>_j
+      // <phi> may differ by more than a factor of two near the centre of the
+      // potential: full two-sum there
       const DF dm = df_sub(own_m1, df_of(d.m1s[j]));
 #pragma unroll
       for (int v = 1; v < NV - 1; ++v) {
         const float2 x = a.qs[v * ld + j];
         dq[v] = R(__fadd_rn(__fsub_rn(x.x, own_q[v].hi), __fsub_rn(x.y, own_q[v].lo)));
       }
-      const DF drho = df_sub(df_sub(df_of(a.qs[j]), own_q[0]), df_mul(df_f, dm));
-      dq[0] = R(__fadd_rn(drho.hi, drho.lo));
-      const DF t = df_add(df_mul(dm, df_add(df_2t, dm)), df_sub(df_of(d.vars[j]), own_var));
-      const DF dE = df_sub(df_sub(df_of(a.qs[(NV - 1) * ld + j]), own_q[NV - 1]), df_mul(df_kf2, t));
-      dq[NV - 1] = R(__fadd_rn(dE.hi, dE.lo));
+      dq[0] = R(df_round(df_sub_close(df_sub_close(df_of(a.qs[j]), own_q[0]), df_mul(df_f, dm))));
+      // 2 (h_r - <phi>_0) + dm with |dm| << |2 (h_r - <phi>_0)|
+      const float sh = __fadd_rn(df_2t.hi, dm.hi);
+      const DF sum{sh, __fadd_rn(__fsub_rn(dm.hi, __fsub_rn(sh, df_2t.hi)), __fadd_rn(df_2t.lo, dm.lo))};
+      const DF t = df_add(df_mul(dm, sum), df_sub_close(df_of(d.vars[j]), own_var));
+      const DF dE = df_sub_close(df_sub_close(df_of(a.qs[(NV - 1) * ld + j]), own_q[NV - 1]), df_mul(df_kf2, t));
+      dq[NV - 1] = R(df_round(dE));
     } else {
       double dq64[NV];
       load_dev(j, dq64);
