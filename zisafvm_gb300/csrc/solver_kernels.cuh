@@ -332,6 +332,15 @@ __device__ __forceinline__ DF df_split(double x) {
 }
 
 // --------------------------------------------------------- reconstruction
+// The 2D mixed reconstruction keeps its stencil-row differences in dynamic
+// shared memory: (MAXL - 1) rows x NV floats per thread.
+template <class S, bool MIXED>
+constexpr bool kRowsInShared = MIXED && S::ND == 2;
+template <class S, bool MIXED>
+constexpr size_t recon_smem_bytes(int threads) {
+  return kRowsInShared<S, MIXED> ? (size_t)(S::MAXL - 1) * S::NV * threads * sizeof(float) : 0;
+}
+
 template <class S, int EQ, int SRC, bool MIXED>
 __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, const StageArgs &a, const int i) {
   using R = std::conditional_t<MIXED, float, double>;
@@ -493,35 +502,83 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   for (int c = 0; c < S::C0; ++c)
 #pragma unroll
     for (int v = 0; v < NV; ++v) b0[c][v] = R(0);
-#pragma unroll 2
-  for (int r = 0; r < S::R0; ++r) {
-    R dq[NV];
-    row_diff(d.l2g[(r + 1) * ld + i], dq);
-#pragma unroll
-    for (int c = 0; c < S::C0; ++c) {
-      const R pc = MIXED ? R(d.pinv32[(c * S::R0 + r) * ld + i]) : R(d.pinv[(c * S::R0 + r) * ld + i]);
-#pragma unroll
-      for (int v = 0; v < NV; ++v) b0[c][v] += pc * dq[v];
-    }
-  }
   R bb[S::NB][S::CB][NV];
 #pragma unroll
-  for (int k = 0; k < S::NB; ++k) {
+  for (int k = 0; k < S::NB; ++k)
 #pragma unroll
     for (int c = 0; c < S::CB; ++c)
 #pragma unroll
       for (int v = 0; v < NV; ++v) bb[k][c][v] = R(0);
-#pragma unroll
-    for (int r = 0; r < S::RB; ++r) {
-      const int l = d.bloc[(k * S::RB + r) * ld + i];
+  if constexpr (kRowsInShared<S, MIXED>) {
+    // The one-sided stencils mostly reuse cells of the central one (the
+    // combined 2D stencil averages about 11 cells for 19 rows), so every
+    // distinct stencil cell is differenced once into shared memory,
+    // rows[((l - 1) * NV + v) * blockDim.x + thread], and all fits read it there.
+    extern __shared__ float rows_smem[];
+    const int bd = blockDim.x, tid = threadIdx.x;
+#pragma unroll 2
+    for (int l = 1; l < S::MAXL; ++l) {
+      const int j = d.l2g[l * ld + i];
       R dq[NV];
-      row_diff(d.l2g[l * ld + i], dq);
+      if (j != j0) {
+        row_diff(j, dq);
+      } else {
 #pragma unroll
-      for (int c = 0; c < S::CB; ++c) {
-        const int pi = (S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i;
-        const R pc = MIXED ? R(d.pinv32[pi]) : R(d.pinv[pi]);
+        for (int v = 0; v < NV; ++v) dq[v] = R(0);
+      }
 #pragma unroll
-        for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
+      for (int v = 0; v < NV; ++v) rows_smem[((l - 1) * NV + v) * bd + tid] = dq[v];
+    }
+#pragma unroll 2
+    for (int r = 0; r < S::R0; ++r) {
+#pragma unroll
+      for (int c = 0; c < S::C0; ++c) {
+        const R pc = R(d.pinv32[(c * S::R0 + r) * ld + i]);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) b0[c][v] += pc * rows_smem[(r * NV + v) * bd + tid];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < S::NB; ++k)
+#pragma unroll
+      for (int r = 0; r < S::RB; ++r) {
+        const int l = d.bloc[(k * S::RB + r) * ld + i];
+        R dq[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) dq[v] = l > 0 ? rows_smem[((l - 1) * NV + v) * bd + tid] : R(0);
+#pragma unroll
+        for (int c = 0; c < S::CB; ++c) {
+          const R pc = R(d.pinv32[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i]);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
+        }
+      }
+  } else {
+#pragma unroll 2
+    for (int r = 0; r < S::R0; ++r) {
+      R dq[NV];
+      row_diff(d.l2g[(r + 1) * ld + i], dq);
+#pragma unroll
+      for (int c = 0; c < S::C0; ++c) {
+        const R pc = MIXED ? R(d.pinv32[(c * S::R0 + r) * ld + i]) : R(d.pinv[(c * S::R0 + r) * ld + i]);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) b0[c][v] += pc * dq[v];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < S::NB; ++k) {
+#pragma unroll
+      for (int r = 0; r < S::RB; ++r) {
+        const int l = d.bloc[(k * S::RB + r) * ld + i];
+        R dq[NV];
+        row_diff(d.l2g[l * ld + i], dq);
+#pragma unroll
+        for (int c = 0; c < S::CB; ++c) {
+          const int pi = (S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i;
+          const R pc = MIXED ? R(d.pinv32[pi]) : R(d.pinv[pi]);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
+        }
       }
     }
   }
@@ -1328,13 +1385,13 @@ void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_c
             gu = c.grid_update > 0 ? c.grid_update : n_ct;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    batch_recon_kernel<S, 1, 1, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   else if (c.eq)
-    batch_recon_kernel<S, 1, 0, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   else if (c.src)
-    batch_recon_kernel<S, 0, 1, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   else
-    batch_recon_kernel<S, 0, 0, MIXED>()<<<gr, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
@@ -1364,13 +1421,13 @@ void launch_batch_stage_t(const BatchInst *inst, const Tile *ct, int n_ct, const
 // Occupancy-limited block counts of the three batch kernels (for the autotuner).
 template <class S>
 void batch_occupancy_t(const BatchCfg &c, int *blocks_per_sm) {
-  auto occ = [](const void *k) {
+  auto occ = [](const void *k, size_t smem = 0) {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 128, smem);
     return b;
   };
   if (c.mixed) {
-    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, true>());
+    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, true>(), recon_smem_bytes<S, true>(128));
     blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, true>);
     blocks_per_sm[2] = occ((const void *)km_update<S, true>);
   } else {
@@ -1404,13 +1461,13 @@ void launch_stage_p(const DevData &D, const Params &P, StageArgs &a, const Launc
   const int nb = (c.n_cells + 127) / 128, nbe = (c.n_edges + 127) / 128;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    recon_kernel<S, 1, 1, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 1, 1, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
   else if (c.eq)
-    recon_kernel<S, 1, 0, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 1, 0, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
   else if (c.src)
-    recon_kernel<S, 0, 1, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 0, 1, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
   else
-    recon_kernel<S, 0, 0, MIXED>()<<<nb, 128, 0, c.stream>>>(D, P, a);
+    recon_kernel<S, 0, 0, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
