@@ -332,13 +332,15 @@ __device__ __forceinline__ DF df_split(double x) {
 }
 
 // --------------------------------------------------------- reconstruction
-// The 2D mixed reconstruction keeps its stencil-row differences in dynamic
-// shared memory: (MAXL - 1) rows x NV floats per thread.
-template <class S, bool MIXED>
-constexpr bool kRowsInShared = MIXED && S::ND == 2;
-template <class S, bool MIXED>
+// The 2D mixed well-balanced reconstruction, whose stencil rows cost FP32-pair
+// arithmetic, keeps the row differences in dynamic shared memory: (MAXL - 1)
+// rows x NV floats per thread.  Elsewhere rows are cheap and the L1 cache is
+// worth more than the shared memory.
+template <class S, int EQ, bool MIXED>
+constexpr bool kRowsInShared = MIXED && EQ && S::ND == 2;
+template <class S, int EQ, bool MIXED>
 constexpr size_t recon_smem_bytes(int threads) {
-  return kRowsInShared<S, MIXED> ? (size_t)(S::MAXL - 1) * S::NV * threads * sizeof(float) : 0;
+  return kRowsInShared<S, EQ, MIXED> ? (size_t)(S::MAXL - 1) * S::NV * threads * sizeof(float) : 0;
 }
 
 template <class S, int EQ, int SRC, bool MIXED>
@@ -509,7 +511,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     for (int c = 0; c < S::CB; ++c)
 #pragma unroll
       for (int v = 0; v < NV; ++v) bb[k][c][v] = R(0);
-  if constexpr (kRowsInShared<S, MIXED>) {
+  if constexpr (kRowsInShared<S, EQ, MIXED>) {
     // The one-sided stencils mostly reuse cells of the central one (the
     // combined 2D stencil averages about 11 cells for 19 rows), so every
     // distinct stencil cell is differenced once into shared memory,
@@ -1385,13 +1387,13 @@ void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_c
             gu = c.grid_update > 0 ? c.grid_update : n_ct;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    batch_recon_kernel<S, 1, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   else if (c.eq)
-    batch_recon_kernel<S, 1, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   else if (c.src)
-    batch_recon_kernel<S, 0, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   else
-    batch_recon_kernel<S, 0, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
@@ -1427,7 +1429,7 @@ void batch_occupancy_t(const BatchCfg &c, int *blocks_per_sm) {
     return b;
   };
   if (c.mixed) {
-    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, true>(), recon_smem_bytes<S, true>(128));
+    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, true>(), recon_smem_bytes<S, 1, true>(128));
     blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, true>);
     blocks_per_sm[2] = occ((const void *)km_update<S, true>);
   } else {
@@ -1461,13 +1463,13 @@ void launch_stage_p(const DevData &D, const Params &P, StageArgs &a, const Launc
   const int nb = (c.n_cells + 127) / 128, nbe = (c.n_edges + 127) / 128;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    recon_kernel<S, 1, 1, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
+    recon_kernel<S, 1, 1, MIXED>()<<<nb, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(D, P, a);
   else if (c.eq)
-    recon_kernel<S, 1, 0, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
+    recon_kernel<S, 1, 0, MIXED>()<<<nb, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(D, P, a);
   else if (c.src)
-    recon_kernel<S, 0, 1, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
+    recon_kernel<S, 0, 1, MIXED>()<<<nb, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(D, P, a);
   else
-    recon_kernel<S, 0, 0, MIXED>()<<<nb, 128, recon_smem_bytes<S, MIXED>(128), c.stream>>>(D, P, a);
+    recon_kernel<S, 0, 0, MIXED>()<<<nb, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(D, P, a);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
