@@ -114,8 +114,9 @@ def algorithmic_bytes_per_cell_stage(mesh, scheme, mixed: bool = False) -> int:
     points and the equilibrium it stores; with gravity the source it writes.
     Mixed form: the pseudo-inverse, moments and scaled quadrature offsets are
     FP32 per cell, the face-point values are written in FP32 beside the FP64
-    cell-average deviation, and the gamma = 2 equilibrium needs <phi> and
-    var(phi) per cell instead of the quadrature-point arrays."""
+    cell-average deviation (and its FP32 copy), and the gamma = 2 equilibrium
+    needs <phi> and var(phi) per cell instead of the quadrature-point arrays
+    and is also written as FP32 pairs for the face kernel."""
     nd = mesh.info["n_dims"]
     nv = nd + 2
     nf = nd + 1
@@ -144,9 +145,9 @@ def algorithmic_bytes_per_cell_stage(mesh, scheme, mixed: bool = False) -> int:
         b += NP * 4                     # pseudo-inverse (FP32)
         b += NC * 4                     # moments (FP32)
         b += nf * nqf * nd * 4          # scaled face-point offsets (FP32, per cell)
-        b += nf * nqf * nv * 4 + nv * 8  # face-point values (FP32) + deviation (FP64) written
+        b += nf * nqf * nv * 4 + nv * 8 + nv * 4  # face-point values (FP32), deviation (FP64 and FP32) written
         if scheme.equilibrium:
-            b += 3 * 8 + 4 * 8          # phi at the reference point, <phi>, var(phi); equilibrium out
+            b += 3 * 8 + 4 * 8 + 3 * 8  # phi at the reference point, <phi>, var(phi); equilibrium out (FP64, FP32 pairs)
         if scheme.gravity:
             b += nqc * nd * 4 * 2 + nd * 8 + 8 + nv * 4   # offsets, w grad phi, sum, 1/vol, source out
     return int(b)
