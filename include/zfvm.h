@@ -119,7 +119,10 @@ enum zfvm_flux { ZFVM_FLUX_HLLC = 0, ZFVM_FLUX_RUSANOV = 1 };
 enum zfvm_equilibrium { ZFVM_EQ_NONE = 0, ZFVM_EQ_ISENTROPIC = 1 };
 enum zfvm_gravity { ZFVM_GRAVITY_NONE = 0, ZFVM_GRAVITY_CONSTANT_RADIAL = 1, ZFVM_GRAVITY_HARMONIC_RADIAL = 2 };
 enum zfvm_flux_bc { ZFVM_FLUX_BC_NONE = 0, ZFVM_FLUX_BC_CONSTANT = 1, ZFVM_FLUX_BC_ISENTROPIC = 2 };
-enum zfvm_boundary { ZFVM_BC_NONE = 0, ZFVM_BC_PERIODIC = 1 };
+/* Ghost cells (the mesh's ghost mask) are periodic images of their interior
+ * source cells, or, when a ghost cell is its own source, frozen at the values
+ * it was set to (FrozenBC, boundary/frozen_boundary_condition.cpp:39-55). */
+enum zfvm_boundary { ZFVM_BC_NONE = 0, ZFVM_BC_PERIODIC = 1, ZFVM_BC_FROZEN = 2 };
 enum zfvm_precision { ZFVM_FP64 = 0, ZFVM_MIXED = 1 };
 
 typedef struct {

@@ -1214,11 +1214,19 @@ static int rate_of_change(Problem &pr, std::vector<Cv> &tend, const std::vector<
   return flux_bc(pr, tend, state);
 }
 
-static void apply_bc(Problem &pr, std::vector<Cv> &u) {
-  if (pr.s.boundary != 1) return;
+// Ghost cells after a stage: periodic images copy their source (boundary 1);
+// FrozenBC::apply (boundary/frozen_boundary_condition.cpp:39-55) writes back the
+// values the ghost cells had when the step started, which are the values they
+// were set to (boundary 2).
+static void apply_bc(Problem &pr, std::vector<Cv> &u, const std::vector<Cv> &u_step) {
   const auto &g = pr.g;
-  for (idx i = 0; i < g.n_cells; ++i)
-    if (g.ghost[i]) u[i] = u[g.source[i]];
+  if (pr.s.boundary == 1) {
+    for (idx i = 0; i < g.n_cells; ++i)
+      if (g.ghost[i]) u[i] = u[g.source[i]];
+  } else if (pr.s.boundary == 2) {
+    for (idx i = 0; i < g.n_cells; ++i)
+      if (g.ghost[i]) u[i] = u_step[i];
+  }
 }
 
 // LocalCFL (model/local_cfl_condition_impl.hpp:24-40) with reduce::min
@@ -1266,12 +1274,12 @@ static int rk_step(Problem &pr, std::vector<Cv> &u0, double dt) {
   if (st) return st;
   for (int s = 1; s < S; ++s) {
     rk_sum(a[s]);
-    apply_bc(pr, ux);
+    apply_bc(pr, ux, u0);
     st = rate_of_change(pr, k[s], ux);
     if (st) return st;
   }
   rk_sum(b);
-  apply_bc(pr, ux);
+  apply_bc(pr, ux, u0);
   u0.swap(ux);
   return 0;
 }
@@ -1297,7 +1305,7 @@ const char *zfvm_oracle_last_error(void) { return g_oracle_err.c_str(); }
 //  [3..7] linear weights          [8] epsilon      [9] exponent
 //  [10] rk stages                 [11] cfl         [12] equilibrium (0/1)
 //  [13] gravity kind              [14] gravity strength
-//  [15] flux bc (0/1/2)           [16] boundary (0 none, 1 periodic copy)
+//  [15] flux bc (0/1/2)           [16] boundary (0 none, 1 periodic copy, 2 frozen)
 //  [17] steps_per_recompute       [18] recompute_threshold
 int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, int64_t n_cells, const int64_t *vi,
                        const uint8_t *ghost, const int64_t *source, int qe, int qv, int qm,
@@ -1440,7 +1448,7 @@ static void store(const std::vector<Cv> &u, double *aos) {
 
 int zfvm_oracle_rate_of_change(zfvm_oracle *o, const double *state, double *tendency) {
   auto u = load(state, o->pr.g.n_cells);
-  apply_bc(o->pr, u);
+  apply_bc(o->pr, u, u);
   std::vector<Cv> t(u.size());
   int st = rate_of_change(o->pr, t, u);
   if (st) {
@@ -1455,14 +1463,14 @@ int zfvm_oracle_rate_of_change(zfvm_oracle *o, const double *state, double *tend
 
 int zfvm_oracle_cfl_dt(zfvm_oracle *o, const double *state, double *dt) {
   auto u = load(state, o->pr.g.n_cells);
-  apply_bc(o->pr, u);
+  apply_bc(o->pr, u, u);
   *dt = cfl_dt(o->pr, u);
   return 0;
 }
 
 int zfvm_oracle_step(zfvm_oracle *o, double *state, double dt) {
   auto u = load(state, o->pr.g.n_cells);
-  apply_bc(o->pr, u);
+  apply_bc(o->pr, u, u);
   int st = rk_step(o->pr, u, dt);
   if (st) {
     g_oracle_err = st == 4 ? "equilibrium solve is not converging" : "non-physical state";
@@ -1477,7 +1485,7 @@ int zfvm_oracle_step(zfvm_oracle *o, double *state, double dt) {
 int zfvm_oracle_run(zfvm_oracle *o, double *state, int64_t n_steps, double t_end, double *t_io, int64_t *steps_out) {
   Problem &pr = o->pr;
   auto u = load(state, pr.g.n_cells);
-  apply_bc(pr, u);
+  apply_bc(pr, u, u);
   double t = *t_io;
   int64_t step = 0;
   double dt = cfl_dt(pr, u);

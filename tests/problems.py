@@ -49,6 +49,26 @@ def vortex_tube_3d(n: int = 70, order: int = 3, seed: int = 1):
     return raw, mesh, scheme, u0
 
 
+def polytrope_2d_frozen(n_rings: int = 60, amplitude: float = 1e-4, seed: int = 11, precision: int = z.FP64,
+                        r_frozen: float = 0.5):
+    """The well-balanced polytrope with the reference's experiment boundary:
+    cells with centres beyond r = 0.5 are frozen ghost cells
+    (Polytrope::boundary_mask, experiments/polytrope.cpp:55-63, with FrozenBC)."""
+    import numpy as np
+    raw = z.RawMesh.generate("disk", n=n_rings, radius=1.0, jitter=0.2, seed=seed)
+    c = raw.vertices[raw.vertex_indices].mean(axis=1)
+    raw.ghost = (np.hypot(c[:, 0], c[:, 1]) > r_frozen).astype(np.uint8)
+    raw.source = np.arange(raw.n_cells, dtype=np.int64)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2), quad=(3, 3, 2))
+    scheme = z.Scheme(flux=z.FLUX_HLLC, gamma=2.0, linear_weights=[100.0, 1.0, 1.0, 1.0], epsilon=1e-6,
+                      exponent=4.0, rk_stages=3, cfl_number=0.45, equilibrium=z.EQ_ISENTROPIC,
+                      gravity=z.GRAVITY_HARMONIC_RADIAL, gravity_strength=1.0, flux_bc=z.FLUX_BC_ISENTROPIC,
+                      boundary=z.BC_FROZEN, precision=precision)
+    u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amplitude,
+                                 width=0.05, x0=0.3, y0=0.0)
+    return raw, mesh, scheme, u0
+
+
 def polytrope_3d(n: int = 40, amplitude: float = 1e-4, seed: int = 3, precision: int = z.FP64, order: int = 3):
     """gamma = 2 isentropic polytrope on the unit cube of n^3 x 6 jittered
     tetrahedra, phi = r^2 / 2 about the origin (the cube is one octant of the

@@ -9,7 +9,7 @@ import pytest
 
 import zisafvm_gb300 as z
 from metrics import perturbation_rel_l1, rel_errors, state_rel_l1
-from problems import polytrope_2d, polytrope_3d, vortex_2d, vortex_tube_3d
+from problems import polytrope_2d, polytrope_2d_frozen, polytrope_3d, vortex_2d, vortex_tube_3d
 
 pytestmark = pytest.mark.gpu
 
@@ -106,5 +106,24 @@ def test_mixed_polytrope_3d(zlib):
     s32.advance(n_steps=20)
     u64, _ = s64.get_state()
     u32, _ = s32.get_state()
+    assert state_rel_l1(u32, u64) < TOL_MIXED
+    assert perturbation_rel_l1(u32, u64, u0) < 1e-4
+
+
+def test_mixed_frozen_ghost_cells(zlib):
+    """Frozen ghost cells in the mixed form: balanced at rest, ghosts unchanged,
+    the perturbation against the FP64 form."""
+    raw, mesh, scheme, u0 = polytrope_2d_frozen(n_rings=40, amplitude=0.0, precision=z.MIXED)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    assert np.abs(s.rate_of_change()).max() < TOL_WB
+    raw, mesh, scheme, u0 = polytrope_2d_frozen(n_rings=40, amplitude=1e-3)
+    s64, s32 = _pair(mesh, scheme, u0)
+    s64.advance(n_steps=20)
+    s32.advance(n_steps=20)
+    u64, _ = s64.get_state()
+    u32, _ = s32.get_state()
+    ghost = raw.ghost == 1
+    assert np.array_equal(u32[ghost], u0[ghost])
     assert state_rel_l1(u32, u64) < TOL_MIXED
     assert perturbation_rel_l1(u32, u64, u0) < 1e-4

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from metrics import rel_errors
-from problems import polytrope_2d, polytrope_3d, vortex_2d, vortex_tube_3d
+from problems import polytrope_2d, polytrope_2d_frozen, polytrope_3d, vortex_2d, vortex_tube_3d
 
 pytestmark = pytest.mark.gpu
 
@@ -168,6 +168,31 @@ def test_polytrope_3d_rhs_steps_and_balance(zlib, olib):
     u_eq = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=0.0)
     s.set_state(u_eq)
     assert np.abs(s.rate_of_change()).max() < 1e-10
+
+
+def test_frozen_ghost_cells(zlib, olib):
+    """FrozenBC: ghost cells beyond r = 0.5 keep their values; the interior
+    matches the oracle (right-hand side, CFL step counting the frozen cells,
+    steps)."""
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d_frozen(n_rings=24, amplitude=1e-2)
+    ghost = raw.ghost == 1
+    assert ghost.any() and (~ghost).any()
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    o = _oracle(olib, raw, mesh, scheme)
+    t_gpu, t_ref = s.rate_of_change(), o.rate_of_change(u0)
+    assert np.abs(t_gpu[~ghost] - t_ref[~ghost]).max() <= 1e-12 * np.abs(t_ref[~ghost]).max()
+    assert not t_gpu[ghost].any()
+    dt_ref = o.cfl_dt(u0)
+    assert abs(s.cfl_dt() - dt_ref) <= 1e-15 * dt_ref
+    s.advance(n_steps=5)
+    u_gpu, t1 = s.get_state()
+    u_ref, t_ref1, _ = o.run(u0, n_steps=5)
+    assert np.array_equal(u_gpu[ghost], u0[ghost])
+    d_gpu, d_ref = u_gpu - u0, u_ref - u0
+    assert np.abs(d_gpu - d_ref).max() <= 1e-9 * np.abs(d_ref).max()
+    assert abs(t1 - t_ref1) < 1e-12 * t_ref1
 
 
 def test_error_status_nonphysical(zlib):

@@ -32,7 +32,7 @@ FLUX_HLLC, FLUX_RUSANOV = 0, 1
 EQ_NONE, EQ_ISENTROPIC = 0, 1
 GRAVITY_NONE, GRAVITY_CONSTANT_RADIAL, GRAVITY_HARMONIC_RADIAL = 0, 1, 2
 FLUX_BC_NONE, FLUX_BC_CONSTANT, FLUX_BC_ISENTROPIC = 0, 1, 2
-BC_NONE, BC_PERIODIC = 0, 1
+BC_NONE, BC_PERIODIC, BC_FROZEN = 0, 1, 2
 FP64, MIXED = 0, 1
 
 STATUS = {0: "ok", 1: "EINVAL", 2: "ENOMEM", 3: "ENONPHYSICAL", 4: "ENEWTON", 5: "ETIMEDOUT", 6: "ECUDA",

@@ -135,7 +135,11 @@ extern "C" int zfvm_mesh_create(const zfvm_mesh_desc *d, zfvm_mesh **out) {
     for (int64_t i = 0; i < d->n_cells; ++i) {
       int64_t s = d->source[i];
       if (s < 0 || s >= d->n_cells) return fail(ZFVM_EINVAL, "periodic source out of range");
-      if (!(m->grid.flags[s] & kInterior)) return fail(ZFVM_EINVAL, "periodic source is a ghost cell");
+      // a ghost cell is either a periodic image of an interior cell or, as its
+      // own source, frozen (FrozenBC, boundary/frozen_boundary_condition.cpp:39-55)
+      if (!(m->grid.flags[s] & kInterior) && s != i)
+        return fail(ZFVM_EINVAL, "periodic source is a ghost cell");
+      if ((m->grid.flags[i] & kInterior) && s != i) return fail(ZFVM_EINVAL, "interior cell with a periodic source");
       m->grid.source[i] = s;
     }
   }

@@ -13,7 +13,8 @@
 
 namespace zfvm {
 
-enum CellFlag : uint8_t { kInterior = 1, kGhost = 2, kGhostL1 = 4 };
+// kFrozen: a ghost cell that is its own source keeps its values (FrozenBC)
+enum CellFlag : uint8_t { kInterior = 1, kGhost = 2, kGhostL1 = 4, kFrozen = 8 };
 
 struct QuadDegrees {
   int edge = 3;

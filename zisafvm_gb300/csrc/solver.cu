@@ -299,7 +299,7 @@ int build_solver(zfvm_solver *s) {
   std::vector<double> h_pinv((size_t)NP * ld, 0.0), h_center((size_t)nd * ld, 0.0), h_il(ld, 0.0),
       h_mom((size_t)NC * ld, 0.0), h_iv(ld, 0.0), h_reff(ld, 1e300);
   for (index_t i = 0; i < n; ++i) {
-    h_flags[i] = g.flags[i];
+    h_flags[i] = g.flags[i] | (((g.flags[i] & kGhost) && g.source[i] == i) ? kFrozen : 0);
     h_src[i] = (int)g.source[i];
     h_iv[i] = 1.0 / g.volumes[i];
     h_il[i] = 1.0 / g.char_length[i];
@@ -682,9 +682,14 @@ extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
   CK(cudaMemcpyAsync(s->aos.p, cvars, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
   k_aos_to_soa<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->aos.p, s->u0.p, (int)n, s->ld, s->nv);
   CK(cudaGetLastError());
+  // the stage state starts as a copy: the update writes interior cells only, so
+  // frozen ghost cells carry their values into every stage from here
+  CK(cudaMemcpyAsync(s->ux.p, s->u0.p, s->u0.n * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
   if (s->qsplit.p) {
+    const size_t half = (size_t)s->nv * s->ld;
     k_split<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->qsplit.p, (int)n, s->ld, s->nv);
     CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(s->qsplit.p + half, s->qsplit.p, half * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
   }
   Clock c{};
   c.t = t;

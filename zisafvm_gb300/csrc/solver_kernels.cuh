@@ -1282,6 +1282,12 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
         if (!finite) set_status(d.clock, kStNonFinite);
       }
     }
+  } else if (last && !a.tend_out && !d.clock->done && i < d.n_cells && (d.flags[i] & kFrozen)) {
+    // a frozen ghost cell keeps its state; LocalCFL still counts it
+    double w[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) w[v] = a.u0[v * d.ld + i];
+    cand = MIXED ? cfl_candidate_1rcp<NV>(w, P.gamma, d.r_eff[i]) : cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
   }
   return cand;
 }
@@ -1297,7 +1303,7 @@ __global__ void __launch_bounds__(128) k_cfl(const DevData d, const Params P, co
   constexpr int NV = S::NV;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double cand = INFINITY;
-  if (i < d.n_cells && (d.flags[i] & kInterior)) {
+  if (i < d.n_cells && (d.flags[i] & (kInterior | kFrozen))) {
     double w[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) w[v] = u[v * d.ld + i];
