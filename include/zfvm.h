@@ -178,6 +178,17 @@ int zfvm_rate_of_change(zfvm_solver *s, double *tendency);
  *  - The solver's device must be current, as for the other entry points. */
 int zfvm_rate_of_change_noalloc(zfvm_solver *s, double *tendency);
 
+/* EulerGlobalReconstruction::compute (reconstruction/global_reconstruction_impl.hpp:100-163):
+ * reconstruct the current state in every interior and first-layer ghost cell;
+ * the limited polynomials stay with the solver until the next call. */
+int zfvm_reconstruct(zfvm_solver *s);
+
+/* GlobalReconstruction::operator()(i, x) (global_reconstruction_decl.hpp:29) for n
+ * points: the reconstruction of cell cells[k] at x[3k .. 3k+2], equilibrium
+ * included, as (rho, m1, m2, m3, E) rows of u (n x 5).  Host arithmetic on the
+ * records of the last zfvm_reconstruct. */
+int zfvm_reconstruction_eval(const zfvm_solver *s, int64_t n, const int64_t *cells, const double *x, double *u);
+
 /* CFL time step of the current state (LocalCFL, local_cfl_condition_impl.hpp:24-40). */
 int zfvm_cfl_dt(zfvm_solver *s, double *dt);
 

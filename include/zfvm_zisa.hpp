@@ -3,9 +3,11 @@
 //
 // Inside a ZisaFVM build (its headers on the include path) the adaptors derive
 // from the reference's abstract classes:
-//   GpuRateOfChange      : zisa::RateOfChange      (ode/rate_of_change.hpp:23-43)
-//   GpuRungeKutta        : zisa::TimeIntegration   (ode/time_integration.hpp:13-48)
-//   GpuLocalCFL          : zisa::CFLCondition      (model/cfl_condition.hpp:12-18)
+//   GpuRateOfChange         : zisa::RateOfChange      (ode/rate_of_change.hpp:23-43)
+//   GpuRungeKutta           : zisa::TimeIntegration   (ode/time_integration.hpp:13-48)
+//   GpuLocalCFL             : zisa::CFLCondition      (model/cfl_condition.hpp:12-18)
+//   GpuGlobalReconstruction : zisa::GlobalReconstruction<euler_var_t>
+//                             (reconstruction/global_reconstruction_decl.hpp:20-32)
 // Outside it (ZFVM_STANDALONE) they implement the same member signatures on a
 // minimal AllVariables stand-in so the boundary compiles and tests on its own.
 //
@@ -15,6 +17,7 @@
 // thrown as std::runtime_error, the equivalent of the reference's LOG_ERR.
 #pragma once
 
+#include <array>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -27,6 +30,7 @@
 #include <zisa/model/cfl_condition.hpp>
 #include <zisa/ode/rate_of_change.hpp>
 #include <zisa/ode/time_integration.hpp>
+#include <zisa/reconstruction/global_reconstruction_decl.hpp>
 #define ZFVM_HAVE_ZISA 1
 #else
 #define ZFVM_HAVE_ZISA 0
@@ -45,6 +49,22 @@ using TimeIntegrationBase = zisa::TimeIntegration;
 using CFLConditionBase = zisa::CFLCondition;
 inline double *cvars_data(AllVariables &u) { return u.cvars.raw(); }
 inline const double *cvars_data(const AllVariables &u) { return u.cvars.raw(); }
+using XYZ = zisa::XYZ;
+using euler_var_t = zisa::euler_var_t;
+using GlobalReconstructionBase = zisa::GlobalReconstruction<zisa::euler_var_t>;
+using CellsView = zisa::array_const_view<zisa::int_t, 1>;
+inline CellsView cells_view(const int64_t *p, int64_t n) {
+  return CellsView(zisa::shape_t<1>{zisa::int_t(n)}, reinterpret_cast<const zisa::int_t *>(p),
+                   zisa::device_type::cpu);
+}
+inline double coord(const XYZ &x, int k) { return x[k]; }
+inline euler_var_t to_cvars(const double *u) {
+  euler_var_t r;
+  for (int k = 0; k < 5; ++k) r[k] = u[k];
+  return r;
+}
+inline int64_t view_size(const CellsView &v) { return int64_t(v.shape(0)); }
+inline const int64_t *view_data(const CellsView &v) { return reinterpret_cast<const int64_t *>(v.raw()); }
 #else
 // Stand-in with the reference's layout: cvars is n_cells x 5, row-major.
 struct AllVariables {
@@ -68,18 +88,40 @@ struct CFLConditionBase {
   virtual ~CFLConditionBase() = default;
   virtual double operator()(const AllVariables &all_variables) = 0;
 };
+using XYZ = std::array<double, 3>;
+using euler_var_t = std::array<double, 5>;  // rho, m1, m2, m3, E
+struct CellsView {
+  const int64_t *ptr = nullptr;
+  int64_t n = 0;
+};
+inline CellsView cells_view(const int64_t *p, int64_t n) { return CellsView{p, n}; }
+inline double coord(const XYZ &x, int k) { return x[k]; }
+inline euler_var_t to_cvars(const double *u) { return {u[0], u[1], u[2], u[3], u[4]}; }
+inline int64_t view_size(const CellsView &v) { return v.n; }
+inline const int64_t *view_data(const CellsView &v) { return v.ptr; }
+struct GlobalReconstructionBase {
+  virtual ~GlobalReconstructionBase() = default;
+  virtual void compute(const AllVariables &current_state) = 0;
+  virtual void compute(const AllVariables &current_state, const CellsView &cells) = 0;
+  virtual euler_var_t operator()(int64_t i, const XYZ &x) const = 0;
+  virtual CellsView stencil(int64_t i) const = 0;
+};
 #endif
 
 // Shared device solver (one mesh + scheme); the adaptors below hold it.
 class DeviceSolver {
  public:
-  DeviceSolver(zfvm_mesh *mesh, const zfvm_scheme_desc &scheme) { check(zfvm_solver_create(mesh, &scheme, &s_)); }
+  DeviceSolver(zfvm_mesh *mesh, const zfvm_scheme_desc &scheme) : mesh_(mesh) {
+    check(zfvm_solver_create(mesh, &scheme, &s_));
+  }
   ~DeviceSolver() { zfvm_solver_destroy(s_); }
   DeviceSolver(const DeviceSolver &) = delete;
   DeviceSolver &operator=(const DeviceSolver &) = delete;
   zfvm_solver *get() const { return s_; }
+  zfvm_mesh *mesh() const { return mesh_; }
 
  private:
+  zfvm_mesh *mesh_ = nullptr;
   zfvm_solver *s_ = nullptr;
 };
 
@@ -134,6 +176,47 @@ class GpuLocalCFL : public CFLConditionBase {
 
  private:
   std::shared_ptr<DeviceSolver> s_;
+};
+
+// EulerGlobalReconstruction on the device: compute() reconstructs the state in
+// every cell (the reference's `cells` subset is reconstructed along with the
+// rest), operator()(i, x) evaluates the limited polynomial plus the
+// equilibrium at x on the host, stencil(i) is the cell's combined stencil.
+class GpuGlobalReconstruction : public GlobalReconstructionBase {
+ public:
+  explicit GpuGlobalReconstruction(std::shared_ptr<DeviceSolver> s) : s_(std::move(s)) {
+    zfvm_mesh_info info;
+    check(zfvm_mesh_get_info(s_->mesh(), &info));
+    const int64_t n = info.n_cells;
+    std::vector<int8_t> ns(n), kh(n), nl(n), order(n * ZFVM_MAX_STENCILS), size(n * ZFVM_MAX_STENCILS),
+        bias(n * ZFVM_MAX_STENCILS), local(n * ZFVM_MAX_STENCILS * ZFVM_MAX_STENCIL_SIZE);
+    std::vector<int32_t> l2g(n * ZFVM_MAX_L2G);
+    check(zfvm_mesh_get_stencils(s_->mesh(), ns.data(), kh.data(), nl.data(), l2g.data(), order.data(),
+                                 size.data(), bias.data(), local.data()));
+    l2g_.resize(l2g.size());
+    for (size_t k = 0; k < l2g.size(); ++k) l2g_[k] = l2g[k];
+    n_l2g_.assign(nl.begin(), nl.end());
+  }
+  void compute(const AllVariables &current_state) override {
+    check(zfvm_set_state(s_->get(), cvars_data(current_state), 0.0));
+    check(zfvm_reconstruct(s_->get()));
+  }
+  void compute(const AllVariables &current_state, const CellsView &) override { compute(current_state); }
+  euler_var_t operator()(int64_t i, const XYZ &x) const override {
+    const double p[3] = {coord(x, 0), coord(x, 1), coord(x, 2)};
+    double u[5];
+    check(zfvm_reconstruction_eval(s_->get(), 1, &i, p, u));
+    return to_cvars(u);
+  }
+  CellsView stencil(int64_t i) const override {
+    return cells_view(l2g_.data() + i * ZFVM_MAX_L2G, n_l2g_[i]);
+  }
+  std::string str() const { return "GB300 global reconstruction (`GpuGlobalReconstruction`)"; }
+
+ private:
+  std::shared_ptr<DeviceSolver> s_;
+  std::vector<int64_t> l2g_;
+  std::vector<int64_t> n_l2g_;
 };
 
 }  // namespace zfvm

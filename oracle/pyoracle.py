@@ -31,6 +31,7 @@ def lib() -> C.CDLL:
         L.zfvm_oracle_set_lsq_mode.argtypes = [vp, C.c_int]
         L.zfvm_oracle_rate_of_change.argtypes = [vp, dp, dp]
         L.zfvm_oracle_cfl_dt.argtypes = [vp, dp, dp]
+        L.zfvm_oracle_reconstruct_eval.argtypes = [vp, dp, C.c_int64, C.c_void_p, dp, dp]
         L.zfvm_oracle_step.argtypes = [vp, dp, C.c_double]
         L.zfvm_oracle_run.argtypes = [vp, dp, C.c_int64, C.c_double, dp, C.POINTER(C.c_int64)]
         L.zfvm_oracle_flux.argtypes = [C.c_int, C.c_double, dp, dp, dp]
@@ -107,6 +108,15 @@ class Oracle:
         u = np.ascontiguousarray(state, dtype=np.float64)
         out = np.zeros_like(u)
         _check(lib().zfvm_oracle_rate_of_change(self._h, _dp(u), _dp(out)))
+        return out
+
+    def reconstruct_eval(self, state: np.ndarray, cells, x) -> np.ndarray:
+        """Reconstruction of cells[k] at x[k] (n x 3): n x 5 rows."""
+        u = np.ascontiguousarray(state, dtype=np.float64)
+        c = np.ascontiguousarray(cells, dtype=np.int64)
+        xx = np.ascontiguousarray(x, dtype=np.float64).reshape(len(c), 3)
+        out = np.zeros((len(c), 5))
+        _check(lib().zfvm_oracle_reconstruct_eval(self._h, _dp(u), len(c), c.ctypes.data, _dp(xx), _dp(out)))
         return out
 
     def cfl_dt(self, state: np.ndarray) -> float:

@@ -1461,6 +1461,42 @@ int zfvm_oracle_rate_of_change(zfvm_oracle *o, const double *state, double *tend
   return 0;
 }
 
+// EulerGlobalReconstruction::compute for the given cells, then
+// LocalReconstruction::operator()(x) (local_reconstruction.hpp:149-163) at one
+// point per entry: background equilibrium + scale * polynomial.
+int zfvm_oracle_reconstruct_eval(zfvm_oracle *o, const double *state, int64_t n, const int64_t *cells,
+                                 const double *x, double *u) {
+  Problem &pr = o->pr;
+  auto s = load(state, pr.g.n_cells);
+  apply_bc(pr, s, s);
+  std::vector<char> done(pr.g.n_cells, 0);
+  for (int64_t k = 0; k < n; ++k) {
+    const idx i = cells[k];
+    if (i < 0 || i >= pr.g.n_cells) {
+      g_oracle_err = "cell index out of range";
+      return 1;
+    }
+    if (done[i]) continue;
+    std::vector<Cv> ul(pr.rc[i].l2g.size());
+    for (size_t l = 0; l < ul.size(); ++l) ul[l] = s[pr.rc[i].l2g[l]];
+    const int st = local_reconstruct(pr, i, ul);
+    if (st) {
+      g_oracle_err = st == 4 ? "equilibrium solve is not converging" : "non-physical state";
+      return st;
+    }
+    done[i] = 1;
+  }
+  for (int64_t k = 0; k < n; ++k) {
+    const idx i = cells[k];
+    const XYZ xyz{{x[3 * k], x[3 * k + 1], x[3 * k + 2]}};
+    const auto bg = pr.s.equilibrium ? pr.rc[i].eq.extrapolate_full(xyz)
+                                     : std::make_pair(RhoE{0, 0}, std::array<double, 2>{0, 0});
+    const Cv v = rc_value(pr.rc[i], xyz, bg);
+    for (int c = 0; c < 5; ++c) u[5 * k + c] = v[c];
+  }
+  return 0;
+}
+
 int zfvm_oracle_cfl_dt(zfvm_oracle *o, const double *state, double *dt) {
   auto u = load(state, o->pr.g.n_cells);
   apply_bc(o->pr, u, u);

@@ -195,6 +195,40 @@ def test_frozen_ghost_cells(zlib, olib):
     assert abs(t1 - t_ref1) < 1e-12 * t_ref1
 
 
+def _points_inside(raw, cells, seed=0):
+    """One random point inside each cell (Dirichlet barycentric weights)."""
+    rng = np.random.default_rng(seed)
+    lam = rng.dirichlet(np.ones(raw.vertex_indices.shape[1]), size=len(cells))
+    return np.einsum("ck,ckd->cd", lam, raw.vertices[raw.vertex_indices[cells]])
+
+
+@pytest.mark.parametrize("case", ["vortex", "polytrope", "tets"])
+def test_reconstruction_at_points(zlib, olib, case):
+    """GlobalReconstruction::operator()(i, x): the GPU reconstruction of the
+    current state evaluated at points inside cells against the oracle's
+    LocalReconstruction (equilibrium + scale * polynomial)."""
+    z = zlib
+    if case == "vortex":
+        raw, mesh, scheme, u0 = vortex_2d(n=20, halo=3, flux=z.FLUX_HLLC)
+    elif case == "polytrope":
+        raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-2)
+    else:
+        raw, mesh, scheme, u0 = vortex_tube_3d(n=5)
+    inner = np.flatnonzero(raw.ghost == 0) if raw.ghost is not None else np.arange(mesh.n_cells)
+    cells = inner[:: max(1, len(inner) // 300)]
+    x = _points_inside(raw, cells)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    s.reconstruct()
+    got = s.reconstruction_eval(cells, x)
+    ref = _oracle(olib, raw, mesh, scheme).reconstruct_eval(u0, cells, x)
+    scale = np.maximum(np.abs(ref).max(axis=0), 1e-300)
+    assert (np.abs(got - ref).max(axis=0) / scale).max() < 1e-12
+    # a cell index outside the mesh is an error, not a read out of bounds
+    with pytest.raises(z.ZfvmError):
+        s.reconstruction_eval([mesh.n_cells], x[:1])
+
+
 def test_error_status_nonphysical(zlib):
     """A negative density is reported as ENONPHYSICAL, not a crash."""
     z = zlib

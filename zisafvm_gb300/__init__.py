@@ -133,6 +133,8 @@ def load_library() -> C.CDLL:
         "zfvm_batch_slot_status": [vp, i32, dp, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)],
         "zfvm_batch_slots": [vp, C.POINTER(i32)],
         "zfvm_solver_footprint": [vp, vp, C.POINTER(i64)],
+        "zfvm_reconstruct": [vp],
+        "zfvm_reconstruction_eval": [vp, i64, C.POINTER(i64), dp, dp],
         "zfvm_server_create": [vp, pp],
         "zfvm_server_destroy": [vp],
         "zfvm_server_submit": [vp, vp, vp, dp, C.c_double, i64, C.c_double, C.POINTER(i64)],
@@ -380,6 +382,18 @@ class Solver:
         a = np.zeros((self.mesh.n_cells, 5))
         _check(load_library().zfvm_rate_of_change(self._h, _dp(a)))
         return a
+
+    def reconstruct(self) -> None:
+        """Reconstruct the current state (GlobalReconstruction::compute)."""
+        _check(load_library().zfvm_reconstruct(self._h))
+
+    def reconstruction_eval(self, cells, x) -> np.ndarray:
+        """Reconstruction of cells[k] at the points x[k] (n x 3), as n x 5 rows."""
+        c = np.ascontiguousarray(cells, dtype=np.int64)
+        xx = np.ascontiguousarray(x, dtype=np.float64).reshape(len(c), 3)
+        out = np.zeros((len(c), 5))
+        _check(load_library().zfvm_reconstruction_eval(self._h, len(c), _i64p(c), _dp(xx), _dp(out)))
+        return out
 
     def cfl_dt(self) -> float:
         dt = C.c_double()

@@ -927,3 +927,95 @@ extern "C" int zfvm_solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc 
   *bytes = b;
   return ZFVM_OK;
 }
+
+namespace {
+
+// GlobalReconstruction::operator()(i, x) on the host from the exported records
+template <class S>
+int eval_records(const zfvm_solver *s, int64_t n, const int64_t *cells, const double *x, double *u) {
+  using PR = PolyRecord<S>;
+  constexpr int NV = S::NV, ND = S::ND, NC = S::NC;
+  const int ld = s->ld;
+  const double *rec = s->poly_host.data();
+  const auto &sc = s->scheme;
+  EqEval ev{sc.gamma, sc.gamma - 1.0, 1.0 / (sc.gamma - 1.0)};
+  for (int64_t k = 0; k < n; ++k) {
+    const int64_t i = cells[k];
+    if (i < 0 || i >= s->n_cells) return fail(ZFVM_EINVAL, "cell index out of range");
+    auto at = [&](int row) { return rec[(size_t)row * ld + i]; };
+    if (at(PR::VALID) != 1.0) return fail(ZFVM_EINVAL, "cell " + std::to_string(i) + " has no reconstruction");
+    double X[ND], C[NC], phi_c[NC];
+    for (int d = 0; d < ND; ++d) X[d] = (x[3 * k + d] - at(PR::XC + d)) * at(PR::IL);
+    for (int c = 0; c < NC; ++c) C[c] = at(PR::MOM + c);
+    basis<ND, NC>(X, C, phi_c);
+    double w[NV];
+    for (int v = 0; v < NV; ++v) {
+      double acc = at(PR::DEV + v);
+      for (int c = 0; c < NC; ++c) acc += at(PR::COEF + c * NV + v) * phi_c[c];
+      w[v] = acc;
+    }
+    if (at(PR::EQ + 3) != 0.0) {
+      const double r = std::sqrt(x[3 * k] * x[3 * k] + x[3 * k + 1] * x[3 * k + 1] + x[3 * k + 2] * x[3 * k + 2]);
+      const double phi = sc.gravity == ZFVM_GRAVITY_CONSTANT_RADIAL ? sc.gravity_strength * r
+                                                                    : 0.5 * sc.gravity_strength * r * r;
+      EqEval::Bound b{at(PR::EQ), at(PR::EQ + 1), at(PR::EQ + 2)};
+      double rho, E;
+      b.at(ev, phi, rho, E);
+      w[0] += rho;
+      w[NV - 1] += E;
+    }
+    double *o = u + 5 * k;
+    for (int v = 0; v < 5; ++v) o[v] = 0.0;
+    for (int v = 0; v < NV - 1; ++v) o[v] = w[v];
+    o[4] = w[NV - 1];
+  }
+  return ZFVM_OK;
+}
+
+int poly_record_size(int shape_id) {
+  switch (shape_id) {
+    case 0: return PolyRecord<S2o3>::SIZE;
+    case 1: return PolyRecord<S2o2>::SIZE;
+    case 2: return PolyRecord<S3o3>::SIZE;
+    default: return PolyRecord<S3o2>::SIZE;
+  }
+}
+
+}  // namespace
+
+// EulerGlobalReconstruction::compute (reconstruction/global_reconstruction_impl.hpp:100-163)
+extern "C" int zfvm_reconstruct(zfvm_solver *s) {
+  if (!s) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
+  const size_t size = (size_t)poly_record_size(s->shape_id) * s->ld;
+  if (s->poly.n != size) s->poly.alloc(size);
+  CK(cudaMemsetAsync(s->poly.p, 0, size * sizeof(double), s->stream));
+  Clock c = read_clock(s);
+  c.done = 0;
+  c.status = 0;
+  write_clock(s, c);
+  StageArgs a = stage_args(s, 0, s->tend.p);
+  a.poly_out = s->poly.p;
+  dispatch_stage(s, a);
+  s->poly_host.resize(size);
+  CK(cudaMemcpyAsync(s->poly_host.data(), s->poly.p, size * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  Clock c2 = read_clock(s);
+  std::string msg;
+  int code = status_to_code(c2.status, msg);
+  if (code) return fail(code, msg);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+// GlobalReconstruction::operator()(i, x) (global_reconstruction_decl.hpp:29)
+extern "C" int zfvm_reconstruction_eval(const zfvm_solver *s, int64_t n, const int64_t *cells, const double *x,
+                                        double *u) {
+  if (!s || (n > 0 && (!cells || !x || !u))) return fail(ZFVM_EINVAL, "null argument");
+  if (s->poly_host.empty()) return fail(ZFVM_EINVAL, "call zfvm_reconstruct first");
+  switch (s->shape_id) {
+    case 0: return eval_records<S2o3>(s, n, cells, x, u);
+    case 1: return eval_records<S2o2>(s, n, cells, x, u);
+    case 2: return eval_records<S3o3>(s, n, cells, x, u);
+    default: return eval_records<S3o2>(s, n, cells, x, u);
+  }
+}

@@ -132,6 +132,8 @@ struct StageArgs {
   // (h_r, f, K) as FP32 (hi, lo) pairs [3][ld]
   float *dev032;
   float2 *eq32;
+  // when non-null: every reconstructed cell's polynomial record [PolyRecord][ld]
+  double *poly_out;
   double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
   float coef32[4];   // the same row rounded to FP32 (mixed form)
   int stage;
@@ -147,7 +149,7 @@ struct Shape {
   static constexpr int NQF = NQF_, NQC = NQC_;
 };
 
-__device__ __forceinline__ double powd(double x, double y) {
+__host__ __device__ __forceinline__ double powd(double x, double y) {
   if (y == 1.0) return x;
   if (y == 2.0) return x * x;
   return pow(x, y);
@@ -156,7 +158,7 @@ __device__ __forceinline__ double powd(double x, double y) {
 // Non-constant monomials of the scaled offset X in poly_index order
 // (math/poly2d_impl.hpp:176-183), minus the normalized moments.
 template <int ND, int NC, class R>
-__device__ __forceinline__ void basis(const R *X, const R *C, R *phi) {
+__host__ __device__ __forceinline__ void basis(const R *X, const R *C, R *phi) {
   if (ND == 2) {
     const R x = X[0], y = X[1];
     R m[5] = {x, y, x * x, x * y, y * y};
@@ -181,14 +183,14 @@ struct EqEval {
   double gamma, gm1, inv_gm1;
   struct Bound {
     double hr, f, K;
-    __device__ __forceinline__ void at(const EqEval &ev, double phi, double &rho, double &E) const {
+    __host__ __device__ __forceinline__ void at(const EqEval &ev, double phi, double &rho, double &E) const {
       double h = hr - phi;
       rho = powd(f * h, ev.inv_gm1);
       double p = K * powd(rho, ev.gamma);
       E = ev.gm1 == 1.0 ? p : p / ev.gm1;
     }
   };
-  __device__ __forceinline__ Bound bind(double h_ref, double K, double phi_ref) const {
+  __host__ __device__ __forceinline__ Bound bind(double h_ref, double K, double phi_ref) const {
     return Bound{h_ref + phi_ref, 1.0 / K * gm1 / gamma, K};
   }
 };
@@ -285,6 +287,16 @@ __device__ int solve_equilibrium(const EqEval &ev, const Params &P, const DevDat
 }
 
 __device__ __forceinline__ void set_status(Clock *c, int bits) { atomicOr(&c->status, bits); }
+
+// Exported reconstruction of one cell (GlobalReconstruction::operator()(i, x)):
+// u(x) = dev0 + sum_c coef[c] (monomial_c((x - xc) / len) - C_c)  (+ the bound
+// equilibrium at x for rho and E).  Layout, one [ld] row each:
+//   dev0[NV] | coef[NC][NV] | xc[ND] | 1/len | C[NC] | h_r, f, K, found | valid
+template <class S>
+struct PolyRecord {
+  static constexpr int DEV = 0, COEF = S::NV, XC = COEF + S::NC * S::NV, IL = XC + S::ND, MOM = IL + 1,
+                       EQ = MOM + S::NC, VALID = EQ + 4, SIZE = VALID + 1;
+};
 
 // ------------------------------------------------- FP32 pair ("double-float")
 // Unevaluated sums hi + lo of two FP32 numbers, with the error-free
@@ -645,6 +657,26 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   }
 #pragma unroll
   for (int c = 0; c < NC; ++c) C[c] = MIXED ? R(d.mom32[c * ld + i]) : R(d.mom[c * ld + i]);
+  if (a.poly_out) {
+    using PR = PolyRecord<S>;
+    double *o = a.poly_out;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) o[(PR::DEV + v) * ld + i] = dev0[v];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) o[(PR::COEF + c * NV + v) * ld + i] = double(pf[c][v]);
+#pragma unroll
+    for (int k = 0; k < ND; ++k) o[(PR::XC + k) * ld + i] = d.center[k * ld + i];
+    o[PR::IL * ld + i] = d.inv_len[i];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) o[(PR::MOM + c) * ld + i] = d.mom[c * ld + i];
+    o[PR::EQ * ld + i] = eqb.hr;
+    o[(PR::EQ + 1) * ld + i] = eqb.f;
+    o[(PR::EQ + 2) * ld + i] = eqb.K;
+    o[(PR::EQ + 3) * ld + i] = (EQ && found) ? 1.0 : 0.0;
+    o[PR::VALID * ld + i] = 1.0;
+  }
   // non-constant part of the limited polynomial at the scaled offset X
   auto poly_X = [&](const R *X, R *pv) {
     R phi[NC];

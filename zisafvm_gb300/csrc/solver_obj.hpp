@@ -82,6 +82,8 @@ struct zfvm_solver {
   zfvm::DBuf<float2> qsplit, m1s, vars;  // mixed: FP32 (hi, lo) pairs of u0, ux; <phi>, var(phi)
   zfvm::DBuf<float2> eq32, phi_fq2;       // mixed + equilibrium: (h_r, f, K) pairs; phi at face points
   zfvm::DBuf<float> dev032;               // mixed: FP32 copy of the cell deviation
+  zfvm::DBuf<double> poly;                // exported reconstruction records (zfvm_reconstruct)
+  std::vector<double> poly_host;
   zfvm::DBuf<zfvm::dev::Clock> clock;
   bool has_src = false, has_eq = false, mixed = false;
   cudaGraphExec_t graph = nullptr;
