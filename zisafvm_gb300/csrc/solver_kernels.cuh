@@ -530,9 +530,13 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     // rows[((l - 1) * NV + v) * blockDim.x + thread], and all fits read it there.
     extern __shared__ float rows_smem[];
     const int bd = blockDim.x, tid = threadIdx.x;
+    // all stencil indices first, as independent loads, parked in the first
+    // slot of their own row until the row is computed
+#pragma unroll
+    for (int l = 1; l < S::MAXL; ++l) rows_smem[((l - 1) * NV) * bd + tid] = __int_as_float(d.l2g[l * ld + i]);
 #pragma unroll 2
     for (int l = 1; l < S::MAXL; ++l) {
-      const int j = d.l2g[l * ld + i];
+      const int j = __float_as_int(rows_smem[((l - 1) * NV) * bd + tid]);
       R dq[NV];
       if (j != j0) {
         row_diff(j, dq);
