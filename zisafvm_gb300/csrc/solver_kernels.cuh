@@ -571,6 +571,40 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
           for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
         }
       }
+  } else if constexpr (MIXED && S::ND == 2) {
+    // all stencil indices first, as independent loads, so the gathers of a
+    // row do not wait on the load of its index (in 3D the extra registers
+    // cost a block per SM, which costs more than the wait)
+    int jc[S::R0], jb[S::NB * S::RB];
+#pragma unroll
+    for (int r = 0; r < S::R0; ++r) jc[r] = d.l2g[(r + 1) * ld + i];
+#pragma unroll
+    for (int kr = 0; kr < S::NB * S::RB; ++kr) jb[kr] = d.l2g[d.bloc[kr * ld + i] * ld + i];
+#pragma unroll 2
+    for (int r = 0; r < S::R0; ++r) {
+      R dq[NV];
+      row_diff(jc[r], dq);
+#pragma unroll
+      for (int c = 0; c < S::C0; ++c) {
+        const R pc = R(d.pinv32[(c * S::R0 + r) * ld + i]);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) b0[c][v] += pc * dq[v];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < S::NB; ++k) {
+#pragma unroll
+      for (int r = 0; r < S::RB; ++r) {
+        R dq[NV];
+        row_diff(jb[k * S::RB + r], dq);
+#pragma unroll
+        for (int c = 0; c < S::CB; ++c) {
+          const R pc = R(d.pinv32[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i]);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
+        }
+      }
+    }
   } else {
 #pragma unroll 2
     for (int r = 0; r < S::R0; ++r) {
