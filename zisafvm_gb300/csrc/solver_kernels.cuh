@@ -355,7 +355,7 @@ constexpr size_t recon_smem_bytes(int threads) {
   return kRowsInShared<S, EQ, MIXED> ? (size_t)(S::MAXL - 1) * S::NV * threads * sizeof(float) : 0;
 }
 
-template <class S, int EQ, int SRC, bool MIXED>
+template <class S, int EQ, int SRC, bool MIXED, bool EXPORT = false>
 __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, const StageArgs &a, const int i) {
   using R = std::conditional_t<MIXED, float, double>;
   constexpr int NV = S::NV, ND = S::ND, NF = S::NF, NC = S::NC;
@@ -695,7 +695,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   }
 #pragma unroll
   for (int c = 0; c < NC; ++c) C[c] = MIXED ? R(d.mom32[c * ld + i]) : R(d.mom[c * ld + i]);
-  if (a.poly_out) {
+  if constexpr (EXPORT) {
     using PR = PolyRecord<S>;
     double *o = a.poly_out;
 #pragma unroll
@@ -1563,6 +1563,34 @@ void launch_stage_p(const DevData &D, const Params &P, StageArgs &a, const Launc
   if (c.ev) cudaEventRecord(c.ev[3], c.stream);
 }
 
+// Reconstruction with the polynomial export (zfvm_reconstruct); a separate
+// instantiation so the stage kernels carry none of it.
+template <class S, int EQ, int SRC, bool MIXED>
+__global__ void __launch_bounds__(128) k_reconstruct_export(const DevData d, const Params P, StageArgs a) {
+  recon_cell<S, EQ, SRC, MIXED, true>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+template <class S, bool MIXED>
+void launch_export_p(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
+  const int nb = (c.n_cells + 127) / 128;
+  if (c.eq && c.src)
+    k_reconstruct_export<S, 1, 1, MIXED><<<nb, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(D, P, a);
+  else if (c.eq)
+    k_reconstruct_export<S, 1, 0, MIXED><<<nb, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(D, P, a);
+  else if (c.src)
+    k_reconstruct_export<S, 0, 1, MIXED><<<nb, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(D, P, a);
+  else
+    k_reconstruct_export<S, 0, 0, MIXED><<<nb, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(D, P, a);
+}
+
+template <class S>
+void launch_export_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
+  if (c.mixed)
+    launch_export_p<S, true>(D, P, a, c);
+  else
+    launch_export_p<S, false>(D, P, a, c);
+}
+
 template <class S>
 void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
   if (c.mixed)
@@ -1582,7 +1610,8 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
   void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c); \
   void launch_batch_stage_##name(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft,  \
                                  int stage, const BatchCfg &c);                                              \
-  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm);
+  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm);                          \
+  void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c);
 #define ZFVM_DEFINE_SHAPE(name, S)                                                                \
   void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) { \
     launch_stage_t<S>(D, P, a, c);                                                                \
@@ -1594,7 +1623,10 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
                                  int stage, const BatchCfg &c) {                                             \
     launch_batch_stage_t<S>(inst, ct, n_ct, ft, n_ft, stage, c);                                             \
   }                                                                                                          \
-  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm) { batch_occupancy_t<S>(c, blocks_per_sm); }
+  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm) { batch_occupancy_t<S>(c, blocks_per_sm); } \
+  void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {             \
+    launch_export_t<S>(D, P, a, c);                                                                          \
+  }
 
 ZFVM_DECLARE_SHAPE(s2o3)
 ZFVM_DECLARE_SHAPE(s2o2)
