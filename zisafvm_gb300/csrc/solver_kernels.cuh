@@ -105,6 +105,7 @@ struct Params {
   int flux_bc;       // 0 none, 1 constant, 2 isentropic
   int n_stages;
   int gamma2;        // gamma == 2: closed-form equilibrium cell averages
+  double inv_gm1;    // 1 / (gamma - 1), computed once on the host
   double a[4][4], b[4];
 };
 
@@ -366,7 +367,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   const int ld = d.ld;
   const double *__restrict__ q = a.q;
   const double gamma = P.gamma;
-  EqEval ev{gamma, gamma - 1.0, 1.0 / (gamma - 1.0)};
+  EqEval ev{gamma, gamma - 1.0, P.inv_gm1};
 
   const int j0 = d.l2g[i];
   double u0[NV];
@@ -966,7 +967,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
   if (!d.factive[e]) return;
   const int lde = d.lde, ld = d.ld;
   const int L = d.fL[e], R = d.fR[e];
-  EqEval ev{P.gamma, P.gamma - 1.0, 1.0 / (P.gamma - 1.0)};
+  EqEval ev{P.gamma, P.gamma - 1.0, P.inv_gm1};
   double nf[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) nf[v] = 0.0;
@@ -976,6 +977,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
 #pragma unroll
     for (int v = 0; v < NV; ++v) nf_rot[v] = 0.0;
     float g32[NV], mL[ND], mR[ND];
+    bool any64 = false;  // some point added to the FP64 accumulators
 #pragma unroll
     for (int v = 0; v < NV; ++v) g32[v] = 0.f;
 #pragma unroll
@@ -1098,6 +1100,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
           for (int k = 0; k < ND; ++k) mR[k] -= float(Eq * ev.gm1) * wq32 * d.frame32[k * lde + e];
         }
       }
+      any64 = true;
       const double wq = d.fqw[qq * lde + e];
       if (rotated) {
 #pragma unroll
@@ -1107,12 +1110,14 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         for (int v = 0; v < NV; ++v) nf[v] += wq * f[v];
       }
     }
-    from_face<NV, ND>(nf_rot, d.frame, lde, e);
+    if (!MIXED || any64) {
+      from_face<NV, ND>(nf_rot, d.frame, lde, e);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) nf[v] += nf_rot[v];
+      for (int v = 0; v < NV; ++v) nf[v] += nf_rot[v];
+    }
     if (MIXED) {
 #pragma unroll
-      for (int v = 0; v < NV; ++v) a.g32[v * lde + e] = g32[v] + float(nf[v]);
+      for (int v = 0; v < NV; ++v) a.g32[v * lde + e] = any64 ? g32[v] + float(nf[v]) : g32[v];
 #pragma unroll
       for (int k = 0; k < ND; ++k) {
         a.mL32[k * lde + e] = mL[k];
