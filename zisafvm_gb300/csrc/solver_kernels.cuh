@@ -861,16 +861,17 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
 }
 
 // The 2D mixed reconstruction is latency-bound: this build of it is held to
-// 128 registers so four blocks of 128 threads fit on an SM.
+// 96 registers so five blocks of 128 threads fit on an SM (the well-balanced
+// one also holds 5 x 38.9 KB of stencil rows in shared memory).
 template <class S, int EQ, int SRC, bool MIXED>
-__global__ void __launch_bounds__(128, 4) k_reconstruct4(const DevData d, const Params P, StageArgs a) {
+__global__ void __launch_bounds__(128, 5) k_reconstruct_2d(const DevData d, const Params P, StageArgs a) {
   recon_cell<S, EQ, SRC, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <class S, int EQ, int SRC, bool MIXED>
 constexpr auto recon_kernel() {
   if constexpr (MIXED && S::ND == 2)
-    return &k_reconstruct4<S, EQ, SRC, MIXED>;
+    return &k_reconstruct_2d<S, EQ, SRC, MIXED>;
   else
     return &k_reconstruct<S, EQ, SRC, MIXED>;
 }
@@ -1413,7 +1414,7 @@ __global__ void __launch_bounds__(128) km_reconstruct(const BatchInst *__restric
 }
 
 template <class S, int EQ, int SRC, bool MIXED>
-__global__ void __launch_bounds__(128, 4) km_reconstruct4(const BatchInst *__restrict__ inst,
+__global__ void __launch_bounds__(128, 5) km_reconstruct_2d(const BatchInst *__restrict__ inst,
                                                           const Tile *__restrict__ tiles, int n_tiles, int stage) {
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const Tile tl = tiles[t];
@@ -1425,7 +1426,7 @@ __global__ void __launch_bounds__(128, 4) km_reconstruct4(const BatchInst *__res
 template <class S, int EQ, int SRC, bool MIXED>
 constexpr auto batch_recon_kernel() {
   if constexpr (MIXED && S::ND == 2)
-    return &km_reconstruct4<S, EQ, SRC, MIXED>;
+    return &km_reconstruct_2d<S, EQ, SRC, MIXED>;
   else
     return &km_reconstruct<S, EQ, SRC, MIXED>;
 }
