@@ -124,6 +124,9 @@ enum zfvm_flux_bc { ZFVM_FLUX_BC_NONE = 0, ZFVM_FLUX_BC_CONSTANT = 1, ZFVM_FLUX_
  * it was set to (FrozenBC, boundary/frozen_boundary_condition.cpp:39-55). */
 enum zfvm_boundary { ZFVM_BC_NONE = 0, ZFVM_BC_PERIODIC = 1, ZFVM_BC_FROZEN = 2 };
 enum zfvm_precision { ZFVM_FP64 = 0, ZFVM_MIXED = 1 };
+/* CWENO_AO (reconstruction/cweno_ao.cpp:35-53) or WENO_AO (weno_ao.cpp:14-24);
+ * selected like EulerExperiment::deduce_reconstruction (euler_experiment_impl.hpp:363-376) */
+enum zfvm_reconstruction { ZFVM_RC_CWENO_AO = 0, ZFVM_RC_WENO_AO = 1 };
 
 typedef struct {
   int32_t flux;                 /* zfvm_flux                                        */
@@ -142,6 +145,7 @@ typedef struct {
   int32_t precision;            /* zfvm_precision                                   */
   int32_t steps_per_recompute;  /* reconstruction.steps_per_recompute (must be 1)   */
   double recompute_threshold;
+  int32_t reconstruction;       /* reconstruction.mode: zfvm_reconstruction           */
 } zfvm_scheme_desc;
 
 int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *scheme, zfvm_solver **out);

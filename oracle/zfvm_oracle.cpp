@@ -861,6 +861,7 @@ struct Scheme {
   int boundary = 0;
   int steps_per_recompute = 1;
   double recompute_threshold = 0.0;
+  int weno_ao = 0;  // reconstruction.mode: 0 CWENO-AO, 1 WENO-AO
 };
 
 struct CellRC {
@@ -990,11 +991,12 @@ static int local_reconstruct(Problem &pr, idx i, std::vector<Cv> &ul) {
     }
     for (int v = 0; v < 5; ++v) polys[k].a[v] = ul[0][v];
   }
-  // CWENO_AO::reconstruct_impl (cweno_ao.cpp:35-53)
-  const int kh = rc.k_high;
-  for (int k = 0; k < rc.ns; ++k)
-    if (k != kh) poly_axpy(polys[kh], rc.lin_w[k], polys[k], -1.0);
-  {
+  // CWENO_AO::reconstruct_impl (cweno_ao.cpp:35-53); WENO_AO::reconstruct
+  // (weno_ao.cpp:14-24) hybridizes the fitted polynomials as they are
+  if (!pr.s.weno_ao) {
+    const int kh = rc.k_high;
+    for (int k = 0; k < rc.ns; ++k)
+      if (k != kh) poly_axpy(polys[kh], rc.lin_w[k], polys[k], -1.0);
     double alpha = 1.0 / rc.lin_w[kh];
     for (int t = 0; t < 175; ++t) polys[kh].a[t] = alpha * polys[kh].a[t];
   }
@@ -1307,6 +1309,7 @@ const char *zfvm_oracle_last_error(void) { return g_oracle_err.c_str(); }
 //  [13] gravity kind              [14] gravity strength
 //  [15] flux bc (0/1/2)           [16] boundary (0 none, 1 periodic copy, 2 frozen)
 //  [17] steps_per_recompute       [18] recompute_threshold
+//  [19] reconstruction (0 CWENO-AO, 1 WENO-AO)
 int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, int64_t n_cells, const int64_t *vi,
                        const uint8_t *ghost, const int64_t *source, int qe, int qv, int qm,
                        const int8_t *n_stencils, const int8_t *k_high, const int8_t *n_l2g, const int32_t *l2g,
@@ -1353,6 +1356,7 @@ int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, i
     s.boundary = (int)scheme[16];
     s.steps_per_recompute = (int)scheme[17];
     s.recompute_threshold = scheme[18];
+    s.weno_ao = (int)scheme[19];
     pr.rc.resize(n_cells);
     for (idx i = 0; i < n_cells; ++i) {
       CellRC &rc = pr.rc[i];

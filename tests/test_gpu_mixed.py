@@ -127,3 +127,15 @@ def test_mixed_frozen_ghost_cells(zlib):
     assert np.array_equal(u32[ghost], u0[ghost])
     assert state_rel_l1(u32, u64) < TOL_MIXED
     assert perturbation_rel_l1(u32, u64, u0) < 1e-4
+
+
+def test_mixed_weno_ao(zlib):
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=40, amplitude=1e-3)
+    scheme.reconstruction = z.RC_WENO_AO
+    s64, s32 = _pair(mesh, scheme, u0)
+    s64.advance(n_steps=20)
+    s32.advance(n_steps=20)
+    u64, _ = s64.get_state()
+    u32, _ = s32.get_state()
+    assert state_rel_l1(u32, u64) < TOL_MIXED
+    assert perturbation_rel_l1(u32, u64, u0) < 1e-4

@@ -229,6 +229,35 @@ def test_reconstruction_at_points(zlib, olib, case):
         s.reconstruction_eval([mesh.n_cells], x[:1])
 
 
+@pytest.mark.parametrize("case", ["vortex", "polytrope"])
+def test_weno_ao(zlib, olib, case):
+    """reconstruction.mode = WENO-AO (weno_ao.cpp:14-24): the fitted
+    polynomials are hybridized without the CWENO central transformation."""
+    z = zlib
+    if case == "vortex":
+        raw, mesh, scheme, u0 = vortex_2d(n=20, halo=3, flux=z.FLUX_HLLC)
+    else:
+        raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-2)
+    scheme.reconstruction = z.RC_WENO_AO
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    o = _oracle(olib, raw, mesh, scheme)
+    inner = raw.ghost == 0 if raw.ghost is not None else np.ones(mesh.n_cells, bool)
+    t_gpu, t_ref = s.rate_of_change(), o.rate_of_change(u0)
+    assert np.abs(t_gpu[inner] - t_ref[inner]).max() <= 1e-12 * np.abs(t_ref[inner]).max()
+    # and it differs from CWENO-AO
+    scheme.reconstruction = z.RC_CWENO_AO
+    s_c = z.Solver(mesh, scheme)
+    s_c.set_state(u0)
+    assert np.abs(s_c.rate_of_change() - t_gpu).max() > 1e-8 * np.abs(t_ref).max()
+    s.advance(n_steps=4)
+    u_gpu, _ = s.get_state()
+    scheme.reconstruction = z.RC_WENO_AO
+    u_ref, _, _ = _oracle(olib, raw, mesh, scheme).run(u0, n_steps=4)
+    d_gpu, d_ref = (u_gpu - u0)[inner], (u_ref - u0)[inner]
+    assert np.abs(d_gpu - d_ref).max() <= 1e-9 * np.abs(d_ref).max()
+
+
 def test_error_status_nonphysical(zlib):
     """A negative density is reported as ENONPHYSICAL, not a crash."""
     z = zlib

@@ -34,6 +34,7 @@ GRAVITY_NONE, GRAVITY_CONSTANT_RADIAL, GRAVITY_HARMONIC_RADIAL = 0, 1, 2
 FLUX_BC_NONE, FLUX_BC_CONSTANT, FLUX_BC_ISENTROPIC = 0, 1, 2
 BC_NONE, BC_PERIODIC, BC_FROZEN = 0, 1, 2
 FP64, MIXED = 0, 1
+RC_CWENO_AO, RC_WENO_AO = 0, 1
 
 STATUS = {0: "ok", 1: "EINVAL", 2: "ENOMEM", 3: "ENONPHYSICAL", 4: "ENEWTON", 5: "ETIMEDOUT", 6: "ECUDA",
           7: "ESETUP"}
@@ -77,7 +78,8 @@ class _SchemeDesc(C.Structure):
                 ("exponent", C.c_double), ("rk_stages", C.c_int32), ("cfl_number", C.c_double),
                 ("equilibrium", C.c_int32), ("gravity", C.c_int32), ("gravity_strength", C.c_double),
                 ("flux_bc", C.c_int32), ("boundary", C.c_int32), ("precision", C.c_int32),
-                ("steps_per_recompute", C.c_int32), ("recompute_threshold", C.c_double)]
+                ("steps_per_recompute", C.c_int32), ("recompute_threshold", C.c_double),
+                ("reconstruction", C.c_int32)]
 
 
 _LIB = None
@@ -327,6 +329,7 @@ class Scheme:
     precision: int = FP64
     steps_per_recompute: int = 1
     recompute_threshold: float = 0.0
+    reconstruction: int = 0  # RC_CWENO_AO or RC_WENO_AO
 
     def desc(self) -> _SchemeDesc:
         d = _SchemeDesc()
@@ -342,7 +345,8 @@ class Scheme:
         lw = list(self.linear_weights) + [0.0] * (5 - len(self.linear_weights))
         return np.array([self.flux, self.gamma, self.specific_gas_constant, *lw, self.epsilon, self.exponent,
                          self.rk_stages, self.cfl_number, self.equilibrium, self.gravity, self.gravity_strength,
-                         self.flux_bc, self.boundary, self.steps_per_recompute, self.recompute_threshold],
+                         self.flux_bc, self.boundary, self.steps_per_recompute, self.recompute_threshold,
+                         self.reconstruction],
                         dtype=np.float64)
 
 

@@ -276,6 +276,9 @@ int build_solver(zfvm_solver *s) {
   P.n_stages = sc.rk_stages;
   P.gamma2 = sc.gamma == 2.0 ? 1 : 0;
   P.inv_gm1 = 1.0 / (sc.gamma - 1.0);
+  if (sc.reconstruction != ZFVM_RC_CWENO_AO && sc.reconstruction != ZFVM_RC_WENO_AO)
+    return fail(ZFVM_EINVAL, "unknown reconstruction mode");
+  P.weno_ao = sc.reconstruction == ZFVM_RC_WENO_AO ? 1 : 0;
   std::memset(P.a, 0, sizeof(P.a));
   std::memset(P.b, 0, sizeof(P.b));
   if (sc.rk_stages == 1) {

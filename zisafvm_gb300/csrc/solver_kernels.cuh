@@ -106,6 +106,7 @@ struct Params {
   int n_stages;
   int gamma2;        // gamma == 2: closed-form equilibrium cell averages
   double inv_gm1;    // 1 / (gamma - 1), computed once on the host
+  int weno_ao;       // reconstruction: 0 CWENO-AO, 1 WENO-AO
   double a[4][4], b[4];
 };
 
@@ -636,17 +637,21 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     }
   }
 
-  // CWENO-AO: p_c = (p_opt - sum_k g_k p_k) / g_c   (cweno_ao.cpp:35-53)
+  // CWENO-AO: p_c = (p_opt - sum_k g_k p_k) / g_c   (cweno_ao.cpp:35-53);
+  // WENO-AO hybridizes p_opt itself (weno_ao.cpp:14-24)
   R pf[NC][NV];
 #pragma unroll
   for (int c = 0; c < NC; ++c)
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       R x = c < S::C0 ? b0[c][v] : R(0);
+      if (!P.weno_ao) {
 #pragma unroll
-      for (int k = 0; k < S::NB; ++k)
-        if (c < S::CB) x -= R(P.lw[k + 1]) * bb[k][c][v];
-      pf[c][v] = x * R(P.inv_lw0);
+        for (int k = 0; k < S::NB; ++k)
+          if (c < S::CB) x -= R(P.lw[k + 1]) * bb[k][c][v];
+        x *= R(P.inv_lw0);
+      }
+      pf[c][v] = x;
     }
   // smoothness indicators in the scaled variables (poly2d_impl.hpp:325-337)
   auto indicator = [&](auto coef, int ncoef) {
