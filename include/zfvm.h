@@ -146,6 +146,8 @@ typedef struct {
   int32_t steps_per_recompute;  /* reconstruction.steps_per_recompute (must be 1)   */
   double recompute_threshold;
   int32_t reconstruction;       /* reconstruction.mode: zfvm_reconstruction           */
+  double step_rejection_drho;   /* RejectLargeDensityChange drho_crit_rel; 0: RejectNothing */
+  int32_t step_rejection_max_exponent; /* smallest step factor 2^-max_exponent       */
 } zfvm_scheme_desc;
 
 int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *scheme, zfvm_solver **out);
@@ -198,6 +200,14 @@ int zfvm_cfl_dt(zfvm_solver *s, double *dt);
 
 /* One Runge-Kutta step of size dt (RungeKutta::compute_step, runge_kutta.cpp:146-171). */
 int zfvm_step(zfvm_solver *s, double dt);
+
+/* Steps rejected so far by RejectLargeDensityChange (ode/step_rejection.cpp:17-56,
+ * TimeLoop::reject_step time_loop.cpp:182-198): with step_rejection_drho > 0, a
+ * step whose density changes anywhere by more than drho * rho is redone from its
+ * start with half the time step; two accepted steps in a row double the factor
+ * again (at most 1, at least 2^-max_exponent).  Applies to zfvm_advance; not
+ * available in batches. */
+int zfvm_step_rejections(zfvm_solver *s, int64_t *n);
 
 /* TimeLoop (fvm_loops/time_loop.cpp:36-81) without IO: steps with the CFL time
  * step until `n_steps` steps are done (if > 0) or t reaches t_end (if > 0),

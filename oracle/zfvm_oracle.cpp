@@ -862,6 +862,8 @@ struct Scheme {
   int steps_per_recompute = 1;
   double recompute_threshold = 0.0;
   int weno_ao = 0;  // reconstruction.mode: 0 CWENO-AO, 1 WENO-AO
+  double reject_drho = 0.0;  // RejectLargeDensityChange drho_crit_rel (0: RejectNothing)
+  int reject_max_exponent = 0;
 };
 
 struct CellRC {
@@ -1310,6 +1312,7 @@ const char *zfvm_oracle_last_error(void) { return g_oracle_err.c_str(); }
 //  [15] flux bc (0/1/2)           [16] boundary (0 none, 1 periodic copy, 2 frozen)
 //  [17] steps_per_recompute       [18] recompute_threshold
 //  [19] reconstruction (0 CWENO-AO, 1 WENO-AO)
+//  [20] step rejection drho_crit_rel [21] step rejection max exponent
 int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, int64_t n_cells, const int64_t *vi,
                        const uint8_t *ghost, const int64_t *source, int qe, int qv, int qm,
                        const int8_t *n_stencils, const int8_t *k_high, const int8_t *n_l2g, const int32_t *l2g,
@@ -1357,6 +1360,8 @@ int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, i
     s.steps_per_recompute = (int)scheme[17];
     s.recompute_threshold = scheme[18];
     s.weno_ao = (int)scheme[19];
+    s.reject_drho = scheme[20];
+    s.reject_max_exponent = (int)scheme[21];
     pr.rc.resize(n_cells);
     for (idx i = 0; i < n_cells; ++i) {
       CellRC &rc = pr.rc[i];
@@ -1528,20 +1533,41 @@ int zfvm_oracle_run(zfvm_oracle *o, double *state, int64_t n_steps, double t_end
   apply_bc(pr, u, u);
   double t = *t_io;
   int64_t step = 0;
-  double dt = cfl_dt(pr, u);
+  // RejectLargeDensityChange (ode/step_rejection.cpp:17-56): factor and is_good
+  const bool rejecting = pr.s.reject_drho > 0.0;
+  const double min_factor = std::pow(2.0, -(double)std::max(0, pr.s.reject_max_exponent));
+  double factor = 1.0;
+  bool is_good = true;
+  double dt = cfl_dt(pr, u) * (rejecting ? factor : 1.0);
   while (true) {
     bool fin = (n_steps > 0 && step >= n_steps) || (t_end > 0.0 && t_end - t <= 1e-12 * t_end);
     if (fin) break;
     double dts = dt;
     if (t_end > 0.0) dts = std::min(dts, t_end - t);
-    int st = rk_step(pr, u, dts);
+    std::vector<Cv> u1 = u;
+    int st = rk_step(pr, u1, dts);
     if (st) {
       g_oracle_err = st == 4 ? "equilibrium solve is not converging" : "non-physical state";
       return st;
     }
+    if (rejecting) {
+      bool good = true;
+      for (idx i = 0; i < (idx)u.size(); ++i)
+        if (std::abs(u[i][0] - u1[i][0]) > pr.s.reject_drho * u[i][0]) good = false;
+      if (!good) {
+        is_good = false;
+        factor = std::max(min_factor, std::min(factor / 2.0, 1.0));
+        dt = factor * dts;  // TimeLoop::reject_step (time_loop.cpp:182-198)
+        continue;
+      }
+      if (is_good) factor *= 2.0;
+      is_good = true;
+      factor = std::max(min_factor, std::min(factor, 1.0));
+    }
+    u.swap(u1);
     t += dts;
     step += 1;
-    dt = cfl_dt(pr, u);
+    dt = cfl_dt(pr, u) * (rejecting ? factor : 1.0);
   }
   store(u, state);
   *t_io = t;

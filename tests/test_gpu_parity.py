@@ -258,6 +258,31 @@ def test_weno_ao(zlib, olib, case):
     assert np.abs(d_gpu - d_ref).max() <= 1e-9 * np.abs(d_ref).max()
 
 
+def test_step_rejection(zlib, olib):
+    """RejectLargeDensityChange in the time loop: rejected steps are redone from
+    their start with half the step, the factor recovers after two good steps;
+    the accepted steps, their times and the state match the oracle's loop."""
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-1)
+    scheme.step_rejection_drho = 2.4e-3
+    scheme.step_rejection_max_exponent = 6
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    t, n = s.advance(n_steps=12)
+    assert n == 12 and s.step_rejections() > 0
+    u_gpu, _ = s.get_state()
+    u_ref, t_ref, n_ref = _oracle(olib, raw, mesh, scheme).run(u0, n_steps=12)
+    assert n_ref == 12 and abs(t - t_ref) <= 1e-12 * t_ref
+    d_gpu, d_ref = u_gpu - u0, u_ref - u0
+    assert np.abs(d_gpu - d_ref).max() <= 1e-9 * np.abs(d_ref).max()
+    # without rejection the same 12 steps take longer steps
+    scheme.step_rejection_drho = 0.0
+    s2 = z.Solver(mesh, scheme)
+    s2.set_state(u0)
+    t2, _ = s2.advance(n_steps=12)
+    assert t2 > t and s2.step_rejections() == 0
+
+
 def test_error_status_nonphysical(zlib):
     """A negative density is reported as ENONPHYSICAL, not a crash."""
     z = zlib

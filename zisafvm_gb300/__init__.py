@@ -79,7 +79,8 @@ class _SchemeDesc(C.Structure):
                 ("equilibrium", C.c_int32), ("gravity", C.c_int32), ("gravity_strength", C.c_double),
                 ("flux_bc", C.c_int32), ("boundary", C.c_int32), ("precision", C.c_int32),
                 ("steps_per_recompute", C.c_int32), ("recompute_threshold", C.c_double),
-                ("reconstruction", C.c_int32)]
+                ("reconstruction", C.c_int32), ("step_rejection_drho", C.c_double),
+                ("step_rejection_max_exponent", C.c_int32)]
 
 
 _LIB = None
@@ -136,6 +137,7 @@ def load_library() -> C.CDLL:
         "zfvm_batch_slots": [vp, C.POINTER(i32)],
         "zfvm_solver_footprint": [vp, vp, C.POINTER(i64)],
         "zfvm_reconstruct": [vp],
+        "zfvm_step_rejections": [vp, C.POINTER(i64)],
         "zfvm_reconstruction_eval": [vp, i64, C.POINTER(i64), dp, dp],
         "zfvm_server_create": [vp, pp],
         "zfvm_server_destroy": [vp],
@@ -330,6 +332,8 @@ class Scheme:
     steps_per_recompute: int = 1
     recompute_threshold: float = 0.0
     reconstruction: int = 0  # RC_CWENO_AO or RC_WENO_AO
+    step_rejection_drho: float = 0.0   # 0: RejectNothing
+    step_rejection_max_exponent: int = 0
 
     def desc(self) -> _SchemeDesc:
         d = _SchemeDesc()
@@ -346,7 +350,7 @@ class Scheme:
         return np.array([self.flux, self.gamma, self.specific_gas_constant, *lw, self.epsilon, self.exponent,
                          self.rk_stages, self.cfl_number, self.equilibrium, self.gravity, self.gravity_strength,
                          self.flux_bc, self.boundary, self.steps_per_recompute, self.recompute_threshold,
-                         self.reconstruction],
+                         self.reconstruction, self.step_rejection_drho, self.step_rejection_max_exponent],
                         dtype=np.float64)
 
 
@@ -386,6 +390,11 @@ class Solver:
         a = np.zeros((self.mesh.n_cells, 5))
         _check(load_library().zfvm_rate_of_change(self._h, _dp(a)))
         return a
+
+    def step_rejections(self) -> int:
+        n = C.c_int64()
+        _check(load_library().zfvm_step_rejections(self._h, C.byref(n)))
+        return n.value
 
     def reconstruct(self) -> None:
         """Reconstruct the current state (GlobalReconstruction::compute)."""

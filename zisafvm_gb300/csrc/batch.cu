@@ -28,25 +28,7 @@ namespace {
 // mode 0: open a step for every slot; mode 1: close the last step only
 __global__ void k_clock_multi(Clock *const *clocks, const double *cfl, int n, int mode) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  Clock *c = clocks[k];
-  if (c->started) {
-    c->t += c->dt;
-    c->step += 1;
-    c->started = 0;
-  }
-  if (mode == 1 || c->done) return;
-  bool fin = (c->n_steps > 0 && c->step >= c->n_steps) ||
-             (c->t_end > 0.0 && c->t_end - c->t <= 1e-12 * c->t_end) || c->status != 0;
-  if (fin) {
-    c->done = 1;
-    return;
-  }
-  double dt = c->fixed_dt > 0.0 ? c->fixed_dt : cfl[k] * __longlong_as_double((long long)c->cfl_min);
-  if (c->t_end > 0.0) dt = fmin(dt, c->t_end - c->t);
-  c->dt = dt;
-  c->cfl_min = 0x7ff0000000000000ull;
-  c->started = 1;
+  if (k < n) clock_step(clocks[k], cfl[k], mode);
 }
 
 // number of slots still running
@@ -241,6 +223,8 @@ extern "C" int zfvm_batch_destroy(zfvm_batch *b) {
 extern "C" int zfvm_batch_add(zfvm_batch *b, zfvm_solver *s, int64_t n_steps, double t_end, int32_t *slot) {
   if (!b || !s) return fail(ZFVM_EINVAL, "null argument");
   if (n_steps <= 0 && !(t_end > 0.0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > 0");
+  if (s->scheme.step_rejection_drho > 0.0)
+    return fail(ZFVM_EINVAL, "step rejection is not supported in batches (advance the solver by itself)");
   BATCH_GUARD_BEGIN
   int k = -1;
   for (int j = 0; j < b->max_slots; ++j) {

@@ -25,25 +25,7 @@ namespace zfvm {
 namespace dev {
 
 // mode 0: open a step; mode 1: close the last step only
-__global__ void k_clock(Clock *c, double cfl, int mode) {
-  if (c->started) {
-    c->t += c->dt;
-    c->step += 1;
-    c->started = 0;
-  }
-  if (mode == 1 || c->done) return;
-  bool fin = (c->n_steps > 0 && c->step >= c->n_steps) ||
-             (c->t_end > 0.0 && c->t_end - c->t <= 1e-12 * c->t_end) || c->status != 0;
-  if (fin) {
-    c->done = 1;
-    return;
-  }
-  double dt = c->fixed_dt > 0.0 ? c->fixed_dt : cfl * __longlong_as_double((long long)c->cfl_min);
-  if (c->t_end > 0.0) dt = fmin(dt, c->t_end - c->t);
-  c->dt = dt;
-  c->cfl_min = 0x7ff0000000000000ull;
-  c->started = 1;
-}
+__global__ void k_clock(Clock *c, double cfl, int mode) { clock_step(c, cfl, mode); }
 
 // state AoS (n x 5) <-> SoA (NV x ld); the 2D layout drops the third momentum
 __global__ void k_aos_to_soa(const double *aos, double *soa, int n, int ld, int nv) {
@@ -109,6 +91,7 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   a.dev0 = s->dev0.p;
   a.dev032 = s->dev032.p;
   a.eq32 = s->eq32.p;
+  a.uprev = s->uprev.p;
   a.nf = s->nfb.p;
   a.src = s->has_src ? s->srcb.p : nullptr;
   a.eqth = s->has_eq ? s->eqth.p : nullptr;
@@ -165,9 +148,28 @@ void launch_cfl(zfvm_solver *s) {
   CK(cudaGetLastError());
 }
 
+// after every clock launch when step rejection is on: put back the start of a
+// rejected step (a no-op launch otherwise)
+void enqueue_restore(zfvm_solver *s) {
+  if (!s->uprev.p) return;
+  const int nb = (s->n_cells + 127) / 128;
+  if (s->nv == 4)
+    k_restore<4><<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
+  else
+    k_restore<5><<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
+  CK(cudaGetLastError());
+}
+
+void close_step(zfvm_solver *s) {
+  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
+  CK(cudaGetLastError());
+  enqueue_restore(s);
+}
+
 void enqueue_step(zfvm_solver *s) {
   k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 0);
   CK(cudaGetLastError());
+  enqueue_restore(s);
   for (int st = 0; st < s->P.n_stages; ++st) {
     StageArgs a = stage_args(s, st, nullptr);
     dispatch_stage(s, a);
@@ -190,6 +192,17 @@ int status_to_code(int st, std::string &msg) {
     return ZFVM_ENONPHYSICAL;
   }
   return ZFVM_OK;
+}
+
+Clock fresh_clock(const zfvm_solver *s, double t) {
+  Clock c{};
+  c.t = t;
+  c.cfl_min = 0x7ff0000000000000ull;
+  c.reject_drho = s->scheme.step_rejection_drho;
+  c.factor = 1.0;
+  c.min_factor = std::pow(2.0, -(double)std::max(0, s->scheme.step_rejection_max_exponent));
+  c.good_prev = 1;
+  return c;
 }
 
 Clock read_clock(zfvm_solver *s) {
@@ -536,13 +549,17 @@ int build_solver(zfvm_solver *s) {
   if (!s->mixed) s->nfb.alloc((size_t)nv * lde);
   s->tend.alloc((size_t)nv * ld);
   s->aos.alloc((size_t)5 * n);
+  if (sc.step_rejection_drho < 0.0) return fail(ZFVM_EINVAL, "negative step_rejection_drho");
+  if (sc.step_rejection_drho > 0.0) {
+    s->uprev.alloc((size_t)nv * ld);
+    s->uprev.zero(s->stream);
+  }
   s->clock.alloc(1);
   for (auto *b : {&s->u0, &s->ux, &s->kbuf, &s->fv, &s->nfb, &s->tend, &s->dev0}) b->zero(s->stream);
   s->fv32.zero(s->stream);
   if (s->has_src) s->srcb.zero(s->stream);
   if (s->has_eq) s->eqth.zero(s->stream);
-  Clock c{};
-  c.cfl_min = 0x7ff0000000000000ull;
+  Clock c = fresh_clock(s, 0.0);
   write_clock(s, c);
   CK(cudaStreamSynchronize(s->stream));
 
@@ -597,6 +614,7 @@ int build_solver(zfvm_solver *s) {
            s->mL32.n + s->mR32.n + s->src32.n + s->kbuf32.n));
   add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n + s->eq32.n + s->phi_fq2.n));
   add(4 * s->dev032.n);
+  add(8 * s->uprev.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
            s->ux.n + s->kbuf.n + s->fv.n + s->nfb.n + s->srcb.n + s->eqth.n + s->tend.n + s->aos.n));
@@ -618,6 +636,8 @@ void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double f
   c.n_steps = n_steps;
   c.t_end = t_end;
   c.fixed_dt = fixed_dt;
+  // step rejection belongs to the time loop (TimeLoop), not to a single step
+  c.reject_drho = fixed_dt > 0.0 ? 0.0 : s->scheme.step_rejection_drho;
   write_clock(s, c);
 }
 
@@ -695,9 +715,7 @@ extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(s->qsplit.p + half, s->qsplit.p, half * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
   }
-  Clock c{};
-  c.t = t;
-  c.cfl_min = 0x7ff0000000000000ull;
+  Clock c = fresh_clock(s, t);
   write_clock(s, c);
   launch_cfl(s);
   CK(cudaStreamSynchronize(s->stream));
@@ -762,8 +780,7 @@ extern "C" int zfvm_step(zfvm_solver *s, double dt) {
   SOLVER_GUARD_BEGIN
   reset_clock_for_run(s, 1, 0.0, dt);
   enqueue_step(s);
-  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
-  CK(cudaGetLastError());
+  close_step(s);
   Clock c = read_clock(s);
   std::string msg;
   int code = status_to_code(c.status, msg);
@@ -780,17 +797,17 @@ extern "C" int zfvm_advance(zfvm_solver *s, int64_t n_steps, double t_end, doubl
   const int chunk = n_steps > 0 ? (int)std::min<int64_t>(n_steps, 16) : 16;
   build_graph(s, chunk);
   int64_t launched = 0;
+  const bool rejecting = s->uprev.p != nullptr;  // rejected steps do not count
   while (true) {
     CK(cudaGraphLaunch(s->graph, s->stream));
     launched += chunk;
-    if (n_steps > 0 && launched >= n_steps) break;
-    if (launched % (chunk * 8) == 0 || n_steps <= 0) {
+    if (n_steps > 0 && launched >= n_steps && !rejecting) break;
+    if (launched % (chunk * 8) == 0 || n_steps <= 0 || rejecting) {
       Clock c = read_clock(s);
       if (c.done) break;
     }
   }
-  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
-  CK(cudaGetLastError());
+  close_step(s);
   Clock c = read_clock(s);
   if (t_out) *t_out = c.t;
   if (steps_out) *steps_out = c.step;
@@ -822,7 +839,7 @@ extern "C" int zfvm_advance_timed(zfvm_solver *s, int64_t n_steps, float *ms) {
   CK(cudaEventElapsedTime(ms, e0, e1));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
+  close_step(s);
   Clock c = read_clock(s);
   std::string msg;
   int code = status_to_code(c.status, msg);
@@ -853,12 +870,13 @@ extern "C" int zfvm_kernel_times(zfvm_solver *s, int64_t n_steps, float *ms) {
   for (auto &e : ev) CK(cudaEventCreate(&e));
   for (int64_t k = 0; k < n_steps; ++k) {
     k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 0);
+    enqueue_restore(s);
     for (int st = 0; st < S; ++st) {
       StageArgs a = stage_args(s, st, nullptr);
       dispatch_stage(s, a, &ev[((size_t)k * S + st) * 4]);
     }
   }
-  k_clock<<<1, 1, 0, s->stream>>>(s->clock.p, s->P.cfl, 1);
+  close_step(s);
   CK(cudaStreamSynchronize(s->stream));
   double acc[3] = {0, 0, 0};
   for (size_t b = 0; b < ev.size(); b += 4)
@@ -911,6 +929,7 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
     if (!mixed) b += 8 * nv * ld;                                               // srcb
   }
   if (has_eq) b += 8 * 4 * ld;                                                  // eqth
+  if (sc.step_rejection_drho > 0.0) b += 8 * nv * ld;                            // uprev
   if (mixed) {
     b += 4 * (NP * ld + nd * nd * lde + NC * ld + nf * nqf * nd * ld + nqc * nd * ld);  // pinv32 frame32 mom32 xfq32 xcq32
     b += 4 * (nv * lde + 2 * nd * lde + kst * nv * ld + nf * nqf * nv * ld);          // g32 mL32 mR32 kbuf32 fv32
@@ -1029,4 +1048,13 @@ extern "C" int zfvm_reconstruction_eval(const zfvm_solver *s, int64_t n, const i
     case 2: return eval_records<S3o3>(s, n, cells, x, u);
     default: return eval_records<S3o2>(s, n, cells, x, u);
   }
+}
+
+// number of steps rejected (RejectLargeDensityChange) since the state was set
+extern "C" int zfvm_step_rejections(zfvm_solver *s, int64_t *n) {
+  if (!s || !n) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
+  *n = read_clock(s).n_rejected;
+  return ZFVM_OK;
+  SOLVER_GUARD_END
 }

@@ -51,7 +51,60 @@ struct Clock {
   unsigned long long cfl_min;  // bits of a positive double
   long long step, n_steps;
   int done, started, status, pad;
+  // RejectLargeDensityChange (ode/step_rejection.cpp:17-56); reject_drho = 0
+  // rejects nothing.  factor scales the CFL step; a rejected step is redone
+  // from its saved start with factor * dt.
+  double reject_drho, factor, min_factor;
+  int rejected, good_prev, restore, retry;
+  long long n_rejected;
 };
+
+// Close the running step and open the next one (mode 0) or only close it
+// (mode 1): the TimeLoop of fvm_loops/time_loop.cpp:36-81 on the device clock.
+__device__ __forceinline__ void clock_step(Clock *c, double cfl, int mode) {
+  if (c->started) {
+    c->started = 0;
+    if (c->rejected) {
+      // RejectLargeDensityChange::check (bad step) + TimeLoop::reject_step
+      c->rejected = 0;
+      c->good_prev = 0;
+      c->factor = fmax(c->min_factor, fmin(0.5 * c->factor, 1.0));
+      c->dt = c->factor * c->dt;
+      c->retry = 1;
+      c->restore = 1;
+      c->n_rejected += 1;
+    } else {
+      c->t += c->dt;
+      c->step += 1;
+      c->restore = 0;
+      if (c->reject_drho > 0.0) {
+        if (c->good_prev) c->factor = fmax(c->min_factor, fmin(2.0 * c->factor, 1.0));
+        c->good_prev = 1;
+      }
+    }
+  } else {
+    c->restore = 0;
+  }
+  if (mode == 1 || c->done) return;
+  bool fin = (c->n_steps > 0 && c->step >= c->n_steps) ||
+             (c->t_end > 0.0 && c->t_end - c->t <= 1e-12 * c->t_end) || c->status != 0;
+  if (fin) {
+    c->done = 1;
+    return;
+  }
+  double dt;
+  if (c->retry) {
+    dt = c->dt;
+    c->retry = 0;
+  } else {
+    dt = c->fixed_dt > 0.0 ? c->fixed_dt : cfl * __longlong_as_double((long long)c->cfl_min);
+    if (c->reject_drho > 0.0) dt *= c->factor;
+  }
+  if (c->t_end > 0.0) dt = fmin(dt, c->t_end - c->t);
+  c->dt = dt;
+  c->cfl_min = 0x7ff0000000000000ull;
+  c->started = 1;
+}
 
 // Device arrays shared by all kernels (struct of pointers, passed by value).
 struct DevData {
@@ -136,6 +189,8 @@ struct StageArgs {
   float2 *eq32;
   // when non-null: every reconstructed cell's polynomial record [PolyRecord][ld]
   double *poly_out;
+  // step rejection: the last stage saves the step's start state here [NV][ld]
+  double *uprev;
   double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
   float coef32[4];   // the same row rounded to FP32 (mixed form)
   int stage;
@@ -1354,6 +1409,13 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
           a.ux[v * ld + i] = un[v];
         }
       } else {
+        if (a.uprev) {
+          // RejectLargeDensityChange::check: |rho_1 - rho_0| > drho_crit rho_0 in any cell
+          const double rho0 = a.u0[i];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) a.uprev[v * ld + i] = a.u0[v * ld + i];
+          if (fabs(un[0] - rho0) > d.clock->reject_drho * rho0) atomicOr(&d.clock->rejected, 1);
+        }
 #pragma unroll
         for (int v = 0; v < NV; ++v) a.u0[v * ld + i] = un[v];
         cand = MIXED ? cfl_candidate_1rcp<NV>(un, P.gamma, d.r_eff[i]) : cfl_candidate<NV>(un, P.gamma, d.r_eff[i]);
@@ -1391,6 +1453,24 @@ __global__ void __launch_bounds__(128) k_cfl(const DevData d, const Params P, co
     cand = cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
   }
   block_min_to_clock(cand, d.clock);
+}
+
+// TimeLoop::reject_step: put back the saved start of a rejected step (interior
+// cells; ghost cells never change) and, in the mixed form, its FP32 pairs.
+template <int NV>
+__global__ void k_restore(const Clock *clock, const uint8_t *flags, const double *uprev, double *u0, float2 *pairs,
+                          int n, int ld) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !clock->restore || !(flags[i] & kInterior)) return;
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const double x = uprev[(size_t)v * ld + i];
+    u0[(size_t)v * ld + i] = x;
+    if (pairs) {
+      const DF p = df_split(x);
+      pairs[(size_t)v * ld + i] = make_float2(p.hi, p.lo);
+    }
+  }
 }
 
 // ------------------------------------------------- multi-instance kernels

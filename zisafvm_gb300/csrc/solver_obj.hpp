@@ -83,6 +83,7 @@ struct zfvm_solver {
   zfvm::DBuf<float2> eq32, phi_fq2;       // mixed + equilibrium: (h_r, f, K) pairs; phi at face points
   zfvm::DBuf<float> dev032;               // mixed: FP32 copy of the cell deviation
   zfvm::DBuf<double> poly;                // exported reconstruction records (zfvm_reconstruct)
+  zfvm::DBuf<double> uprev;               // step rejection: start state of the running step
   std::vector<double> poly_host;
   zfvm::DBuf<zfvm::dev::Clock> clock;
   bool has_src = false, has_eq = false, mixed = false;
@@ -95,6 +96,7 @@ struct zfvm_solver {
 // helpers shared with the batch engine (solver.cu)
 zfvm::dev::StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out);
 zfvm::dev::Clock read_clock(zfvm_solver *s);
+zfvm::dev::Clock fresh_clock(const zfvm_solver *s, double t);
 void write_clock(zfvm_solver *s, const zfvm::dev::Clock &c);
 void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt);
 // ZFVM_* status and message for the device status bits of a Clock
