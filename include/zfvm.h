@@ -148,6 +148,8 @@ typedef struct {
   int32_t reconstruction;       /* reconstruction.mode: zfvm_reconstruction           */
   double step_rejection_drho;   /* RejectLargeDensityChange drho_crit_rel; 0: RejectNothing */
   int32_t step_rejection_max_exponent; /* smallest step factor 2^-max_exponent       */
+  double heating_rate;          /* heating.rate (model/heating.hpp:52-77); 0: none   */
+  double heating_r0, heating_r1; /* heating.lower_boundary / upper_boundary           */
 } zfvm_scheme_desc;
 
 int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *scheme, zfvm_solver **out);

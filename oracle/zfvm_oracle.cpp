@@ -864,6 +864,7 @@ struct Scheme {
   int weno_ao = 0;  // reconstruction.mode: 0 CWENO-AO, 1 WENO-AO
   double reject_drho = 0.0;  // RejectLargeDensityChange drho_crit_rel (0: RejectNothing)
   int reject_max_exponent = 0;
+  double heat_rate = 0.0, heat_r0 = 0.0, heat_r1 = 0.0;  // heating.{rate, lower_boundary, upper_boundary}
 };
 
 struct CellRC {
@@ -1208,6 +1209,29 @@ static int flux_bc(Problem &pr, std::vector<Cv> &tend, const std::vector<Cv> &st
 }
 
 // SumRatesOfChange{Zero, FluxLoop, GravitySource, FluxBC} (ode/rate_of_change.cpp:21-54)
+// Heating (model/heating.hpp:29-77): dE/dt += average over the cell of
+// rho(x) * rate(x), rho from the reconstruction of this stage, rate = epsilon on
+// lower_boundary <= |x| <= upper_boundary.
+static void heating_source(Problem &pr, std::vector<Cv> &tend) {
+  if (pr.s.heat_rate == 0.0) return;
+  const auto &g = pr.g;
+#pragma omp parallel for schedule(static, 8) num_threads(pr.threads)
+  for (idx i = 0; i < g.n_cells; ++i) {
+    const auto &rc = pr.rc[i];
+    const QR &cell = g.cells[i];
+    double acc = 0.0;
+    for (size_t q = 0; q < cell.w.size(); ++q) {
+      const XYZ &x = cell.x[q];
+      const double r = std::sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+      const double rate = (pr.s.heat_r0 <= r && r <= pr.s.heat_r1) ? pr.s.heat_rate : 0.0;
+      const auto bg = pr.s.equilibrium ? rc.pv_cell[q] : std::make_pair(RhoE{0, 0}, std::array<double, 2>{0, 0});
+      const double f = rc_value(rc, x, bg)[0] * rate;
+      acc = q == 0 ? cell.w[q] * f : acc + cell.w[q] * f;
+    }
+    tend[i][4] += acc / cell.volume;
+  }
+}
+
 static int rate_of_change(Problem &pr, std::vector<Cv> &tend, const std::vector<Cv> &state) {
   for (auto &t : tend) t = Cv{0, 0, 0, 0, 0};
   int st = compute_patch(pr, tend, state, pr.interior_cells, pr.interior_faces);
@@ -1215,6 +1239,7 @@ static int rate_of_change(Problem &pr, std::vector<Cv> &tend, const std::vector<
   st = compute_patch(pr, tend, state, pr.exterior_cells, pr.exterior_faces);
   if (st) return st;
   gravity_source(pr, tend);
+  heating_source(pr, tend);
   return flux_bc(pr, tend, state);
 }
 
@@ -1313,6 +1338,7 @@ const char *zfvm_oracle_last_error(void) { return g_oracle_err.c_str(); }
 //  [17] steps_per_recompute       [18] recompute_threshold
 //  [19] reconstruction (0 CWENO-AO, 1 WENO-AO)
 //  [20] step rejection drho_crit_rel [21] step rejection max exponent
+//  [22] heating rate              [23] heating r0   [24] heating r1
 int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, int64_t n_cells, const int64_t *vi,
                        const uint8_t *ghost, const int64_t *source, int qe, int qv, int qm,
                        const int8_t *n_stencils, const int8_t *k_high, const int8_t *n_l2g, const int32_t *l2g,
@@ -1362,6 +1388,9 @@ int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, i
     s.weno_ao = (int)scheme[19];
     s.reject_drho = scheme[20];
     s.reject_max_exponent = (int)scheme[21];
+    s.heat_rate = scheme[22];
+    s.heat_r0 = scheme[23];
+    s.heat_r1 = scheme[24];
     pr.rc.resize(n_cells);
     for (idx i = 0; i < n_cells; ++i) {
       CellRC &rc = pr.rc[i];

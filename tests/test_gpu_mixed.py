@@ -139,3 +139,16 @@ def test_mixed_weno_ao(zlib):
     u32, _ = s32.get_state()
     assert state_rel_l1(u32, u64) < TOL_MIXED
     assert perturbation_rel_l1(u32, u64, u0) < 1e-4
+
+
+def test_mixed_heating(zlib):
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=40, amplitude=1e-3)
+    scheme.heating_rate, scheme.heating_r0, scheme.heating_r1 = 0.3, 0.2, 0.6
+    s64, s32 = _pair(mesh, scheme, u0)
+    t64, t32 = s64.rate_of_change(), s32.rate_of_change()
+    assert np.abs(t32[:, 4] - t64[:, 4]).max() <= 1e-6 * np.abs(t64[:, 4]).max()
+    s64.advance(n_steps=20)
+    s32.advance(n_steps=20)
+    u64, _ = s64.get_state()
+    u32, _ = s32.get_state()
+    assert state_rel_l1(u32, u64) < TOL_MIXED

@@ -283,6 +283,32 @@ def test_step_rejection(zlib, olib):
     assert t2 > t and s2.step_rejections() == 0
 
 
+@pytest.mark.parametrize("well_balanced", [True, False])
+def test_heating(zlib, olib, well_balanced):
+    """Heating source (model/heating.hpp): the cell average of rho * rate with
+    rate = epsilon on a radial shell, rho from the reconstruction."""
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-2)
+    scheme.heating_rate, scheme.heating_r0, scheme.heating_r1 = 0.3, 0.2, 0.6
+    if not well_balanced:
+        scheme.equilibrium, scheme.flux_bc = z.EQ_NONE, z.FLUX_BC_CONSTANT
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    o = _oracle(olib, raw, mesh, scheme)
+    t_gpu, t_ref = s.rate_of_change(), o.rate_of_change(u0)
+    assert np.abs(t_gpu - t_ref).max() <= 1e-12 * np.abs(t_ref).max()
+    heat = dict(heating_rate=0.0)
+    s0 = z.Solver(mesh, z.Scheme(**{**scheme.__dict__, **heat}))
+    s0.set_state(u0)
+    dE = t_gpu[:, 4] - s0.rate_of_change()[:, 4]
+    assert dE.max() > 0 and np.abs(t_gpu[:, :4] - s0.rate_of_change()[:, :4]).max() == 0
+    s.advance(n_steps=3)
+    u_gpu, _ = s.get_state()
+    u_ref, _, _ = o.run(u0, n_steps=3)
+    d_gpu, d_ref = u_gpu - u0, u_ref - u0
+    assert np.abs(d_gpu - d_ref).max() <= 1e-9 * np.abs(d_ref).max()
+
+
 def test_error_status_nonphysical(zlib):
     """A negative density is reported as ENONPHYSICAL, not a crash."""
     z = zlib

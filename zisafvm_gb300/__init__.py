@@ -80,7 +80,8 @@ class _SchemeDesc(C.Structure):
                 ("flux_bc", C.c_int32), ("boundary", C.c_int32), ("precision", C.c_int32),
                 ("steps_per_recompute", C.c_int32), ("recompute_threshold", C.c_double),
                 ("reconstruction", C.c_int32), ("step_rejection_drho", C.c_double),
-                ("step_rejection_max_exponent", C.c_int32)]
+                ("step_rejection_max_exponent", C.c_int32), ("heating_rate", C.c_double),
+                ("heating_r0", C.c_double), ("heating_r1", C.c_double)]
 
 
 _LIB = None
@@ -334,6 +335,9 @@ class Scheme:
     reconstruction: int = 0  # RC_CWENO_AO or RC_WENO_AO
     step_rejection_drho: float = 0.0   # 0: RejectNothing
     step_rejection_max_exponent: int = 0
+    heating_rate: float = 0.0  # heating.rate; 0: no heating
+    heating_r0: float = 0.0
+    heating_r1: float = 0.0
 
     def desc(self) -> _SchemeDesc:
         d = _SchemeDesc()
@@ -350,7 +354,8 @@ class Scheme:
         return np.array([self.flux, self.gamma, self.specific_gas_constant, *lw, self.epsilon, self.exponent,
                          self.rk_stages, self.cfl_number, self.equilibrium, self.gravity, self.gravity_strength,
                          self.flux_bc, self.boundary, self.steps_per_recompute, self.recompute_threshold,
-                         self.reconstruction, self.step_rejection_drho, self.step_rejection_max_exponent],
+                         self.reconstruction, self.step_rejection_drho, self.step_rejection_max_exponent,
+                         self.heating_rate, self.heating_r0, self.heating_r1],
                         dtype=np.float64)
 
 

@@ -272,6 +272,7 @@ int build_solver(zfvm_solver *s) {
   s->mixed = sc.precision == ZFVM_MIXED;
   s->has_src = sc.gravity != ZFVM_GRAVITY_NONE;
   if (s->has_eq && !s->has_src) return fail(ZFVM_EINVAL, "isentropic well-balancing needs gravity");
+  if (sc.heating_rate != 0.0 && !s->has_src) return fail(ZFVM_EINVAL, "heating needs a gravity source in this build");
   if (sc.flux_bc == ZFVM_FLUX_BC_ISENTROPIC && !s->has_eq)
     return fail(ZFVM_EINVAL, "isentropic flux boundary needs isentropic well-balancing");
   Params &P = s->P;
@@ -468,6 +469,17 @@ int build_solver(zfvm_solver *s) {
     s->cqx.upload(h_cqx);
     s->cqw.upload(h_cqw);
     s->phi_fq.upload(h_phi_fq);
+    if (sc.heating_rate != 0.0) {
+      // make_heating_source (model/heating.hpp:52-77): rate on r0 <= |x| <= r1
+      std::vector<double> hw((size_t)nqc * ld, 0.0);
+      for (index_t i = 0; i < n; ++i)
+        for (int q = 0; q < nqc; ++q) {
+          const double r = norm(g.cell_qx[i * nqc + q]);
+          const bool in = sc.heating_r0 <= r && r <= sc.heating_r1;
+          hw[(size_t)q * ld + i] = in ? sc.heating_rate * g.cell_qw[i * nqc + q] : 0.0;
+        }
+      s->heat_w.upload(hw);
+    }
     if (!s->mixed) s->srcb.alloc((size_t)nv * ld);
   }
   if (s->has_eq) s->eqth.alloc((size_t)4 * ld);
@@ -582,6 +594,7 @@ int build_solver(zfvm_solver *s) {
   D.m1s = s->m1s.p;
   D.vars = s->vars.p;
   D.phi_fq2 = s->phi_fq2.p;
+  D.heat_w = s->heat_w.p;
   D.phi_var = s->phi_var.p;
   D.bloc = s->bloc.p;
   D.center = s->center.p;
@@ -615,6 +628,7 @@ int build_solver(zfvm_solver *s) {
   add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n + s->eq32.n + s->phi_fq2.n));
   add(4 * s->dev032.n);
   add(8 * s->uprev.n);
+  add(8 * s->heat_w.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
            s->ux.n + s->kbuf.n + s->fv.n + s->nfb.n + s->srcb.n + s->eqth.n + s->tend.n + s->aos.n));
@@ -930,6 +944,7 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
   }
   if (has_eq) b += 8 * 4 * ld;                                                  // eqth
   if (sc.step_rejection_drho > 0.0) b += 8 * nv * ld;                            // uprev
+  if (sc.heating_rate != 0.0 && has_src) b += 8 * nqc * ld;                       // heat_w
   if (mixed) {
     b += 4 * (NP * ld + nd * nd * lde + NC * ld + nf * nqf * nd * ld + nqc * nd * ld);  // pinv32 frame32 mom32 xfq32 xcq32
     b += 4 * (nv * lde + 2 * nd * lde + kst * nv * ld + nf * nqf * nv * ld);          // g32 mL32 mR32 kbuf32 fv32

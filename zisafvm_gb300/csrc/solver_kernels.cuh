@@ -144,6 +144,7 @@ struct DevData {
   const float2 *m1s;     // [ld] phi_m1 as an FP32 (hi, lo) pair
   const float2 *vars;    // [ld] phi_var as an FP32 (hi, lo) pair
   const float2 *phi_fq2; // [NQF][lde] phi at the face points as FP32 (hi, lo) pairs
+  const double *heat_w;  // [NQC][ld] w_q * heating rate at x_q, or null (no heating)
   Clock *clock;
 };
 
@@ -410,6 +411,32 @@ constexpr bool kRowsInShared = MIXED && EQ && S::ND == 2;
 template <class S, int EQ, bool MIXED>
 constexpr size_t recon_smem_bytes(int threads) {
   return kRowsInShared<S, EQ, MIXED> ? (size_t)(S::MAXL - 1) * S::NV * threads * sizeof(float) : 0;
+}
+
+// Heating (model/heating.hpp:29-45) in the mixed form: sum_q w_q rate(x_q)
+// rho(x_q) with rho = equilibrium (FP64) + cell deviation (FP64) + polynomial
+// part (FP32); the caller divides by the volume.
+template <class S, int EQ, bool MIXED, class PolyX>
+__device__ __forceinline__ double heating(const DevData &d, const EqEval &ev, const EqEval::Bound &eqb, bool found,
+                                          const double *dev0, const PolyX &poly_X, int i) {
+  using R = std::conditional_t<MIXED, float, double>;
+  constexpr int ND = S::ND, NV = S::NV;
+  const int ld = d.ld;
+  double h = 0.0;
+  R hp = R(0);
+#pragma unroll
+  for (int qq = 0; qq < S::NQC; ++qq) {
+    const double hw = d.heat_w[qq * ld + i];
+    double r_eq = 0.0, E_eq = 0.0;
+    if (EQ && found) eqb.at(ev, d.phi_cq[qq * ld + i], r_eq, E_eq);
+    h += hw * (r_eq + dev0[0]);
+    R X[ND], pv[NV];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) X[k] = R(d.xcq32[(qq * ND + k) * ld + i]);
+    poly_X(X, pv);
+    hp += R(hw) * pv[0];
+  }
+  return h + double(hp);
 }
 
 template <class S, int EQ, int SRC, bool MIXED, bool EXPORT = false>
@@ -880,6 +907,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       mg0 += dev0[1 + k] * G;
     }
     s_acc[NV - 1] += -mg0 + double(acc[NV - 1]);
+    if (d.heat_w) s_acc[NV - 1] += heating<S, EQ, MIXED>(d, ev, eqb, found, dev0, poly_X, i);
     const double iv = d.inv_vol[i];
 #pragma unroll
     for (int v = 0; v < NV; ++v) a.src32[v * ld + i] = float(s_acc[v] * iv);
@@ -908,6 +936,12 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
         mg += du[1 + k] * g[k];
       }
       s_acc[NV - 1] += w * (-mg);
+      if (d.heat_w) {
+        // Heating (model/heating.hpp:29-45): rho(x_q) * rate(x_q), rho the full reconstruction
+        double r_eq = 0.0, E_eq = 0.0;
+        if (EQ && found) eqb.at(ev, d.phi_cq[qq * ld + i], r_eq, E_eq);
+        s_acc[NV - 1] += d.heat_w[qq * ld + i] * (r_eq + r);
+      }
     }
     const double iv = d.inv_vol[i];
 #pragma unroll
@@ -1217,7 +1251,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
       for (int k = 0; k < ND; ++k) nf[1 + k] = pn * d.frame[k * lde + e];
     }
   }
-  if (MIXED) {
+  if constexpr (MIXED) {
     // boundary face: flux of the cell average (FluxBC); with an equilibrium and
     // no FluxBC the cell's surface source term on this face remains
     float mLb[ND];
@@ -1241,10 +1275,10 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
       a.mL32[k * lde + e] = mLb[k];
       a.mR32[k * lde + e] = 0.f;
     }
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int v = 0; v < NV; ++v) a.nf[v * lde + e] = nf[v];
+    for (int v = 0; v < NV; ++v) a.nf[v * lde + e] = nf[v];
+  }
 }
 
 template <class S, int FLUX, int EQ, bool MIXED>

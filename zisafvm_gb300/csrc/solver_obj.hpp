@@ -84,6 +84,7 @@ struct zfvm_solver {
   zfvm::DBuf<float> dev032;               // mixed: FP32 copy of the cell deviation
   zfvm::DBuf<double> poly;                // exported reconstruction records (zfvm_reconstruct)
   zfvm::DBuf<double> uprev;               // step rejection: start state of the running step
+  zfvm::DBuf<double> heat_w;              // heating: w_q * rate(x_q) at the cell quadrature points
   std::vector<double> poly_host;
   zfvm::DBuf<zfvm::dev::Clock> clock;
   bool has_src = false, has_eq = false, mixed = false;
