@@ -954,18 +954,25 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
   recon_cell<S, EQ, SRC, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
-// The 2D mixed reconstruction is latency-bound: this build of it is held to
-// 96 registers so five blocks of 128 threads fit on an SM (the well-balanced
-// one also holds 5 x 38.9 KB of stencil rows in shared memory).
+// The mixed reconstruction is latency-bound: its builds are held to the
+// register count that fits kMixedReconBlocks blocks of 128 threads per SM
+// (2D: 96 registers, five blocks -- the well-balanced one also holds 5 x 38.9 KB
+// of stencil rows in shared memory; 3D order 2: 128, four; 3D order 3: 168,
+// three; the 3D well-balanced builds keep their own allocation, which a bound
+// would only turn into spills).
+template <class S, int EQ>
+constexpr int kMixedReconBlocks = S::ND == 2 ? 5 : (EQ ? 1 : (S::C0 <= 3 ? 4 : 3));
+
 template <class S, int EQ, int SRC, bool MIXED>
-__global__ void __launch_bounds__(128, 5) k_reconstruct_2d(const DevData d, const Params P, StageArgs a) {
+__global__ void __launch_bounds__(128, kMixedReconBlocks<S, EQ>) k_reconstruct_mixed(const DevData d, const Params P,
+                                                                                 StageArgs a) {
   recon_cell<S, EQ, SRC, MIXED>(d, P, a, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 template <class S, int EQ, int SRC, bool MIXED>
 constexpr auto recon_kernel() {
-  if constexpr (MIXED && S::ND == 2)
-    return &k_reconstruct_2d<S, EQ, SRC, MIXED>;
+  if constexpr (MIXED)
+    return &k_reconstruct_mixed<S, EQ, SRC, MIXED>;
   else
     return &k_reconstruct<S, EQ, SRC, MIXED>;
 }
@@ -1533,8 +1540,9 @@ __global__ void __launch_bounds__(128) km_reconstruct(const BatchInst *__restric
 }
 
 template <class S, int EQ, int SRC, bool MIXED>
-__global__ void __launch_bounds__(128, 5) km_reconstruct_2d(const BatchInst *__restrict__ inst,
-                                                          const Tile *__restrict__ tiles, int n_tiles, int stage) {
+__global__ void __launch_bounds__(128, kMixedReconBlocks<S, EQ>) km_reconstruct_mixed(const BatchInst *__restrict__ inst,
+                                                                                  const Tile *__restrict__ tiles,
+                                                                                  int n_tiles, int stage) {
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const Tile tl = tiles[t];
     const BatchInst &I = inst[tl.slot];
@@ -1544,8 +1552,8 @@ __global__ void __launch_bounds__(128, 5) km_reconstruct_2d(const BatchInst *__r
 
 template <class S, int EQ, int SRC, bool MIXED>
 constexpr auto batch_recon_kernel() {
-  if constexpr (MIXED && S::ND == 2)
-    return &km_reconstruct_2d<S, EQ, SRC, MIXED>;
+  if constexpr (MIXED)
+    return &km_reconstruct_mixed<S, EQ, SRC, MIXED>;
   else
     return &km_reconstruct<S, EQ, SRC, MIXED>;
 }
