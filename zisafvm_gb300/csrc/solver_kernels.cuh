@@ -877,9 +877,12 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   if (SRC && MIXED) {
     // volume part, split into the FP64 cell-average deviation times
     // sum_q w_q grad phi_q and the FP32 polynomial part
-    R acc[NV];
+    // (0, -rho' grad phi, -m . grad phi) with rho', m deviation-sized: FP32
+    R acc[NV], G[ND];
 #pragma unroll
     for (int v = 0; v < NV; ++v) acc[v] = R(0);
+#pragma unroll
+    for (int k = 0; k < ND; ++k) G[k] = R(0);
 #pragma unroll
     for (int qq = 0; qq < S::NQC; ++qq) {
       R X[ND], wg[ND], pv[NV];
@@ -887,6 +890,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       for (int k = 0; k < ND; ++k) {
         X[k] = R(d.xcq32[(qq * ND + k) * ld + i]);
         wg[k] = R(d.wg32[(qq * ND + k) * ld + i]);
+        G[k] += wg[k];
       }
       poly_X(X, pv);
       R mg = R(0);
@@ -899,18 +903,19 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     }
     // the surface part p_eq n_out cancels face by face against the flux
     // baseline and is accounted for in k_face_flux
-    double mg0 = 0.0;
+    R mg0 = R(0);
+    const R d0 = R(dev0[0]);
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
-      const double G = d.gphi_w[k * ld + i];
-      s_acc[1 + k] += -dev0[0] * G + double(acc[1 + k]);
-      mg0 += dev0[1 + k] * G;
+      acc[1 + k] -= d0 * G[k];
+      mg0 += R(dev0[1 + k]) * G[k];
     }
-    s_acc[NV - 1] += -mg0 + double(acc[NV - 1]);
-    if (d.heat_w) s_acc[NV - 1] += heating<S, EQ, MIXED>(d, ev, eqb, found, dev0, poly_X, i);
+    acc[NV - 1] -= mg0;
     const double iv = d.inv_vol[i];
+    const R ivr = R(iv);
+    if (d.heat_w) acc[NV - 1] += R(heating<S, EQ, MIXED>(d, ev, eqb, found, dev0, poly_X, i));
 #pragma unroll
-    for (int v = 0; v < NV; ++v) a.src32[v * ld + i] = float(s_acc[v] * iv);
+    for (int v = 0; v < NV; ++v) a.src32[v * ld + i] = float(acc[v] * ivr);
   } else if (SRC) {
     // volume part: (0, -rho' grad phi, -m . grad phi), rho' = delta (well-balanced)
     // or the full reconstruction (gravity_source_loop.hpp:60-84,121-148)
