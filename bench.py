@@ -745,7 +745,7 @@ def run_serving(args, rank, world, local, pg):
         "latency_ms": {"p50": percentile(lat, 50), "p99": percentile(lat, 99), "mean": float(np.mean(lat)),
                        "queued_p50": percentile(queued, 50), "queued_p99": percentile(queued, 99)},
         "server": {"completed": st["completed"], "failed": st["failed"], "bytes_peak": st["bytes_peak"],
-                   "busy_s": st["busy_s"], "makespan_s": makespan, "rounds": st["rounds"],
+                   "busy_s": st["busy_s"], "setup_s": st["setup_s"], "makespan_s": makespan, "rounds": st["rounds"],
                    "throughput_while_busy": st["cell_stage_updates"] / max(st["busy_s"], 1e-9)},
         "fp64": {"value": st64["cell_stage_updates"] / makespan64,
                  "latency_ms": {"p50": percentile(lat64, 50), "p99": percentile(lat64, 99)},

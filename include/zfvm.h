@@ -276,6 +276,8 @@ typedef struct {
   int64_t cell_stage_updates;  /* work of the completed solves                  */
   int64_t rounds;
   double busy_s;               /* worker time spent stepping running solves      */
+  double setup_s;              /* set-up thread time creating solvers and
+                                  uploading initial states (overlaps busy_s)     */
 } zfvm_server_stats;
 /* Device bytes zfvm_solver_create will allocate for this mesh and scheme. */
 int zfvm_solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc *scheme, int64_t *bytes);

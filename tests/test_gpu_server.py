@@ -131,3 +131,21 @@ def test_failed_request_does_not_disturb_others(zlib):
     st = srv.stats()
     srv.close()
     assert st["failed"] == 1 and st["completed"] == 1
+
+
+def test_close_with_requests_in_every_phase(zlib):
+    """Closing a server whose requests are queued, being set up and running
+    returns and frees their solvers; a new server then runs normally."""
+    reqs = _requests()
+    srv = z.Server(max_slots=2, steps_per_round=1)
+    for mesh, scheme, u0, _, _ in reqs * 2:
+        srv.submit(mesh, scheme, u0, n_steps=10000)
+    time.sleep(0.5)
+    t0 = time.perf_counter()
+    srv.close()
+    assert time.perf_counter() - t0 < 60
+    mesh, scheme, u0, n, t_end = reqs[1]
+    srv = z.Server(max_slots=2, steps_per_round=4)
+    u, t, steps, _ = srv.wait(srv.submit(mesh, scheme, u0, n_steps=n, t_end=t_end), timeout_s=120)
+    srv.close()
+    assert steps == n and np.isfinite(u).all()

@@ -69,7 +69,7 @@ class _ServerDesc(C.Structure):
 class _ServerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "failed", "queued", "running", "bytes_in_use",
                                           "bytes_peak", "budget_bytes", "cell_stage_updates", "rounds")] + \
-               [("busy_s", C.c_double)]
+               [("busy_s", C.c_double), ("setup_s", C.c_double)]
 
 
 class _SchemeDesc(C.Structure):

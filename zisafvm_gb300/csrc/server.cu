@@ -7,12 +7,14 @@
 //      budget and a batch slot is free -- a request that does not fit may be
 //      overtaken by smaller ones behind it, but only kMaxOvertaken times,
 //      after which admission waits for it;
-//   2. creates their solvers, uploads their states and adds them to the batch,
-//      so new requests join the solves already on the device;
+//   2. hands them to a set-up thread, which creates their solvers and uploads
+//      their states while the batch keeps stepping, and adds the solvers that
+//      are ready to the batch, so new requests join the solves on the device;
 //   3. replays `steps_per_round` batched steps (one persistent launch per phase
 //      per RK stage for all running requests of one kernel configuration);
 //   4. retires finished requests: their final state is copied to the host,
-//      their solver is freed and the budget returned, and waiters are woken.
+//      the budget is returned and waiters are woken; the set-up thread frees
+//      the solver.
 // The state of every running request stays on the device between rounds.
 // There is no counterpart in the reference, which runs one solve per process.
 #include <cuda_runtime.h>
@@ -70,18 +72,24 @@ struct zfvm_server {
   zfvm_server_desc desc{};
   int device = 0;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work, cv_done, cv_setup;
   std::map<int64_t, std::unique_ptr<Request>> reqs;
   std::deque<int64_t> queue;
   std::vector<Request *> running;  // worker thread only
+  // set-up thread hand-over (under mu): admitted requests to create, created
+  // ones ready for the batch, retired solvers to free
+  std::deque<Request *> to_create, ready;
+  std::deque<zfvm_solver *> to_destroy;
+  int creating = 0;      // admitted requests not yet ready
+  uint64_t changes = 0;  // bumped by anything that can make admission possible
   int64_t next_id = 1;
-  bool stop = false;
+  bool stop = false, setup_stop = false;
   zfvm_batch *batch = nullptr;
-  std::thread worker;
+  std::thread worker, setup;
   // statistics (under mu)
   int64_t submitted = 0, completed = 0, failed = 0, bytes_in_use = 0, bytes_peak = 0, cell_stages = 0;
   int64_t rounds = 0;
-  double busy_s = 0.0;
+  double busy_s = 0.0, setup_s = 0.0;
   std::string fatal;
 };
 
@@ -100,14 +108,16 @@ void finish(zfvm_server *S, Request *r, int code, const std::string &msg) {
   } else {
     ++S->failed;
   }
+  ++S->changes;
   S->cv_done.notify_all();
+  S->cv_work.notify_all();
 }
 
 // Pick queued requests that fit: arrival order, bounded overtaking.
 std::vector<Request *> pick_admissions(zfvm_server *S) {
   std::vector<Request *> out;
   int64_t free_bytes = S->desc.hbm_budget_bytes - S->bytes_in_use;
-  int free_slots = S->desc.max_slots - (int)S->running.size();
+  int free_slots = S->desc.max_slots - (int)S->running.size() - S->creating;
   std::vector<Request *> skipped;
   for (auto it = S->queue.begin(); it != S->queue.end() && free_slots > 0;) {
     Request *r = S->reqs[*it].get();
@@ -134,20 +144,73 @@ std::vector<Request *> pick_admissions(zfvm_server *S) {
 
 std::string last_error_str() { return std::string(zfvm_last_error()); }
 
-void start_request(zfvm_server *S, Request *r) {
-  zfvm_solver *s = nullptr;
-  int st = zfvm_solver_create(r->mesh, &r->scheme, &s);
-  if (st == ZFVM_OK) st = zfvm_set_state(s, r->state.data(), r->t0);
+std::string stopped_message(const zfvm_server *S) {
+  return S->fatal.empty() ? "server stopped" : "server failed: " + S->fatal;
+}
+
+// Set-up thread: create the solvers of admitted requests, free retired ones.
+void setup_main(zfvm_server *S) {
+  cudaSetDevice(S->device);
+  for (;;) {
+    Request *r = nullptr;
+    zfvm_solver *dead = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cv_setup.wait(lk, [&] { return S->setup_stop || !S->to_create.empty() || !S->to_destroy.empty(); });
+      if (!S->to_destroy.empty()) {
+        dead = S->to_destroy.front();
+        S->to_destroy.pop_front();
+      } else if (!S->to_create.empty()) {
+        r = S->to_create.front();
+        S->to_create.pop_front();
+      } else {
+        break;  // stopping and nothing left
+      }
+    }
+    if (dead) {
+      zfvm_solver_destroy(dead);
+      continue;
+    }
+    const auto t0 = SteadyClock::now();
+    zfvm_solver *s = nullptr;
+    int st = zfvm_solver_create(r->mesh, &r->scheme, &s);
+    if (st == ZFVM_OK) st = zfvm_set_state(s, r->state.data(), r->t0);
+    const std::string msg = st == ZFVM_OK ? std::string() : last_error_str();
+    if (st != ZFVM_OK && s) {
+      zfvm_solver_destroy(s);
+      s = nullptr;
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->setup_s += std::chrono::duration<double>(SteadyClock::now() - t0).count();
+    --S->creating;
+    if (st != ZFVM_OK) {
+      finish(S, r, st, msg);
+    } else if (S->stop) {
+      // the worker has stopped and drained the ready list already
+      S->to_destroy.push_back(s);
+      finish(S, r, ZFVM_EINVAL, stopped_message(S));
+    } else {
+      r->solver = s;
+      S->ready.push_back(r);
+      ++S->changes;
+      S->cv_work.notify_all();
+    }
+  }
+}
+
+// Worker: put a created solver into the batch.
+void add_ready(zfvm_server *S, Request *r) {
   int32_t slot = -1;
-  if (st == ZFVM_OK) st = zfvm_batch_add(S->batch, s, r->n_steps, r->t_end, &slot);
+  const int st = zfvm_batch_add(S->batch, r->solver, r->n_steps, r->t_end, &slot);
   if (st != ZFVM_OK) {
     const std::string msg = last_error_str();
-    if (s) zfvm_solver_destroy(s);
     std::lock_guard<std::mutex> lk(S->mu);
+    S->to_destroy.push_back(r->solver);
+    r->solver = nullptr;
+    S->cv_setup.notify_all();
     finish(S, r, st, msg);
     return;
   }
-  r->solver = s;
   r->slot = slot;
   S->running.push_back(r);
 }
@@ -173,10 +236,11 @@ int retire(zfvm_server *S, bool all) {
     if (code == ZFVM_OK && status != 0) code = status_to_code(status, msg);
     if (code == ZFVM_OK && all && !done) code = ZFVM_EINVAL, msg = "server stopped before the solve finished";
     r->steps_out = steps;
-    zfvm_solver_destroy(r->solver);
-    r->solver = nullptr;
     {
       std::lock_guard<std::mutex> lk(S->mu);
+      S->to_destroy.push_back(r->solver);
+      r->solver = nullptr;
+      S->cv_setup.notify_all();
       finish(S, r, code, msg);
     }
     S->running.erase(S->running.begin() + k);
@@ -187,16 +251,26 @@ int retire(zfvm_server *S, bool all) {
 
 void worker_main(zfvm_server *S) {
   cudaSetDevice(S->device);
+  uint64_t seen = ~uint64_t(0);
   for (;;) {
-    std::vector<Request *> admit;
+    std::vector<Request *> ready;
     {
       std::unique_lock<std::mutex> lk(S->mu);
+      // with nothing on the device, sleep until something can change:
+      // a submission, a released budget or a solver becoming ready
       if (S->running.empty())
-        S->cv_work.wait(lk, [&] { return S->stop || !S->queue.empty(); });
+        S->cv_work.wait(lk, [&] { return S->stop || !S->ready.empty() || S->changes != seen; });
       if (S->stop) break;
-      admit = pick_admissions(S);
+      seen = S->changes;
+      for (Request *r : pick_admissions(S)) {
+        S->to_create.push_back(r);
+        ++S->creating;
+      }
+      if (!S->to_create.empty()) S->cv_setup.notify_all();
+      ready.assign(S->ready.begin(), S->ready.end());
+      S->ready.clear();
     }
-    for (Request *r : admit) start_request(S, r);
+    for (Request *r : ready) add_ready(S, r);
     if (S->running.empty()) continue;
     const auto t0 = SteadyClock::now();
     int32_t n_run = 0;
@@ -218,13 +292,28 @@ void worker_main(zfvm_server *S) {
     ++S->rounds;
   }
   retire(S, true);
+  // S->stop is set: fail what is queued or waiting for the set-up thread; a
+  // solver the set-up thread is still creating is failed when it is done
   std::lock_guard<std::mutex> lk(S->mu);
+  const std::string msg = stopped_message(S);
   for (int64_t id : S->queue) {
     Request *r = S->reqs[id].get();
     r->t_admit = r->t_submit;
-    finish(S, r, ZFVM_EINVAL, S->fatal.empty() ? "server stopped" : "server failed: " + S->fatal);
+    finish(S, r, ZFVM_EINVAL, msg);
   }
   S->queue.clear();
+  for (Request *r : S->to_create) {
+    --S->creating;
+    finish(S, r, ZFVM_EINVAL, msg);
+  }
+  S->to_create.clear();
+  for (Request *r : S->ready) {
+    S->to_destroy.push_back(r->solver);
+    r->solver = nullptr;
+    finish(S, r, ZFVM_EINVAL, msg);
+  }
+  S->ready.clear();
+  S->cv_setup.notify_all();
 }
 
 }  // namespace
@@ -244,8 +333,20 @@ extern "C" int zfvm_server_create(const zfvm_server_desc *desc, zfvm_server **ou
     const int st = zfvm_batch_create(desc->max_slots, &S->batch);
     if (st != ZFVM_OK) return st;
     try {
+      S->setup = std::thread(setup_main, S.get());
+    } catch (const std::system_error &e) {
+      zfvm_batch_destroy(S->batch);
+      return fail(ZFVM_ENOMEM, std::string("cannot start the set-up thread: ") + e.what());
+    }
+    try {
       S->worker = std::thread(worker_main, S.get());
     } catch (const std::system_error &e) {
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->setup_stop = true;
+      }
+      S->cv_setup.notify_all();
+      S->setup.join();
       zfvm_batch_destroy(S->batch);
       return fail(ZFVM_ENOMEM, std::string("cannot start the worker thread: ") + e.what());
     }
@@ -264,6 +365,13 @@ extern "C" int zfvm_server_destroy(zfvm_server *S) {
   }
   S->cv_work.notify_all();
   if (S->worker.joinable()) S->worker.join();
+  // the set-up thread frees the solvers handed to it, then exits
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->setup_stop = true;
+  }
+  S->cv_setup.notify_all();
+  if (S->setup.joinable()) S->setup.join();
   zfvm_batch_destroy(S->batch);
   delete S;
   return ZFVM_OK;
@@ -290,12 +398,13 @@ extern "C" int zfvm_server_submit(zfvm_server *S, zfvm_mesh *mesh, const zfvm_sc
     r->bytes = bytes;
     r->t_submit = SteadyClock::now();
     std::lock_guard<std::mutex> lk(S->mu);
-    if (S->stop) return fail(ZFVM_EINVAL, S->fatal.empty() ? "server stopped" : "server failed: " + S->fatal);
+    if (S->stop) return fail(ZFVM_EINVAL, stopped_message(S));
     r->id = S->next_id++;
     *id = r->id;
     S->queue.push_back(r->id);
     S->reqs[r->id] = std::move(r);
     ++S->submitted;
+    ++S->changes;
   } catch (const std::bad_alloc &) {
     return fail(ZFVM_ENOMEM, "host allocation failed");
   }
@@ -358,5 +467,6 @@ extern "C" int zfvm_server_get_stats(zfvm_server *S, zfvm_server_stats *st) {
   st->cell_stage_updates = S->cell_stages;
   st->rounds = S->rounds;
   st->busy_s = S->busy_s;
+  st->setup_s = S->setup_s;
   return ZFVM_OK;
 }
