@@ -159,6 +159,26 @@ int zfvm_solver_destroy(zfvm_solver *s);
 int zfvm_set_state(zfvm_solver *s, const double *cvars, double t);
 int zfvm_get_state(zfvm_solver *s, double *cvars, double *t);
 
+/* Snapshot files (io/dump_snapshot_impl.hpp:21-38, model/models.cpp:7-27,
+ * model/all_variables.cpp:74-113): datasets "time", "n_steps", "rho", "mv1",
+ * "mv2", "mv3", "E", "n_avars", "mq0".. under the reference's names, in an
+ * uncompressed NumPy .npz file (numpy.load reads it).  cvars is n_cells x 5,
+ * avars n_cells x n_avars, both row-major as in AllVariables.  with_clock = 0
+ * leaves out "time" and "n_steps" (the steady-state file).  The file is
+ * written to "<path>.tmp" and renamed into place; at most 4 GiB. */
+int zfvm_snapshot_write(const char *path, int64_t n_cells, const double *cvars, int32_t n_avars,
+                        const double *avars, int32_t with_clock, double t, int64_t n_steps);
+int zfvm_snapshot_info(const char *path, int64_t *n_cells, int32_t *n_avars, int32_t *has_clock);
+/* n_cells and n_avars must match the file; t and n_steps may be null. */
+int zfvm_snapshot_read(const char *path, int64_t n_cells, double *cvars, int32_t n_avars, double *avars,
+                       double *t, int64_t *n_steps);
+/* DumpSnapshot::do_visualization for a solver: its current state and time,
+ * with the caller's step count. */
+int zfvm_solver_write_snapshot(zfvm_solver *s, const char *path, int64_t n_steps);
+/* Restart (LoadSnapshot::do_load, io/load_snapshot.cpp:9-13): state and time
+ * from the file; the file's step count is returned in *n_steps (may be null). */
+int zfvm_solver_read_snapshot(zfvm_solver *s, const char *path, int64_t *n_steps);
+
 /* One evaluation of the summed rate of change of the current state
  * (SumRatesOfChange::compute, ode/rate_of_change.cpp:21-27); output n_cells x 5.
  * Ghost-cell rows are zero. */

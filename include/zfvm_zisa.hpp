@@ -18,6 +18,7 @@
 #pragma once
 
 #include <array>
+#include <cstdio>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -31,6 +32,8 @@
 #include <zisa/ode/rate_of_change.hpp>
 #include <zisa/ode/time_integration.hpp>
 #include <zisa/reconstruction/global_reconstruction_decl.hpp>
+#include <zisa/io/data_source.hpp>
+#include <zisa/io/visualization.hpp>
 #define ZFVM_HAVE_ZISA 1
 #else
 #define ZFVM_HAVE_ZISA 0
@@ -49,6 +52,13 @@ using TimeIntegrationBase = zisa::TimeIntegration;
 using CFLConditionBase = zisa::CFLCondition;
 inline double *cvars_data(AllVariables &u) { return u.cvars.raw(); }
 inline const double *cvars_data(const AllVariables &u) { return u.cvars.raw(); }
+inline double *avars_data(AllVariables &u) { return u.avars.raw(); }
+inline const double *avars_data(const AllVariables &u) { return u.avars.raw(); }
+inline int64_t n_cells_of(const AllVariables &u) { return int64_t(u.cvars.shape(0)); }
+inline int32_t n_avars_of(const AllVariables &u) { return int32_t(u.avars.shape(1)); }
+using VisualizationBase = zisa::Visualization;
+using DataSourceBase = zisa::DataSource;
+using SimulationClock = zisa::SimulationClock;
 using XYZ = zisa::XYZ;
 using euler_var_t = zisa::euler_var_t;
 using GlobalReconstructionBase = zisa::GlobalReconstruction<zisa::euler_var_t>;
@@ -66,13 +76,44 @@ inline euler_var_t to_cvars(const double *u) {
 inline int64_t view_size(const CellsView &v) { return int64_t(v.shape(0)); }
 inline const int64_t *view_data(const CellsView &v) { return reinterpret_cast<const int64_t *>(v.raw()); }
 #else
-// Stand-in with the reference's layout: cvars is n_cells x 5, row-major.
+// Stand-in with the reference's layout: cvars is n_cells x 5 and avars
+// n_cells x n_avars, both row-major.
 struct AllVariables {
-  std::vector<double> cvars;
-  explicit AllVariables(size_t n_cells = 0) : cvars(n_cells * 5, 0.0) {}
+  std::vector<double> cvars, avars;
+  int32_t n_avars = 0;
+  explicit AllVariables(size_t n_cells = 0, int32_t n_avars_ = 0)
+      : cvars(n_cells * 5, 0.0), avars(n_cells * n_avars_, 0.0), n_avars(n_avars_) {}
 };
 inline double *cvars_data(AllVariables &u) { return u.cvars.data(); }
 inline const double *cvars_data(const AllVariables &u) { return u.cvars.data(); }
+inline double *avars_data(AllVariables &u) { return u.avars.data(); }
+inline const double *avars_data(const AllVariables &u) { return u.avars.data(); }
+inline int64_t n_cells_of(const AllVariables &u) { return int64_t(u.cvars.size() / 5); }
+inline int32_t n_avars_of(const AllVariables &u) { return u.n_avars; }
+// SimulationClock's time and step count, as DumpSnapshot and LoadSnapshot use them.
+struct SimulationClock {
+  double t = 0.0;
+  int64_t n_steps = 0;
+  double current_time() const { return t; }
+  int64_t current_step() const { return n_steps; }
+  void advance_to(double t_, int64_t n_) { t = t_, n_steps = n_; }
+};
+struct VisualizationBase {
+  virtual ~VisualizationBase() = default;
+  void operator()(const AllVariables &u, const SimulationClock &clock) { do_visualization(u, clock); }
+  void steady_state(const AllVariables &u) { do_steady_state(u); }
+
+ protected:
+  virtual void do_visualization(const AllVariables &u, const SimulationClock &clock) = 0;
+  virtual void do_steady_state(const AllVariables &u) = 0;
+};
+struct DataSourceBase {
+  virtual ~DataSourceBase() = default;
+  void operator()(AllVariables &u, SimulationClock &clock) { do_load(u, clock); }
+
+ protected:
+  virtual void do_load(AllVariables &u, SimulationClock &clock) = 0;
+};
 struct RateOfChangeBase {
   virtual ~RateOfChangeBase() = default;
   virtual void compute(AllVariables &tendency, const AllVariables &current_state, double t) const = 0;
@@ -217,6 +258,54 @@ class GpuGlobalReconstruction : public GlobalReconstructionBase {
   std::shared_ptr<DeviceSolver> s_;
   std::vector<int64_t> l2g_;
   std::vector<int64_t> n_l2g_;
+};
+
+// DumpSnapshot (io/dump_snapshot_impl.hpp:21-38) writing .npz snapshot files
+// with the reference's dataset names.  `pattern` is a printf pattern of the
+// generation number, the FileNameGenerator's dir + stem + pattern + suffix
+// (io/file_name_generator.cpp:9-27), e.g. "out/snapshot_%04d.npz".
+class NpzDumpSnapshot : public VisualizationBase {
+ public:
+  NpzDumpSnapshot(std::string pattern, std::string steady_state_name, int first_generation = 0)
+      : pattern_(std::move(pattern)), steady_(std::move(steady_state_name)), count_(first_generation) {}
+  std::string filename(int generation) const {
+    std::vector<char> buf(pattern_.size() + 32);
+    std::snprintf(buf.data(), buf.size(), pattern_.c_str(), generation);
+    return std::string(buf.data());
+  }
+
+ protected:
+  void do_visualization(const AllVariables &u, const SimulationClock &clock) override {
+    write(filename(count_++), u, 1, clock.current_time(), int64_t(clock.current_step()));
+  }
+  void do_steady_state(const AllVariables &u) override { write(steady_, u, 0, 0.0, 0); }
+
+ private:
+  static void write(const std::string &name, const AllVariables &u, int32_t with_clock, double t, int64_t n) {
+    check(zfvm_snapshot_write(name.c_str(), n_cells_of(u), cvars_data(u), n_avars_of(u), avars_data(u), with_clock,
+                              t, n));
+  }
+  std::string pattern_, steady_;
+  int count_;
+};
+
+// LoadSnapshot (io/load_snapshot.cpp:9-13): the state from a snapshot file and
+// the clock advanced to its time and step count.  The AllVariables must have
+// the file's numbers of cells and advected variables.
+class NpzLoadSnapshot : public DataSourceBase {
+ public:
+  explicit NpzLoadSnapshot(std::string file_name) : file_(std::move(file_name)) {}
+
+ protected:
+  void do_load(AllVariables &u, SimulationClock &clock) override {
+    double t = 0.0;
+    int64_t n = 0;
+    check(zfvm_snapshot_read(file_.c_str(), n_cells_of(u), cvars_data(u), n_avars_of(u), avars_data(u), &t, &n));
+    clock.advance_to(t, n);
+  }
+
+ private:
+  std::string file_;
 };
 
 }  // namespace zfvm

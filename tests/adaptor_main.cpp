@@ -1,9 +1,11 @@
 // Drives the solver through the C++ adaptors of include/zfvm_zisa.hpp, the way
 // a ZisaFVM time loop would: LocalCFL, RateOfChange, RungeKutta::compute_step
-// and GlobalReconstruction.  Prints the results for tests/test_adaptors.py.
+// and GlobalReconstruction, then DumpSnapshot / LoadSnapshot.  Prints the
+// results for tests/test_adaptors.py.
 #define ZFVM_STANDALONE 1
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "zfvm_zisa.hpp"
@@ -99,6 +101,19 @@ int main(int argc, char **argv) {
   for (double a : tend.cvars) s_t += a;
   for (double a : u1->cvars) s_u += a;
   std::printf("sums %.17g %.17g\n", s_t, s_u);
+
+  // DumpSnapshot / LoadSnapshot round trip of the stepped state
+  const std::string dir = argc > 2 ? argv[2] : ".";
+  zfvm::NpzDumpSnapshot dump(dir + "/snapshot_%04d.npz", dir + "/steady_state.npz");
+  zfvm::SimulationClock clock;
+  clock.advance_to(dt, 1);
+  dump(*u1, clock);
+  zfvm::NpzLoadSnapshot load(dump.filename(0));
+  zfvm::AllVariables back(nc);
+  zfvm::SimulationClock clock2;
+  load(back, clock2);
+  std::printf("snapshot %d %.17g %lld\n", int(back.cvars == u1->cvars), clock2.current_time(),
+              (long long)clock2.current_step());
   ds.reset();
   zfvm_mesh_destroy(mesh);
   return 0;

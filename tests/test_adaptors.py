@@ -1,6 +1,7 @@
 """The C++ drop-in adaptors (include/zfvm_zisa.hpp: GpuLocalCFL, GpuRateOfChange,
-GpuRungeKutta, GpuGlobalReconstruction) compile against the C ABI, and on a GPU
-give the same numbers as the library's other bindings."""
+GpuRungeKutta, GpuGlobalReconstruction, NpzDumpSnapshot, NpzLoadSnapshot)
+compile against the C ABI, and on a GPU give the same numbers as the
+library's other bindings."""
 import subprocess
 from pathlib import Path
 
@@ -28,7 +29,7 @@ def test_adaptors_compile_and_link(tmp_path, zlib):
 def test_adaptors_match_python_binding(tmp_path, zlib):
     z = zlib
     exe = _build(tmp_path, zlib)
-    r = subprocess.run([str(exe), "10"], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([str(exe), "10", str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     out = {ln.split()[0]: ln.split()[1:] for ln in r.stdout.splitlines()}
     from problems import polytrope_2d
@@ -43,6 +44,11 @@ def test_adaptors_match_python_binding(tmp_path, zlib):
     u1, _ = s.get_state()
     assert float(out["sums"][0]) == pytest.approx(tend.sum(), rel=1e-14, abs=1e-14)
     assert float(out["sums"][1]) == pytest.approx(u1.sum(), rel=1e-14)
+    # the snapshot holds the stepped state and the clock, and reads back equal
+    assert out["snapshot"][0] == "1" and out["snapshot"][2] == "1"
+    assert float(out["snapshot"][1]) == dt
+    snap = z.read_snapshot(tmp_path / "snapshot_0000.npz")
+    assert np.array_equal(snap["cvars"], u1) and snap["n_steps"] == 1
     cell = int(out["cell"][0])
     s.set_state(u0)
     s.reconstruct()

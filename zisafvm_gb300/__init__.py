@@ -13,6 +13,7 @@ code), but every solver call needs the CUDA library and a device, and raises
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 from pathlib import Path
 
@@ -146,6 +147,11 @@ def load_library() -> C.CDLL:
         "zfvm_server_poll": [vp, i64, C.POINTER(i32)],
         "zfvm_server_wait": [vp, i64, C.c_double, dp, dp, C.POINTER(i64), dp],
         "zfvm_server_get_stats": [vp, vp],
+        "zfvm_snapshot_write": [C.c_char_p, i64, dp, i32, dp, i32, C.c_double, i64],
+        "zfvm_snapshot_info": [C.c_char_p, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)],
+        "zfvm_snapshot_read": [C.c_char_p, i64, dp, i32, dp, dp, C.POINTER(i64)],
+        "zfvm_solver_write_snapshot": [vp, C.c_char_p, i64],
+        "zfvm_solver_read_snapshot": [vp, C.c_char_p, C.POINTER(i64)],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -391,6 +397,16 @@ class Solver:
         _check(load_library().zfvm_get_state(self._h, _dp(a), C.byref(t)))
         return a, t.value
 
+    def write_snapshot(self, path, n_steps: int = 0) -> None:
+        """Current state and time to a snapshot file (see `write_snapshot`)."""
+        _check(load_library().zfvm_solver_write_snapshot(self._h, os.fsencode(path), n_steps))
+
+    def read_snapshot(self, path) -> int:
+        """Restart from a snapshot file: state and time; returns its step count."""
+        n = C.c_int64()
+        _check(load_library().zfvm_solver_read_snapshot(self._h, os.fsencode(path), C.byref(n)))
+        return n.value
+
     def rate_of_change(self) -> np.ndarray:
         a = np.zeros((self.mesh.n_cells, 5))
         _check(load_library().zfvm_rate_of_change(self._h, _dp(a)))
@@ -500,6 +516,34 @@ class Batch:
         _check(load_library().zfvm_batch_slot_status(self._h, slot, C.byref(t), C.byref(st), C.byref(done),
                                                      C.byref(status)))
         return {"t": t.value, "steps": st.value, "done": bool(done.value), "status": status.value}
+
+
+def write_snapshot(path, cvars: np.ndarray, t: float | None = None, n_steps: int | None = None,
+                   avars: np.ndarray | None = None) -> None:
+    """Write a snapshot file: the reference's datasets ("time", "n_steps", "rho",
+    "mv1", "mv2", "mv3", "E", "n_avars", "mq<k>") in an uncompressed .npz.
+    Without `t` the file has no clock (the steady-state file)."""
+    u = np.ascontiguousarray(cvars, dtype=np.float64)
+    assert u.ndim == 2 and u.shape[1] == 5
+    q = None if avars is None else np.ascontiguousarray(avars, dtype=np.float64).reshape(u.shape[0], -1)
+    na = 0 if q is None else q.shape[1]
+    _check(load_library().zfvm_snapshot_write(os.fsencode(path), u.shape[0], _dp(u), na,
+                                              None if q is None else _dp(q), int(t is not None),
+                                              0.0 if t is None else float(t), int(n_steps or 0)))
+
+
+def read_snapshot(path) -> dict:
+    """Read a snapshot file: {"cvars", "avars", "time", "n_steps"} (the clock
+    entries are None in a steady-state file)."""
+    lib = load_library()
+    n, na, hc = C.c_int64(), C.c_int32(), C.c_int32()
+    _check(lib.zfvm_snapshot_info(os.fsencode(path), C.byref(n), C.byref(na), C.byref(hc)))
+    u = np.zeros((n.value, 5))
+    q = np.zeros((n.value, na.value))
+    t, st = C.c_double(), C.c_int64()
+    _check(lib.zfvm_snapshot_read(os.fsencode(path), n.value, _dp(u), na.value, _dp(q) if na.value else None,
+                                  C.byref(t) if hc.value else None, C.byref(st) if hc.value else None))
+    return {"cvars": u, "avars": q, "time": t.value if hc.value else None, "n_steps": st.value if hc.value else None}
 
 
 def solver_footprint(mesh: "Mesh", scheme: "Scheme") -> int:

@@ -27,7 +27,7 @@ CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno
 NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
              "--expt-relaxed-constexpr"]
 
-HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp"]
+HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp", "snapshot.cpp"]
 CUDA_SOURCES = ["solver.cu", "batch.cu", "server.cu", "noalloc.cu", "inst_s2o3.cu", "inst_s2o2.cu", "inst_s3o3.cu", "inst_s3o2.cu"]
 
 

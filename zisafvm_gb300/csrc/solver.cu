@@ -750,6 +750,45 @@ extern "C" int zfvm_get_state(zfvm_solver *s, double *cvars, double *t) {
   SOLVER_GUARD_END
 }
 
+extern "C" int zfvm_solver_write_snapshot(zfvm_solver *s, const char *path, int64_t n_steps) {
+  if (!s || !path) return fail(ZFVM_EINVAL, "null argument");
+  std::vector<double> u;
+  try {
+    u.resize((size_t)s->n_cells * 5);
+  } catch (const std::bad_alloc &) {
+    return fail(ZFVM_ENOMEM, "host allocation failed");
+  }
+  double t = 0.0;
+  int st = zfvm_get_state(s, u.data(), &t);
+  if (st != ZFVM_OK) return st;
+  return zfvm_snapshot_write(path, s->n_cells, u.data(), 0, nullptr, 1, t, n_steps);
+}
+
+extern "C" int zfvm_solver_read_snapshot(zfvm_solver *s, const char *path, int64_t *n_steps) {
+  if (!s || !path) return fail(ZFVM_EINVAL, "null argument");
+  int64_t n = 0;
+  int32_t na = 0, has_clock = 0;
+  int st = zfvm_snapshot_info(path, &n, &na, &has_clock);
+  if (st != ZFVM_OK) return st;
+  if (n != s->n_cells)
+    return fail(ZFVM_EINVAL, std::string(path) + " holds " + std::to_string(n) + " cells, the solver's mesh " +
+                                 std::to_string(s->n_cells));
+  if (!has_clock) return fail(ZFVM_EINVAL, std::string(path) + " has no \"time\" and \"n_steps\" (a steady state?)");
+  std::vector<double> u;
+  try {
+    u.resize((size_t)n * 5);
+  } catch (const std::bad_alloc &) {
+    return fail(ZFVM_ENOMEM, "host allocation failed");
+  }
+  double t = 0.0;
+  int64_t steps = 0;
+  st = zfvm_snapshot_read(path, n, u.data(), 0, nullptr, &t, &steps);
+  if (st != ZFVM_OK) return st;
+  st = zfvm_set_state(s, u.data(), t);
+  if (st == ZFVM_OK && n_steps) *n_steps = steps;
+  return st;
+}
+
 extern "C" int zfvm_rate_of_change(zfvm_solver *s, double *tendency) {
   if (!s || !tendency) return fail(ZFVM_EINVAL, "null argument");
   SOLVER_GUARD_BEGIN
