@@ -150,7 +150,10 @@ typedef struct {
   int32_t step_rejection_max_exponent; /* smallest step factor 2^-max_exponent       */
   double heating_rate;          /* heating.rate (model/heating.hpp:52-77); 0: none   */
   double heating_r0, heating_r1; /* heating.lower_boundary / upper_boundary           */
+  int32_t n_avars;              /* advected variables (AllVariables::avars columns,
+                                   choose_n_avars); 0..ZFVM_MAX_AVARS                */
 } zfvm_scheme_desc;
+#define ZFVM_MAX_AVARS 64
 
 int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *scheme, zfvm_solver **out);
 int zfvm_solver_destroy(zfvm_solver *s);
@@ -158,6 +161,14 @@ int zfvm_solver_destroy(zfvm_solver *s);
 /* Upload / download the state (n_cells x 5 AoS host doubles) and the time. */
 int zfvm_set_state(zfvm_solver *s, const double *cvars, double t);
 int zfvm_get_state(zfvm_solver *s, double *cvars, double *t);
+/* Upload / download the advected variables (AllVariables::avars: mass-weighted
+ * tracers mq, n_cells x n_avars row-major).  A solver with n_avars > 0 starts
+ * with them zero.  They are reconstructed like the conserved variables but each
+ * on its own (LocalReconstruction::compute_tracer, local_reconstruction.hpp:
+ * 127-147) and transported with the numerical flux's wave speeds
+ * (HLLCBatten::tracer_flux, flux/hllc.hpp:178-197), always in FP64. */
+int zfvm_set_avars(zfvm_solver *s, const double *avars);
+int zfvm_get_avars(zfvm_solver *s, double *avars);
 
 /* Snapshot files (io/dump_snapshot_impl.hpp:21-38, model/models.cpp:7-27,
  * model/all_variables.cpp:74-113): datasets "time", "n_steps", "rho", "mv1",
@@ -178,6 +189,10 @@ int zfvm_solver_write_snapshot(zfvm_solver *s, const char *path, int64_t n_steps
 /* Restart (LoadSnapshot::do_load, io/load_snapshot.cpp:9-13): state and time
  * from the file; the file's step count is returned in *n_steps (may be null). */
 int zfvm_solver_read_snapshot(zfvm_solver *s, const char *path, int64_t *n_steps);
+
+/* The rate of change of the conserved and the advected variables
+ * (n_cells x 5 and n_cells x n_avars); ghost-cell rows are zero. */
+int zfvm_rate_of_change_all(zfvm_solver *s, double *tendency, double *avars_tendency);
 
 /* One evaluation of the summed rate of change of the current state
  * (SumRatesOfChange::compute, ode/rate_of_change.cpp:21-27); output n_cells x 5.

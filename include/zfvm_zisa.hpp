@@ -152,7 +152,7 @@ struct GlobalReconstructionBase {
 // Shared device solver (one mesh + scheme); the adaptors below hold it.
 class DeviceSolver {
  public:
-  DeviceSolver(zfvm_mesh *mesh, const zfvm_scheme_desc &scheme) : mesh_(mesh) {
+  DeviceSolver(zfvm_mesh *mesh, const zfvm_scheme_desc &scheme) : mesh_(mesh), n_avars_(scheme.n_avars) {
     check(zfvm_solver_create(mesh, &scheme, &s_));
   }
   ~DeviceSolver() { zfvm_solver_destroy(s_); }
@@ -160,10 +160,24 @@ class DeviceSolver {
   DeviceSolver &operator=(const DeviceSolver &) = delete;
   zfvm_solver *get() const { return s_; }
   zfvm_mesh *mesh() const { return mesh_; }
+  int32_t n_avars() const { return n_avars_; }
+  // upload / download a whole AllVariables (cvars, and avars when the scheme has them)
+  void set(const AllVariables &u, double t) const {
+    if (n_avars_of(u) != n_avars_) throw std::runtime_error("zfvm: AllVariables has the wrong number of avars");
+    check(zfvm_set_state(s_, cvars_data(u), t));
+    if (n_avars_) check(zfvm_set_avars(s_, avars_data(u)));
+  }
+  double get_into(AllVariables &u) const {
+    double t;
+    check(zfvm_get_state(s_, cvars_data(u), &t));
+    if (n_avars_) check(zfvm_get_avars(s_, avars_data(u)));
+    return t;
+  }
 
  private:
   zfvm_mesh *mesh_ = nullptr;
   zfvm_solver *s_ = nullptr;
+  int32_t n_avars_ = 0;
 };
 
 // SumRatesOfChange{Zero, FluxLoop, GravitySource, FluxBC} of the configured scheme.
@@ -171,8 +185,8 @@ class GpuRateOfChange : public RateOfChangeBase {
  public:
   explicit GpuRateOfChange(std::shared_ptr<DeviceSolver> s) : s_(std::move(s)) {}
   void compute(AllVariables &tendency, const AllVariables &current_state, double t) const override {
-    check(zfvm_set_state(s_->get(), cvars_data(current_state), t));
-    check(zfvm_rate_of_change(s_->get(), cvars_data(tendency)));
+    s_->set(current_state, t);
+    check(zfvm_rate_of_change_all(s_->get(), cvars_data(tendency), avars_data(tendency)));
   }
   std::string str() const override { return "GB300 rate of change (`GpuRateOfChange`)"; }
 
@@ -188,10 +202,9 @@ class GpuRungeKutta : public TimeIntegrationBase {
                                              double dt) override {
     // the reference keeps u0 for reuse and returns its other buffer
     if (!ux_ || ux_ == u0) ux_ = std::make_shared<AllVariables>(*u0);
-    check(zfvm_set_state(s_->get(), cvars_data(*u0), t));
+    s_->set(*u0, t);
     check(zfvm_step(s_->get(), dt));
-    double t_new;
-    check(zfvm_get_state(s_->get(), cvars_data(*ux_), &t_new));
+    s_->get_into(*ux_);
     auto out = ux_;
     ux_ = u0;
     return out;

@@ -34,6 +34,10 @@ def lib() -> C.CDLL:
         L.zfvm_oracle_reconstruct_eval.argtypes = [vp, dp, C.c_int64, C.c_void_p, dp, dp]
         L.zfvm_oracle_step.argtypes = [vp, dp, C.c_double]
         L.zfvm_oracle_run.argtypes = [vp, dp, C.c_int64, C.c_double, dp, C.POINTER(C.c_int64)]
+        L.zfvm_oracle_rate_of_change_av.argtypes = [vp, dp, dp, dp, dp]
+        L.zfvm_oracle_step_av.argtypes = [vp, dp, dp, C.c_double]
+        L.zfvm_oracle_run_av.argtypes = [vp, dp, dp, C.c_int64, C.c_double, dp, C.POINTER(C.c_int64)]
+        L.zfvm_oracle_tracer_flux.argtypes = [C.c_int, C.c_double, dp, dp, C.c_double, C.c_double, dp]
         L.zfvm_oracle_flux.argtypes = [C.c_int, C.c_double, dp, dp, dp]
         L.zfvm_oracle_euler_flux.argtypes = [C.c_double, dp, dp]
         L.zfvm_oracle_poly_eval.argtypes = [C.c_int, C.c_int, dp, dp, dp, C.c_double, dp, dp]
@@ -104,11 +108,18 @@ class Oracle:
                     _check(lib().zfvm_oracle_set_pinv(self._h, i, k, _dp(P), P.shape[1], P.shape[0]))
         lib().zfvm_oracle_set_lsq_mode(self._h, 1)
 
-    def rate_of_change(self, state: np.ndarray) -> np.ndarray:
+    def rate_of_change(self, state: np.ndarray, avars: np.ndarray | None = None):
+        """Tendency of the state; with advected variables (n x na) also theirs:
+        (tendency, avars tendency)."""
         u = np.ascontiguousarray(state, dtype=np.float64)
         out = np.zeros_like(u)
-        _check(lib().zfvm_oracle_rate_of_change(self._h, _dp(u), _dp(out)))
-        return out
+        if avars is None:
+            _check(lib().zfvm_oracle_rate_of_change(self._h, _dp(u), _dp(out)))
+            return out
+        q = np.ascontiguousarray(avars, dtype=np.float64)
+        qout = np.zeros_like(q)
+        _check(lib().zfvm_oracle_rate_of_change_av(self._h, _dp(u), _dp(q), _dp(out), _dp(qout)))
+        return out, qout
 
     def reconstruct_eval(self, state: np.ndarray, cells, x) -> np.ndarray:
         """Reconstruction of cells[k] at x[k] (n x 3): n x 5 rows."""
@@ -125,23 +136,42 @@ class Oracle:
         _check(lib().zfvm_oracle_cfl_dt(self._h, _dp(u), C.byref(dt)))
         return dt.value
 
-    def step(self, state: np.ndarray, dt: float) -> np.ndarray:
+    def step(self, state: np.ndarray, dt: float, avars: np.ndarray | None = None):
         u = np.array(state, dtype=np.float64, copy=True)
-        _check(lib().zfvm_oracle_step(self._h, _dp(u), dt))
-        return u
+        if avars is None:
+            _check(lib().zfvm_oracle_step(self._h, _dp(u), dt))
+            return u
+        q = np.array(avars, dtype=np.float64, copy=True)
+        _check(lib().zfvm_oracle_step_av(self._h, _dp(u), _dp(q), dt))
+        return u, q
 
-    def run(self, state: np.ndarray, n_steps: int = 0, t_end: float = 0.0, t0: float = 0.0):
+    def run(self, state: np.ndarray, n_steps: int = 0, t_end: float = 0.0, t0: float = 0.0,
+            avars: np.ndarray | None = None):
+        """(state, t, steps), or (state, avars, t, steps) with advected variables."""
         u = np.array(state, dtype=np.float64, copy=True)
         t = C.c_double(t0)
         s = C.c_int64()
-        _check(lib().zfvm_oracle_run(self._h, _dp(u), n_steps, t_end, C.byref(t), C.byref(s)))
-        return u, t.value, s.value
+        if avars is None:
+            _check(lib().zfvm_oracle_run(self._h, _dp(u), n_steps, t_end, C.byref(t), C.byref(s)))
+            return u, t.value, s.value
+        q = np.array(avars, dtype=np.float64, copy=True)
+        _check(lib().zfvm_oracle_run_av(self._h, _dp(u), _dp(q), n_steps, t_end, C.byref(t), C.byref(s)))
+        return u, q, t.value, s.value
 
 
 def flux(kind: int, gamma: float, uL, uR) -> np.ndarray:
     a, b, f = np.asarray(uL, float), np.asarray(uR, float), np.zeros(5)
     lib().zfvm_oracle_flux(kind, gamma, _dp(a), _dp(b), _dp(f))
     return f
+
+
+def tracer_flux(kind: int, gamma: float, uL, uR, qL: float, qR: float) -> float:
+    """Flux of an advected variable between face-frame states uL, uR."""
+    a = np.ascontiguousarray(uL, dtype=np.float64)
+    b = np.ascontiguousarray(uR, dtype=np.float64)
+    f = C.c_double()
+    _check(lib().zfvm_oracle_tracer_flux(kind, gamma, _dp(a), _dp(b), qL, qR, C.byref(f)))
+    return f.value
 
 
 def euler_flux(gamma: float, u) -> np.ndarray:

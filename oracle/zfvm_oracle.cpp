@@ -344,8 +344,9 @@ static Cv euler_flux(const Cv &u, double p) {
   return {u[1], v * u[1] + p, v * u[2], v * u[3], v * (u[4] + p)};
 }
 
-// HLLCBatten<IdealGasEOS>::flux (flux/hllc.hpp:35-176)
-static Cv hllc(const EOS &eos, const Cv &uL, const Cv &uR) {
+// HLLCBatten<IdealGasEOS>::flux (flux/hllc.hpp:35-176); the wave speeds
+// (s_L, s*, s_R) it returns beside the flux go to speeds when given.
+static Cv hllc(const EOS &eos, const Cv &uL, const Cv &uR, double *speeds = nullptr) {
   auto xL = eos.xvars(uL), xR = eos.xvars(uR);
   double ratio = std::sqrt(uR[0] / uL[0]);
   auto roe = [&](double a, double b) { return (a + b * ratio) / (1.0 + ratio); };
@@ -361,6 +362,7 @@ static Cv hllc(const EOS &eos, const Cv &uL, const Cv &uR) {
   double sL = std::min(vL - aL, v_t - a_t);
   double sR = std::max(vR + aR, v_t + a_t);
   double s_star = (uR[1] * (sR - vR) - uL[1] * (sL - vL) + pL - pR) / (uR[0] * (sR - vR) - uL[0] * (sL - vL));
+  if (speeds) speeds[0] = sL, speeds[1] = s_star, speeds[2] = sR;
   const Cv &uK = 0.0 <= s_star ? uL : uR;
   double pK = 0.0 <= s_star ? pL : pR;
   Cv nf = euler_flux(uK, pK);
@@ -377,15 +379,40 @@ static Cv hllc(const EOS &eos, const Cv &uL, const Cv &uR) {
   return nf;
 }
 
-// Rusanov flux: a new flux with HLLCBatten's call signature.
-static Cv rusanov(const EOS &eos, const Cv &uL, const Cv &uR) {
+// Rusanov flux: a new flux with HLLCBatten's call signature; its one speed
+// s_max goes to speeds[0] when given.
+static Cv rusanov(const EOS &eos, const Cv &uL, const Cv &uR, double *speeds = nullptr) {
   auto xL = eos.xvars(uL), xR = eos.xvars(uR);
   double vL = uL[1] / uL[0], vR = uR[1] / uR[0];
   double smax = std::max(std::fabs(vL) + xL[1], std::fabs(vR) + xR[1]);
+  if (speeds) speeds[0] = smax;
   Cv fL = euler_flux(uL, xL[0]), fR = euler_flux(uR, xR[0]);
   Cv nf;
   for (int k = 0; k < 5; ++k) nf[k] = 0.5 * (fL[k] + fR[k]) - 0.5 * smax * (uR[k] - uL[k]);
   return nf;
+}
+
+// HLLCBatten::tracer_flux (flux/hllc.hpp:178-197): the flux of an advected
+// variable mq (a mass-weighted tracer) through the face, upwinded on s*, with
+// the HLLC star-state correction when the fan straddles the face.  uL, uR are
+// in the face frame.
+static double tracer_flux_hllc(const Cv &uL, const Cv &uR, double mqL, double mqR, const double *speeds) {
+  const double sL = speeds[0], s_star = speeds[1], sR = speeds[2];
+  const double mqK = 0.0 <= s_star ? mqL : mqR;
+  const double vK = 0.0 <= s_star ? uL[1] / uL[0] : uR[1] / uR[0];
+  const double fK = mqK * vK;
+  if (sL < 0.0 && 0.0 < sR) {
+    const double sK = 0.0 <= s_star ? sL : sR;
+    const double cK = (sK - vK) / (sK - s_star);
+    return fK + sK * (cK * mqK - mqK);
+  }
+  return fK;
+}
+
+// The Rusanov flux of an advected variable (no counterpart in the reference,
+// which has no Rusanov flux): (mqL vL + mqR vR) / 2 - s_max (mqR - mqL) / 2.
+static double tracer_flux_rusanov(const Cv &uL, const Cv &uR, double mqL, double mqR, const double *speeds) {
+  return 0.5 * (mqL * (uL[1] / uL[0]) + mqR * (uR[1] / uR[0])) - 0.5 * speeds[0] * (mqR - mqL);
 }
 
 // coord_transform / inv_coord_transform (model/euler_variables.cpp:29-67)
@@ -865,6 +892,7 @@ struct Scheme {
   double reject_drho = 0.0;  // RejectLargeDensityChange drho_crit_rel (0: RejectNothing)
   int reject_max_exponent = 0;
   double heat_rate = 0.0, heat_r0 = 0.0, heat_r1 = 0.0;  // heating.{rate, lower_boundary, upper_boundary}
+  int na = 0;  // advected variables (AllVariables::avars columns)
 };
 
 struct CellRC {
@@ -882,6 +910,7 @@ struct CellRC {
   std::vector<std::pair<RhoE, std::array<double, 2>>> pv_cell;  // cell quadrature points
   std::vector<std::vector<std::pair<RhoE, std::array<double, 2>>>> pv_face;  // per local face, qp
   Poly poly;
+  std::vector<Poly> tpoly;  // scalar polynomials of the advected variables (variable 0 used)
   idx steps_since = 0;
 };
 
@@ -935,6 +964,8 @@ static int compute_equilibrium(Problem &pr, idx i, const std::vector<Cv> &ul) {
   return 0;
 }
 
+static Poly hybrid_poly(const Problem &pr, idx i, const std::vector<Cv> &ul);
+
 // LocalReconstruction::compute + CWENO_AO::reconstruct_impl + HybridWENO
 static int local_reconstruct(Problem &pr, idx i, std::vector<Cv> &ul) {
   auto &rc = pr.rc[i];
@@ -955,6 +986,17 @@ static int local_reconstruct(Problem &pr, idx i, std::vector<Cv> &ul) {
     ul[il][4] -= rc.rhoEbar[il][1];
     ul[il] = cv_div(ul[il], rc.scale);
   }
+  rc.poly = hybrid_poly(pr, i, ul);
+  ++rc.steps_since;
+  return 0;
+}
+
+// HybridWENO::compute_polys + CWENO_AO::reconstruct_impl / WENO_AO::reconstruct
+// + eno_hybridize of the stencil values ul (local stencil order), for a
+// WENOPoly (five variables) or a ScalarPoly (variable 0, the others zero).
+static Poly hybrid_poly(const Problem &pr, idx i, const std::vector<Cv> &ul) {
+  const auto &rc = pr.rc[i];
+  const auto &g = pr.g;
   // compute_polys (hybrid_weno.cpp:255-276)
   std::vector<Poly> polys(rc.ns);
   const XYZ &xc = g.centers[i];
@@ -1015,9 +1057,22 @@ static int local_reconstruct(Problem &pr, idx i, std::vector<Cv> &ul) {
   }
   Poly p(0, {0.0}, XYZ{}, 1.0, 2);
   for (int k = 0; k < rc.ns; ++k) poly_axpy(p, nlw[k] / al_tot, polys[k], 1.0);
-  rc.poly = p;
-  ++rc.steps_since;
-  return 0;
+  return p;
+}
+
+// LocalReconstruction::compute_tracer (local_reconstruction.hpp:127-147) with
+// EulerGlobalReconstruction::set_tracer_local (global_reconstruction_impl.hpp:
+// 178-192): every advected variable is reconstructed on its own, from its raw
+// cell averages, without equilibrium or scaling.
+static void tracer_reconstruct(Problem &pr, idx i, const std::vector<double> &aq) {
+  auto &rc = pr.rc[i];
+  const int na = pr.s.na;
+  rc.tpoly.resize(na);
+  std::vector<Cv> ul(rc.l2g.size());
+  for (int t = 0; t < na; ++t) {
+    for (size_t l = 0; l < rc.l2g.size(); ++l) ul[l] = Cv{aq[(size_t)rc.l2g[l] * na + t], 0.0, 0.0, 0.0, 0.0};
+    rc.tpoly[t] = hybrid_poly(pr, i, ul);
+  }
 }
 
 // LocalReconstruction::operator()(x) at cached point values
@@ -1064,9 +1119,11 @@ static int local_face_of(const Grid &g, idx i, idx e) {
   return -1;
 }
 
-// EulerGlobalReconstruction::compute + FluxLoop::compute_patch
+// EulerGlobalReconstruction::compute + FluxLoop::compute_patch; aq / atend are
+// the advected variables and their tendency, n_cells x na row-major.
 static int compute_patch(Problem &pr, std::vector<Cv> &tend, const std::vector<Cv> &state, const std::vector<idx> &cells,
-                         const std::vector<idx> &faces) {
+                         const std::vector<idx> &faces, const std::vector<double> &aq, std::vector<double> &atend) {
+  const int na = pr.s.na;
   const auto &g = pr.g;
   int err = 0;
   const idx nc = (idx)cells.size();
@@ -1081,6 +1138,7 @@ static int compute_patch(Problem &pr, std::vector<Cv> &tend, const std::vector<C
 #pragma omp critical
       err = st;
     }
+    if (na) tracer_reconstruct(pr, i, aq);
   }
   if (err) return err;
   const idx nf = (idx)faces.size();
@@ -1091,6 +1149,7 @@ static int compute_patch(Problem &pr, std::vector<Cv> &tend, const std::vector<C
     idx iL = g.lr[e].first, iR = g.lr[e].second;
     int kL = local_face_of(g, iL, e), kR = local_face_of(g, iR, e);
     Cv nf{0, 0, 0, 0, 0};
+    std::vector<double> qnf(na, 0.0);
     for (size_t q = 0; q < face.w.size(); ++q) {
       double w = face.w[q];
       const XYZ &x = face.x[q];
@@ -1098,8 +1157,23 @@ static int compute_patch(Problem &pr, std::vector<Cv> &tend, const std::vector<C
       Cv uR = rc_value(pr.rc[iR], x, pr.rc[iR].pv_face[kR][q]);
       coord_transform(uL, g.fn[e], g.ft1[e], g.ft2[e]);
       coord_transform(uR, g.fn[e], g.ft1[e], g.ft2[e]);
-      Cv f = pr.s.flux == 0 ? hllc(pr.s.eos, uL, uR) : rusanov(pr.s.eos, uL, uR);
+      double speeds[3] = {0.0, 0.0, 0.0};
+      Cv f = pr.s.flux == 0 ? hllc(pr.s.eos, uL, uR, speeds) : rusanov(pr.s.eos, uL, uR, speeds);
       for (int k = 0; k < 5; ++k) nf[k] += w * f[k];
+      // the advected variables (flux_loop.hpp:157-161)
+      for (int t = 0; t < na; ++t) {
+        const double qL = pr.rc[iL].tpoly[t].eval(x)[0], qR = pr.rc[iR].tpoly[t].eval(x)[0];
+        qnf[t] += w * (pr.s.flux == 0 ? tracer_flux_hllc(uL, uR, qL, qR, speeds)
+                                      : tracer_flux_rusanov(uL, uR, qL, qR, speeds));
+      }
+    }
+    for (int t = 0; t < na; ++t) {
+      const double qfL = qnf[t] / g.volumes[iL];
+#pragma omp atomic
+      atend[(size_t)iL * na + t] -= qfL;
+      const double qfR = qnf[t] / g.volumes[iR];
+#pragma omp atomic
+      atend[(size_t)iR * na + t] += qfR;
     }
     inv_coord_transform(nf, g.fn[e], g.ft1[e], g.ft2[e]);
     for (int k = 0; k < 5; ++k) {
@@ -1232,11 +1306,13 @@ static void heating_source(Problem &pr, std::vector<Cv> &tend) {
   }
 }
 
-static int rate_of_change(Problem &pr, std::vector<Cv> &tend, const std::vector<Cv> &state) {
+static int rate_of_change(Problem &pr, std::vector<Cv> &tend, const std::vector<Cv> &state,
+                          const std::vector<double> &aq, std::vector<double> &atend) {
   for (auto &t : tend) t = Cv{0, 0, 0, 0, 0};
-  int st = compute_patch(pr, tend, state, pr.interior_cells, pr.interior_faces);
+  atend.assign(aq.size(), 0.0);  // ZeroRateOfChange (ode/rate_of_change.cpp:49-54)
+  int st = compute_patch(pr, tend, state, pr.interior_cells, pr.interior_faces, aq, atend);
   if (st) return st;
-  st = compute_patch(pr, tend, state, pr.exterior_cells, pr.exterior_faces);
+  st = compute_patch(pr, tend, state, pr.exterior_cells, pr.exterior_faces, aq, atend);
   if (st) return st;
   gravity_source(pr, tend);
   heating_source(pr, tend);
@@ -1247,14 +1323,22 @@ static int rate_of_change(Problem &pr, std::vector<Cv> &tend, const std::vector<
 // FrozenBC::apply (boundary/frozen_boundary_condition.cpp:39-55) writes back the
 // values the ghost cells had when the step started, which are the values they
 // were set to (boundary 2).
-static void apply_bc(Problem &pr, std::vector<Cv> &u, const std::vector<Cv> &u_step) {
+static void apply_bc(Problem &pr, std::vector<Cv> &u, const std::vector<Cv> &u_step, std::vector<double> &aq,
+                     const std::vector<double> &aq_step) {
   const auto &g = pr.g;
+  const int na = pr.s.na;
   if (pr.s.boundary == 1) {
     for (idx i = 0; i < g.n_cells; ++i)
-      if (g.ghost[i]) u[i] = u[g.source[i]];
+      if (g.ghost[i]) {
+        u[i] = u[g.source[i]];
+        for (int t = 0; t < na; ++t) aq[(size_t)i * na + t] = aq[(size_t)g.source[i] * na + t];
+      }
   } else if (pr.s.boundary == 2) {
     for (idx i = 0; i < g.n_cells; ++i)
-      if (g.ghost[i]) u[i] = u_step[i];
+      if (g.ghost[i]) {
+        u[i] = u_step[i];
+        for (int t = 0; t < na; ++t) aq[(size_t)i * na + t] = aq_step[(size_t)i * na + t];
+      }
   }
 }
 
@@ -1273,7 +1357,7 @@ static double cfl_dt(Problem &pr, const std::vector<Cv> &u) {
 }
 
 // RungeKutta::compute_step (ode/runge_kutta.cpp:146-202)
-static int rk_step(Problem &pr, std::vector<Cv> &u0, double dt) {
+static int rk_step(Problem &pr, std::vector<Cv> &u0, std::vector<double> &q0, double dt) {
   const int S = pr.s.stages;
   double a[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, b[3] = {0, 0, 0};
   if (S == 1) {
@@ -1287,8 +1371,12 @@ static int rk_step(Problem &pr, std::vector<Cv> &u0, double dt) {
     b[0] = 1.0 / 6, b[1] = 1.0 / 6, b[2] = 2.0 / 3;
   }
   const idx n = (idx)u0.size();
+  const size_t nq = q0.size();
   std::vector<std::vector<Cv>> k(S, std::vector<Cv>(n));
+  std::vector<std::vector<double>> kq(S, std::vector<double>(nq));
   std::vector<Cv> ux(n);
+  std::vector<double> qx(nq);
+  // runge_kutta_sum over all of AllVariables (ode/runge_kutta.cpp:181-202)
   auto rk_sum = [&](const double *coef) {
 #pragma omp parallel for schedule(static, 8) num_threads(pr.threads)
     for (idx i = 0; i < n; ++i)
@@ -1298,18 +1386,25 @@ static int rk_step(Problem &pr, std::vector<Cv> &u0, double dt) {
           if (coef[s] != 0.0) dudt += coef[s] * k[s][i][v];
         ux[i][v] = u0[i][v] + dt * dudt;
       }
+    for (size_t j = 0; j < nq; ++j) {
+      double dqdt = 0.0;
+      for (int s = 0; s < S; ++s)
+        if (coef[s] != 0.0) dqdt += coef[s] * kq[s][j];
+      qx[j] = q0[j] + dt * dqdt;
+    }
   };
-  int st = rate_of_change(pr, k[0], u0);
+  int st = rate_of_change(pr, k[0], u0, q0, kq[0]);
   if (st) return st;
   for (int s = 1; s < S; ++s) {
     rk_sum(a[s]);
-    apply_bc(pr, ux, u0);
-    st = rate_of_change(pr, k[s], ux);
+    apply_bc(pr, ux, u0, qx, q0);
+    st = rate_of_change(pr, k[s], ux, qx, kq[s]);
     if (st) return st;
   }
   rk_sum(b);
-  apply_bc(pr, ux, u0);
+  apply_bc(pr, ux, u0, qx, q0);
   u0.swap(ux);
+  q0.swap(qx);
   return 0;
 }
 
@@ -1391,6 +1486,8 @@ int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, i
     s.heat_rate = scheme[22];
     s.heat_r0 = scheme[23];
     s.heat_r1 = scheme[24];
+    s.na = (int)scheme[25];
+    if (s.na < 0) throw Error{7, "negative number of advected variables"};
     pr.rc.resize(n_cells);
     for (idx i = 0; i < n_cells; ++i) {
       CellRC &rc = pr.rc[i];
@@ -1484,19 +1581,44 @@ static void store(const std::vector<Cv> &u, double *aos) {
     for (int k = 0; k < 5; ++k) aos[i * 5 + k] = u[i][k];
 }
 
-int zfvm_oracle_rate_of_change(zfvm_oracle *o, const double *state, double *tendency) {
+// Advected variables of a call: n_cells x na row-major, zero when the caller
+// passes none (only allowed with na = 0).
+static bool load_avars(const Problem &pr, const double *avars, std::vector<double> &q) {
+  q.assign((size_t)pr.g.n_cells * pr.s.na, 0.0);
+  if (pr.s.na == 0) return true;
+  if (!avars) {
+    g_oracle_err = "the scheme has advected variables: pass them";
+    return false;
+  }
+  std::copy(avars, avars + q.size(), q.begin());
+  return true;
+}
+
+int zfvm_oracle_rate_of_change_av(zfvm_oracle *o, const double *state, const double *avars, double *tendency,
+                                  double *atend) {
   auto u = load(state, o->pr.g.n_cells);
-  apply_bc(o->pr, u, u);
+  std::vector<double> q, tq;
+  if (!load_avars(o->pr, avars, q)) return 1;
+  apply_bc(o->pr, u, u, q, q);
   std::vector<Cv> t(u.size());
-  int st = rate_of_change(o->pr, t, u);
+  int st = rate_of_change(o->pr, t, u, q, tq);
   if (st) {
     g_oracle_err = st == 4 ? "equilibrium solve is not converging" : "non-physical state";
     return st;
   }
+  const int na = o->pr.s.na;
   for (idx i = 0; i < o->pr.g.n_cells; ++i)
-    if (o->pr.g.ghost[i]) t[i] = Cv{0, 0, 0, 0, 0};
+    if (o->pr.g.ghost[i]) {
+      t[i] = Cv{0, 0, 0, 0, 0};
+      for (int k = 0; k < na; ++k) tq[(size_t)i * na + k] = 0.0;
+    }
   store(t, tendency);
+  if (na && atend) std::copy(tq.begin(), tq.end(), atend);
   return 0;
+}
+
+int zfvm_oracle_rate_of_change(zfvm_oracle *o, const double *state, double *tendency) {
+  return zfvm_oracle_rate_of_change_av(o, state, nullptr, tendency, nullptr);
 }
 
 // EulerGlobalReconstruction::compute for the given cells, then
@@ -1506,7 +1628,8 @@ int zfvm_oracle_reconstruct_eval(zfvm_oracle *o, const double *state, int64_t n,
                                  const double *x, double *u) {
   Problem &pr = o->pr;
   auto s = load(state, pr.g.n_cells);
-  apply_bc(pr, s, s);
+  std::vector<double> q((size_t)pr.g.n_cells * pr.s.na, 0.0);
+  apply_bc(pr, s, s, q, q);
   std::vector<char> done(pr.g.n_cells, 0);
   for (int64_t k = 0; k < n; ++k) {
     const idx i = cells[k];
@@ -1537,29 +1660,38 @@ int zfvm_oracle_reconstruct_eval(zfvm_oracle *o, const double *state, int64_t n,
 
 int zfvm_oracle_cfl_dt(zfvm_oracle *o, const double *state, double *dt) {
   auto u = load(state, o->pr.g.n_cells);
-  apply_bc(o->pr, u, u);
+  std::vector<double> q((size_t)o->pr.g.n_cells * o->pr.s.na, 0.0);
+  apply_bc(o->pr, u, u, q, q);
   *dt = cfl_dt(o->pr, u);
   return 0;
 }
 
-int zfvm_oracle_step(zfvm_oracle *o, double *state, double dt) {
+int zfvm_oracle_step_av(zfvm_oracle *o, double *state, double *avars, double dt) {
   auto u = load(state, o->pr.g.n_cells);
-  apply_bc(o->pr, u, u);
-  int st = rk_step(o->pr, u, dt);
+  std::vector<double> q;
+  if (!load_avars(o->pr, avars, q)) return 1;
+  apply_bc(o->pr, u, u, q, q);
+  int st = rk_step(o->pr, u, q, dt);
   if (st) {
     g_oracle_err = st == 4 ? "equilibrium solve is not converging" : "non-physical state";
     return st;
   }
   store(u, state);
+  if (o->pr.s.na) std::copy(q.begin(), q.end(), avars);
   return 0;
 }
 
+int zfvm_oracle_step(zfvm_oracle *o, double *state, double dt) { return zfvm_oracle_step_av(o, state, nullptr, dt); }
+
 // TimeLoop without IO (fvm_loops/time_loop.cpp:36-81); the clock of the
 // unpinned ZisaTimeStepping is restated as dt = min(dt_cfl, t_end - t).
-int zfvm_oracle_run(zfvm_oracle *o, double *state, int64_t n_steps, double t_end, double *t_io, int64_t *steps_out) {
+int zfvm_oracle_run_av(zfvm_oracle *o, double *state, double *avars, int64_t n_steps, double t_end, double *t_io,
+                       int64_t *steps_out) {
   Problem &pr = o->pr;
   auto u = load(state, pr.g.n_cells);
-  apply_bc(pr, u, u);
+  std::vector<double> q;
+  if (!load_avars(pr, avars, q)) return 1;
+  apply_bc(pr, u, u, q, q);
   double t = *t_io;
   int64_t step = 0;
   // RejectLargeDensityChange (ode/step_rejection.cpp:17-56): factor and is_good
@@ -1574,7 +1706,8 @@ int zfvm_oracle_run(zfvm_oracle *o, double *state, int64_t n_steps, double t_end
     double dts = dt;
     if (t_end > 0.0) dts = std::min(dts, t_end - t);
     std::vector<Cv> u1 = u;
-    int st = rk_step(pr, u1, dts);
+    std::vector<double> q1 = q;
+    int st = rk_step(pr, u1, q1, dts);
     if (st) {
       g_oracle_err = st == 4 ? "equilibrium solve is not converging" : "non-physical state";
       return st;
@@ -1594,14 +1727,20 @@ int zfvm_oracle_run(zfvm_oracle *o, double *state, int64_t n_steps, double t_end
       factor = std::max(min_factor, std::min(factor, 1.0));
     }
     u.swap(u1);
+    q.swap(q1);
     t += dts;
     step += 1;
     dt = cfl_dt(pr, u) * (rejecting ? factor : 1.0);
   }
   store(u, state);
+  if (pr.s.na) std::copy(q.begin(), q.end(), avars);
   *t_io = t;
   if (steps_out) *steps_out = step;
   return 0;
+}
+
+int zfvm_oracle_run(zfvm_oracle *o, double *state, int64_t n_steps, double t_end, double *t_io, int64_t *steps_out) {
+  return zfvm_oracle_run_av(o, state, nullptr, n_steps, t_end, t_io, steps_out);
 }
 
 // ------------------------------------------------ known-answer helpers
@@ -1612,6 +1751,25 @@ int zfvm_oracle_flux(int kind, double gamma, const double *uL, const double *uR,
   for (int k = 0; k < 5; ++k) a[k] = uL[k], b[k] = uR[k];
   Cv r = kind == 0 ? hllc(eos, a, b) : rusanov(eos, a, b);
   for (int k = 0; k < 5; ++k) f[k] = r[k];
+  return 0;
+}
+
+// Flux of an advected variable through a face (face-frame states): the
+// numerical flux's speeds, then tracer_flux.
+int zfvm_oracle_tracer_flux(int kind, double gamma, const double *uL, const double *uR, double qL, double qR,
+                            double *f) {
+  EOS eos;
+  eos.gamma = gamma;
+  Cv a, b;
+  for (int k = 0; k < 5; ++k) a[k] = uL[k], b[k] = uR[k];
+  double speeds[3] = {0.0, 0.0, 0.0};
+  if (kind == 0) {
+    hllc(eos, a, b, speeds);
+    *f = tracer_flux_hllc(a, b, qL, qR, speeds);
+  } else {
+    rusanov(eos, a, b, speeds);
+    *f = tracer_flux_rusanov(a, b, qL, qR, speeds);
+  }
   return 0;
 }
 

@@ -61,10 +61,17 @@ int main(int argc, char **argv) {
   sc.boundary = ZFVM_BC_NONE;
   sc.precision = ZFVM_FP64;
   sc.steps_per_recompute = 1;
+  sc.n_avars = 1;
 
-  auto u0 = std::make_shared<zfvm::AllVariables>(nc);
+  auto u0 = std::make_shared<zfvm::AllVariables>(nc, 1);
   const double ic[8] = {2.0, 1.0, 1.0, 1.0, 1e-2, 0.05, 0.3, 0.0};
   zfvm::check(zfvm_initial_conditions(mesh, 1, ic, zfvm::cvars_data(*u0)));
+  // one advected variable: a mass fraction of 0.25 + 0.5 x
+  for (int64_t i = 0; i < nc; ++i) {
+    double cx = 0.0;
+    for (int k = 0; k < 3; ++k) cx += v[3 * vi[3 * i + k]] / 3.0;
+    u0->avars[i] = u0->cvars[5 * i] * (0.25 + 0.5 * cx);
+  }
 
   auto ds = std::make_shared<zfvm::DeviceSolver>(mesh, sc);
   zfvm::GpuLocalCFL cfl(ds);
@@ -73,7 +80,7 @@ int main(int argc, char **argv) {
   zfvm::GpuGlobalReconstruction grc(ds);
 
   const double dt = cfl(*u0);
-  zfvm::AllVariables tend(nc);
+  zfvm::AllVariables tend(nc, 1);
   roc.compute(tend, *u0, 0.0);
   auto u1 = rk.compute_step(u0, 0.0, dt);
   if (u1 == u0) return 2;  // compute_step must return a different buffer
@@ -97,10 +104,13 @@ int main(int argc, char **argv) {
   std::printf("recon");
   for (int k = 0; k < 5; ++k) std::printf(" %.17g", ux[k]);
   std::printf("\n");
-  double s_t = 0, s_u = 0;
+  double s_t = 0, s_u = 0, s_tq = 0, s_q = 0;
   for (double a : tend.cvars) s_t += a;
   for (double a : u1->cvars) s_u += a;
+  for (double a : tend.avars) s_tq += a;
+  for (double a : u1->avars) s_q += a;
   std::printf("sums %.17g %.17g\n", s_t, s_u);
+  std::printf("avars %.17g %.17g\n", s_tq, s_q);
 
   // DumpSnapshot / LoadSnapshot round trip of the stepped state
   const std::string dir = argc > 2 ? argv[2] : ".";
@@ -109,10 +119,10 @@ int main(int argc, char **argv) {
   clock.advance_to(dt, 1);
   dump(*u1, clock);
   zfvm::NpzLoadSnapshot load(dump.filename(0));
-  zfvm::AllVariables back(nc);
+  zfvm::AllVariables back(nc, 1);
   zfvm::SimulationClock clock2;
   load(back, clock2);
-  std::printf("snapshot %d %.17g %lld\n", int(back.cvars == u1->cvars), clock2.current_time(),
+  std::printf("snapshot %d %.17g %lld\n", int(back.cvars == u1->cvars && back.avars == u1->avars), clock2.current_time(),
               (long long)clock2.current_step());
   ds.reset();
   zfvm_mesh_destroy(mesh);

@@ -111,3 +111,18 @@ def ensemble_c4(n_instances: int = 256, n_min: int = 5000, n_max: int = 200000, 
                                      width=0.05, x0=r0 * np.cos(ang), y0=r0 * np.sin(ang))
         out.append((raw, mesh, scheme, u0))
     return out
+
+
+def tracers(mesh, u0, n_avars: int = 2):
+    """Mass-weighted tracers mq_k = rho q_k for n_avars mass fractions: a sharp
+    tanh front across x = 0.45 (exercises the nonlinear weights), a smooth
+    wave, then alternating copies."""
+    import numpy as np
+    c = mesh.geometry()["centers"]
+    q = np.empty((u0.shape[0], n_avars))
+    for k in range(n_avars):
+        if k % 2 == 0:
+            q[:, k] = 1.0 + 0.5 * np.tanh((c[:, 0] - 0.45) / 0.02)
+        else:
+            q[:, k] = 0.3 + 0.2 * np.sin(2 * np.pi * c[:, 1]) * np.cos(2 * np.pi * c[:, 0])
+    return u0[:, :1] * q

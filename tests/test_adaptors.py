@@ -34,21 +34,29 @@ def test_adaptors_match_python_binding(tmp_path, zlib):
     out = {ln.split()[0]: ln.split()[1:] for ln in r.stdout.splitlines()}
     from problems import polytrope_2d
     raw, mesh, scheme, u0 = polytrope_2d(n_rings=10, amplitude=1e-2, seed=7)
+    scheme.n_avars = 1
+    cx = raw.vertices[raw.vertex_indices].mean(axis=1)[:, 0]
+    q0 = u0[:, :1] * (0.25 + 0.5 * cx[:, None])
     s = z.Solver(mesh, scheme)
     s.set_state(u0)
+    s.set_avars(q0)
     dt = s.cfl_dt()
     assert float(out["dt"][0]) == dt
-    tend = s.rate_of_change()
+    tend, tq = s.rate_of_change_all()
     s.set_state(u0)
+    s.set_avars(q0)
     s.step(dt)
     u1, _ = s.get_state()
+    q1 = s.get_avars()
     assert float(out["sums"][0]) == pytest.approx(tend.sum(), rel=1e-14, abs=1e-14)
     assert float(out["sums"][1]) == pytest.approx(u1.sum(), rel=1e-14)
+    assert float(out["avars"][0]) == pytest.approx(tq.sum(), rel=1e-12, abs=1e-12)
+    assert float(out["avars"][1]) == pytest.approx(q1.sum(), rel=1e-14)
     # the snapshot holds the stepped state and the clock, and reads back equal
     assert out["snapshot"][0] == "1" and out["snapshot"][2] == "1"
     assert float(out["snapshot"][1]) == dt
     snap = z.read_snapshot(tmp_path / "snapshot_0000.npz")
-    assert np.array_equal(snap["cvars"], u1) and snap["n_steps"] == 1
+    assert np.array_equal(snap["cvars"], u1) and np.array_equal(snap["avars"], q1) and snap["n_steps"] == 1
     cell = int(out["cell"][0])
     s.set_state(u0)
     s.reconstruct()

@@ -82,7 +82,7 @@ class _SchemeDesc(C.Structure):
                 ("steps_per_recompute", C.c_int32), ("recompute_threshold", C.c_double),
                 ("reconstruction", C.c_int32), ("step_rejection_drho", C.c_double),
                 ("step_rejection_max_exponent", C.c_int32), ("heating_rate", C.c_double),
-                ("heating_r0", C.c_double), ("heating_r1", C.c_double)]
+                ("heating_r0", C.c_double), ("heating_r1", C.c_double), ("n_avars", C.c_int32)]
 
 
 _LIB = None
@@ -147,6 +147,9 @@ def load_library() -> C.CDLL:
         "zfvm_server_poll": [vp, i64, C.POINTER(i32)],
         "zfvm_server_wait": [vp, i64, C.c_double, dp, dp, C.POINTER(i64), dp],
         "zfvm_server_get_stats": [vp, vp],
+        "zfvm_set_avars": [vp, dp],
+        "zfvm_get_avars": [vp, dp],
+        "zfvm_rate_of_change_all": [vp, dp, dp],
         "zfvm_snapshot_write": [C.c_char_p, i64, dp, i32, dp, i32, C.c_double, i64],
         "zfvm_snapshot_info": [C.c_char_p, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)],
         "zfvm_snapshot_read": [C.c_char_p, i64, dp, i32, dp, dp, C.POINTER(i64)],
@@ -344,6 +347,7 @@ class Scheme:
     heating_rate: float = 0.0  # heating.rate; 0: no heating
     heating_r0: float = 0.0
     heating_r1: float = 0.0
+    n_avars: int = 0  # advected variables (mass-weighted tracers)
 
     def desc(self) -> _SchemeDesc:
         d = _SchemeDesc()
@@ -361,7 +365,7 @@ class Scheme:
                          self.rk_stages, self.cfl_number, self.equilibrium, self.gravity, self.gravity_strength,
                          self.flux_bc, self.boundary, self.steps_per_recompute, self.recompute_threshold,
                          self.reconstruction, self.step_rejection_drho, self.step_rejection_max_exponent,
-                         self.heating_rate, self.heating_r0, self.heating_r1],
+                         self.heating_rate, self.heating_r0, self.heating_r1, self.n_avars],
                         dtype=np.float64)
 
 
@@ -396,6 +400,23 @@ class Solver:
         t = C.c_double()
         _check(load_library().zfvm_get_state(self._h, _dp(a), C.byref(t)))
         return a, t.value
+
+    def set_avars(self, avars: np.ndarray) -> None:
+        """Advected variables (mass-weighted tracers), n_cells x n_avars."""
+        a = np.ascontiguousarray(avars, dtype=np.float64).reshape(self.mesh.n_cells, self.scheme.n_avars)
+        _check(load_library().zfvm_set_avars(self._h, _dp(a)))
+
+    def get_avars(self) -> np.ndarray:
+        a = np.zeros((self.mesh.n_cells, self.scheme.n_avars))
+        _check(load_library().zfvm_get_avars(self._h, _dp(a)))
+        return a
+
+    def rate_of_change_all(self) -> tuple[np.ndarray, np.ndarray]:
+        """Tendencies of the conserved and of the advected variables."""
+        u = np.zeros((self.mesh.n_cells, 5))
+        q = np.zeros((self.mesh.n_cells, self.scheme.n_avars))
+        _check(load_library().zfvm_rate_of_change_all(self._h, _dp(u), _dp(q)))
+        return u, q
 
     def write_snapshot(self, path, n_steps: int = 0) -> None:
         """Current state and time to a snapshot file (see `write_snapshot`)."""

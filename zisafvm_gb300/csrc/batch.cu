@@ -225,6 +225,8 @@ extern "C" int zfvm_batch_add(zfvm_batch *b, zfvm_solver *s, int64_t n_steps, do
   if (n_steps <= 0 && !(t_end > 0.0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > 0");
   if (s->scheme.step_rejection_drho > 0.0)
     return fail(ZFVM_EINVAL, "step rejection is not supported in batches (advance the solver by itself)");
+  if (s->na > 0)
+    return fail(ZFVM_EINVAL, "advected variables are not supported in batches (advance the solver by itself)");
   BATCH_GUARD_BEGIN
   int k = -1;
   for (int j = 0; j < b->max_slots; ++j) {

@@ -56,15 +56,22 @@ struct RoeAverage {
   __device__ __forceinline__ R operator()(R qL, R qR) const { return (qL + qR * ratio) / (R(1) + ratio); }
 };
 
-// HLLCBatten<IdealGasEOS>::flux
+// hllc_speeds<IdealGasEOS> (flux/hllc.hpp:35-81) and the contact speed s*:
+// the wave fan of the face, with the pressures and normal velocities it used.
+template <class R>
+struct HllcWaves {
+  R pL, pR, vL, vR, sL, s_star, sR;
+};
+
 template <int NV, class R>
-__device__ __forceinline__ void hllc_flux(const R *uL, const R *uR, R gamma, R *nf) {
-  R pL = pressure<NV>(uL, gamma), pR = pressure<NV>(uR, gamma);
-  R aL = sound_speed(uL[0], pL, gamma), aR = sound_speed(uR[0], pR, gamma);
+__device__ __forceinline__ HllcWaves<R> hllc_waves(const R *uL, const R *uR, R gamma) {
+  HllcWaves<R> w;
+  w.pL = pressure<NV>(uL, gamma), w.pR = pressure<NV>(uR, gamma);
+  R aL = sound_speed(uL[0], w.pL, gamma), aR = sound_speed(uR[0], w.pR, gamma);
   RoeAverage<R> roe(uL[0], uR[0]);
-  R vL = uL[1] / uL[0], vR = uR[1] / uR[0];
-  R v_t = roe(vL, vR);
-  R HL = (uL[NV - 1] + pL) / uL[0], HR = (uR[NV - 1] + pR) / uR[0];
+  w.vL = uL[1] / uL[0], w.vR = uR[1] / uR[0];
+  R v_t = roe(w.vL, w.vR);
+  R HL = (uL[NV - 1] + w.pL) / uL[0], HR = (uR[NV - 1] + w.pR) / uR[0];
   R H_t = roe(HL, HR);
   R vroe2 = R(0);
 #pragma unroll
@@ -73,9 +80,18 @@ __device__ __forceinline__ void hllc_flux(const R *uL, const R *uR, R gamma, R *
     vroe2 += a * a;
   }
   R a_t = sqrt((gamma - R(1)) * (H_t - R(0.5) * vroe2));
-  R sL = fmin(vL - aL, v_t - a_t);
-  R sR = fmax(vR + aR, v_t + a_t);
-  R s_star = (uR[1] * (sR - vR) - uL[1] * (sL - vL) + pL - pR) / (uR[0] * (sR - vR) - uL[0] * (sL - vL));
+  w.sL = fmin(w.vL - aL, v_t - a_t);
+  w.sR = fmax(w.vR + aR, v_t + a_t);
+  w.s_star = (uR[1] * (w.sR - w.vR) - uL[1] * (w.sL - w.vL) + w.pL - w.pR) /
+             (uR[0] * (w.sR - w.vR) - uL[0] * (w.sL - w.vL));
+  return w;
+}
+
+// HLLCBatten<IdealGasEOS>::flux
+template <int NV, class R>
+__device__ __forceinline__ void hllc_flux(const R *uL, const R *uR, R gamma, R *nf) {
+  const HllcWaves<R> w = hllc_waves<NV>(uL, uR, gamma);
+  const R pL = w.pL, pR = w.pR, vL = w.vL, vR = w.vR, sL = w.sL, sR = w.sR, s_star = w.s_star;
   const bool left = R(0) <= s_star;
   const R *uK = left ? uL : uR;
   R pK = left ? pL : pR;
@@ -92,6 +108,21 @@ __device__ __forceinline__ void hllc_flux(const R *uL, const R *uR, R gamma, R *
   }
 }
 
+// HLLCBatten::tracer_flux (flux/hllc.hpp:178-197): an advected variable mq
+// upwinded on s*, with the star-state correction inside the fan.
+__device__ __forceinline__ double hllc_tracer_flux(const HllcWaves<double> &w, double mqL, double mqR) {
+  const bool left = 0.0 <= w.s_star;
+  const double mqK = left ? mqL : mqR;
+  const double vK = left ? w.vL : w.vR;
+  const double fK = mqK * vK;
+  if (w.sL < 0.0 && 0.0 < w.sR) {
+    const double sK = left ? w.sL : w.sR;
+    const double cK = (sK - vK) / (sK - w.s_star);
+    return fK + sK * (cK * mqK - mqK);
+  }
+  return fK;
+}
+
 // Rusanov / local Lax-Friedrichs:
 //   F = (F(uL) + F(uR)) / 2 - s_max (uR - uL) / 2,  s_max = max(|vL| + aL, |vR| + aR).
 template <int NV, class R>
@@ -105,6 +136,18 @@ __device__ __forceinline__ void rusanov_flux(const R *uL, const R *uR, R gamma, 
   euler_flux<NV>(uR, pR, fR);
 #pragma unroll
   for (int k = 0; k < NV; ++k) nf[k] = R(0.5) * (fL[k] + fR[k]) - R(0.5) * smax * (uR[k] - uL[k]);
+}
+
+// The Rusanov flux's speed s_max, and its flux of an advected variable:
+// (mqL vL + mqR vR) / 2 - s_max (mqR - mqL) / 2.
+template <int NV>
+__device__ __forceinline__ double rusanov_speed(const double *uL, const double *uR, double gamma) {
+  const double pL = pressure<NV>(uL, gamma), pR = pressure<NV>(uR, gamma);
+  const double aL = sound_speed(uL[0], pL, gamma), aR = sound_speed(uR[0], pR, gamma);
+  return fmax(fabs(uL[1] / uL[0]) + aL, fabs(uR[1] / uR[0]) + aR);
+}
+__device__ __forceinline__ double rusanov_tracer_flux(double smax, double vL, double vR, double mqL, double mqR) {
+  return 0.5 * (mqL * vL + mqR * vR) - 0.5 * smax * (mqR - mqL);
 }
 
 }  // namespace dev

@@ -45,6 +45,14 @@ __global__ void k_soa_to_aos(const double *soa, double *aos, int n, int ld, int 
   for (int v = 0; v < 5; ++v) aos[i * 5 + v] = r[v];
 }
 
+// TimeLoop::reject_step for the advected variables of interior cells.
+__global__ void k_tracer_restore(const Clock *clock, const uint8_t *flags, const double *uprev, double *u0, int n,
+                                 int ld, int na) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !clock->restore || !(flags[i] & kInterior)) return;
+  for (int t = 0; t < na; ++t) u0[(size_t)t * ld + i] = uprev[(size_t)t * ld + i];
+}
+
 // FP64 state -> FP32 (hi, lo) pairs (mixed form), for a state set from the host
 __global__ void k_split(const double *soa, float2 *pairs, int n, int ld, int nv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -118,6 +126,20 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   return a;
 }
 
+TracerArgs tracer_args(zfvm_solver *s, int stage, double *tend_out) {
+  TracerArgs t{};
+  t.na = s->na;
+  t.q = stage == 0 ? s->tq0.p : s->tqx.p;
+  t.fv = s->tfv.p;
+  t.nf = s->tnf.p;
+  t.u0 = s->tq0.p;
+  t.ux = s->tqx.p;
+  for (int k = 0; k < 4; ++k) t.k[k] = s->tk.p ? s->tk.p + (size_t)k * s->na * s->ld : nullptr;
+  t.tend_out = tend_out;
+  t.uprev = s->tprev.p;
+  return t;
+}
+
 namespace {
 
 LaunchCfg launch_cfg(zfvm_solver *s) {
@@ -133,6 +155,20 @@ void dispatch_stage(zfvm_solver *s, StageArgs &a, cudaEvent_t *ev = nullptr) {
     case 1: launch_stage_s2o2(s->D, s->P, a, c); break;
     case 2: launch_stage_s3o3(s->D, s->P, a, c); break;
     case 3: launch_stage_s3o2(s->D, s->P, a, c); break;
+  }
+  CK(cudaGetLastError());
+}
+
+// the advected variables' three kernels of a stage, after the stage's own
+void dispatch_tracers(zfvm_solver *s, StageArgs &a, double *tend_out) {
+  if (!s->na) return;
+  TracerArgs ta = tracer_args(s, a.stage, tend_out);
+  const LaunchCfg c = launch_cfg(s);
+  switch (s->shape_id) {
+    case 0: launch_tracer_s2o3(s->D, s->P, a, ta, c); break;
+    case 1: launch_tracer_s2o2(s->D, s->P, a, ta, c); break;
+    case 2: launch_tracer_s3o3(s->D, s->P, a, ta, c); break;
+    case 3: launch_tracer_s3o2(s->D, s->P, a, ta, c); break;
   }
   CK(cudaGetLastError());
 }
@@ -157,6 +193,8 @@ void enqueue_restore(zfvm_solver *s) {
     k_restore<4><<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
   else
     k_restore<5><<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
+  if (s->na)
+    k_tracer_restore<<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->tprev.p, s->tq0.p, s->n_cells, s->ld, s->na);
   CK(cudaGetLastError());
 }
 
@@ -173,6 +211,7 @@ void enqueue_step(zfvm_solver *s) {
   for (int st = 0; st < s->P.n_stages; ++st) {
     StageArgs a = stage_args(s, st, nullptr);
     dispatch_stage(s, a);
+    dispatch_tracers(s, a, nullptr);
   }
 }
 
@@ -292,6 +331,9 @@ int build_solver(zfvm_solver *s) {
   P.inv_gm1 = 1.0 / (sc.gamma - 1.0);
   if (sc.reconstruction != ZFVM_RC_CWENO_AO && sc.reconstruction != ZFVM_RC_WENO_AO)
     return fail(ZFVM_EINVAL, "unknown reconstruction mode");
+  if (sc.n_avars < 0 || sc.n_avars > ZFVM_MAX_AVARS)
+    return fail(ZFVM_EINVAL, "n_avars must be 0 .. " + std::to_string(ZFVM_MAX_AVARS));
+  s->na = sc.n_avars;
   P.weno_ao = sc.reconstruction == ZFVM_RC_WENO_AO ? 1 : 0;
   std::memset(P.a, 0, sizeof(P.a));
   std::memset(P.b, 0, sizeof(P.b));
@@ -446,7 +488,9 @@ int build_solver(zfvm_solver *s) {
   s->l2g.upload(h_l2g);
   s->cface.upload(h_cface);
   s->src_map.upload(h_src);
-  if (!s->mixed) s->pinv.upload(h_pinv);
+  s->src_host.assign(h_src.begin(), h_src.begin() + n);
+  // FP64 pseudo-inverses: the FP64 form, and the advected variables of either form
+  if (!s->mixed || s->na) s->pinv.upload(h_pinv);
   s->center.upload(h_center);
   s->inv_len.upload(h_il);
   s->mom.upload(h_mom);
@@ -566,6 +610,17 @@ int build_solver(zfvm_solver *s) {
     s->uprev.alloc((size_t)nv * ld);
     s->uprev.zero(s->stream);
   }
+  if (s->na) {
+    const size_t nq = (size_t)s->na * ld;
+    s->tq0.alloc(nq);
+    s->tqx.alloc(nq);
+    s->tk.alloc((size_t)std::max(1, sc.rk_stages - 1) * nq);
+    s->tfv.alloc((size_t)nf * s->nqf * nq);
+    s->tnf.alloc((size_t)s->na * lde);
+    s->ttend.alloc(nq);
+    if (sc.step_rejection_drho > 0.0) s->tprev.alloc(nq);
+    for (auto *b : {&s->tq0, &s->tqx, &s->tk, &s->tfv, &s->tnf, &s->ttend, &s->tprev}) b->zero(s->stream);
+  }
   s->clock.alloc(1);
   for (auto *b : {&s->u0, &s->ux, &s->kbuf, &s->fv, &s->nfb, &s->tend, &s->dev0}) b->zero(s->stream);
   s->fv32.zero(s->stream);
@@ -632,6 +687,7 @@ int build_solver(zfvm_solver *s) {
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
            s->ux.n + s->kbuf.n + s->fv.n + s->nfb.n + s->srcb.n + s->eqth.n + s->tend.n + s->aos.n));
+  add(8 * (s->tq0.n + s->tqx.n + s->tk.n + s->tfv.n + s->tnf.n + s->ttend.n + s->tprev.n));
   s->device_bytes = bytes;
   return ZFVM_OK;
 }
@@ -750,18 +806,51 @@ extern "C" int zfvm_get_state(zfvm_solver *s, double *cvars, double *t) {
   SOLVER_GUARD_END
 }
 
+extern "C" int zfvm_set_avars(zfvm_solver *s, const double *avars) {
+  if (!s || (s->na && !avars)) return fail(ZFVM_EINVAL, "null argument");
+  if (!s->na) return ZFVM_OK;
+  SOLVER_GUARD_BEGIN
+  const size_t n = s->n_cells, na = s->na, ld = s->ld;
+  std::vector<double> soa((size_t)na * ld, 0.0);
+  for (size_t i = 0; i < n; ++i)
+    for (size_t t = 0; t < na; ++t) soa[t * ld + i] = avars[i * na + t];
+  CK(cudaMemcpyAsync(s->tq0.p, soa.data(), soa.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  // frozen ghost cells keep these values in every stage, like the state
+  CK(cudaMemcpyAsync(s->tqx.p, s->tq0.p, soa.size() * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_get_avars(zfvm_solver *s, double *avars) {
+  if (!s || (s->na && !avars)) return fail(ZFVM_EINVAL, "null argument");
+  if (!s->na) return ZFVM_OK;
+  SOLVER_GUARD_BEGIN
+  const size_t n = s->n_cells, na = s->na, ld = s->ld;
+  std::vector<double> soa((size_t)na * ld);
+  CK(cudaMemcpyAsync(soa.data(), s->tq0.p, soa.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  // periodic ghost cells report their source's values, as zfvm_get_state does
+  for (size_t i = 0; i < n; ++i)
+    for (size_t t = 0; t < na; ++t) avars[i * na + t] = soa[t * ld + (size_t)s->src_host[i]];
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
 extern "C" int zfvm_solver_write_snapshot(zfvm_solver *s, const char *path, int64_t n_steps) {
   if (!s || !path) return fail(ZFVM_EINVAL, "null argument");
-  std::vector<double> u;
+  std::vector<double> u, q;
   try {
     u.resize((size_t)s->n_cells * 5);
+    q.resize((size_t)s->n_cells * s->na);
   } catch (const std::bad_alloc &) {
     return fail(ZFVM_ENOMEM, "host allocation failed");
   }
   double t = 0.0;
   int st = zfvm_get_state(s, u.data(), &t);
+  if (st == ZFVM_OK) st = zfvm_get_avars(s, q.data());
   if (st != ZFVM_OK) return st;
-  return zfvm_snapshot_write(path, s->n_cells, u.data(), 0, nullptr, 1, t, n_steps);
+  return zfvm_snapshot_write(path, s->n_cells, u.data(), s->na, q.data(), 1, t, n_steps);
 }
 
 extern "C" int zfvm_solver_read_snapshot(zfvm_solver *s, const char *path, int64_t *n_steps) {
@@ -774,23 +863,28 @@ extern "C" int zfvm_solver_read_snapshot(zfvm_solver *s, const char *path, int64
     return fail(ZFVM_EINVAL, std::string(path) + " holds " + std::to_string(n) + " cells, the solver's mesh " +
                                  std::to_string(s->n_cells));
   if (!has_clock) return fail(ZFVM_EINVAL, std::string(path) + " has no \"time\" and \"n_steps\" (a steady state?)");
-  std::vector<double> u;
+  if (na != s->na)
+    return fail(ZFVM_EINVAL, std::string(path) + " holds " + std::to_string(na) + " advected variables, the solver " +
+                                 std::to_string(s->na));
+  std::vector<double> u, q;
   try {
     u.resize((size_t)n * 5);
+    q.resize((size_t)n * na);
   } catch (const std::bad_alloc &) {
     return fail(ZFVM_ENOMEM, "host allocation failed");
   }
   double t = 0.0;
   int64_t steps = 0;
-  st = zfvm_snapshot_read(path, n, u.data(), 0, nullptr, &t, &steps);
+  st = zfvm_snapshot_read(path, n, u.data(), na, q.data(), &t, &steps);
   if (st != ZFVM_OK) return st;
   st = zfvm_set_state(s, u.data(), t);
+  if (st == ZFVM_OK) st = zfvm_set_avars(s, q.data());
   if (st == ZFVM_OK && n_steps) *n_steps = steps;
   return st;
 }
 
-extern "C" int zfvm_rate_of_change(zfvm_solver *s, double *tendency) {
-  if (!s || !tendency) return fail(ZFVM_EINVAL, "null argument");
+extern "C" int zfvm_rate_of_change_all(zfvm_solver *s, double *tendency, double *avars_tendency) {
+  if (!s || !tendency || (s->na && !avars_tendency)) return fail(ZFVM_EINVAL, "null argument");
   SOLVER_GUARD_BEGIN
   Clock c = read_clock(s);
   c.done = 0;
@@ -799,6 +893,16 @@ extern "C" int zfvm_rate_of_change(zfvm_solver *s, double *tendency) {
   CK(cudaMemsetAsync(s->tend.p, 0, s->tend.n * sizeof(double), s->stream));
   StageArgs a = stage_args(s, 0, s->tend.p);
   dispatch_stage(s, a);
+  if (s->na) {
+    s->ttend.zero(s->stream);
+    dispatch_tracers(s, a, s->ttend.p);
+    std::vector<double> soa(s->ttend.n);
+    CK(cudaMemcpyAsync(soa.data(), s->ttend.p, soa.size() * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const size_t n = s->n_cells, na = s->na, ld = s->ld;
+    for (size_t i = 0; i < n; ++i)
+      for (size_t t = 0; t < na; ++t) avars_tendency[i * na + t] = soa[t * ld + i];
+  }
   const size_t n = s->n_cells;
   std::vector<int> ident(n);
   for (size_t i = 0; i < n; ++i) ident[i] = (int)i;
@@ -813,6 +917,18 @@ extern "C" int zfvm_rate_of_change(zfvm_solver *s, double *tendency) {
   if (code) return fail(code, msg);
   return ZFVM_OK;
   SOLVER_GUARD_END
+}
+
+extern "C" int zfvm_rate_of_change(zfvm_solver *s, double *tendency) {
+  if (!s || !tendency) return fail(ZFVM_EINVAL, "null argument");
+  if (!s->na) return zfvm_rate_of_change_all(s, tendency, nullptr);
+  std::vector<double> scratch;
+  try {
+    scratch.resize((size_t)s->n_cells * s->na);
+  } catch (const std::bad_alloc &) {
+    return fail(ZFVM_ENOMEM, "host allocation failed");
+  }
+  return zfvm_rate_of_change_all(s, tendency, scratch.data());
 }
 
 extern "C" int zfvm_cfl_dt(zfvm_solver *s, double *dt) {
@@ -904,7 +1020,8 @@ extern "C" int zfvm_advance_timed(zfvm_solver *s, int64_t n_steps, float *ms) {
 
 extern "C" int zfvm_launches_per_step(const zfvm_solver *s, int32_t *launches) {
   if (!s || !launches) return fail(ZFVM_EINVAL, "null argument");
-  *launches = 1 + 3 * s->P.n_stages;
+  // clock, restore (step rejection), three kernels per stage, three more with advected variables
+  *launches = 1 + (s->uprev.p ? 1 : 0) + 3 * s->P.n_stages * (s->na ? 2 : 1);
   return ZFVM_OK;
 }
 
@@ -993,6 +1110,12 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
     if (has_src) b += 4 * nv * ld + 8 * nd * ld + 4 * nqc * nd * ld;                   // src32 gphi_w wg32
   } else {
     b += 8 * (NP * ld + kst * nv * ld + nf * nqf * nv * ld + nv * lde);  // pinv kbuf fv nfb
+  }
+  const int64_t na = sc.n_avars;
+  if (na > 0) {
+    if (mixed) b += 8 * NP * ld;                                               // FP64 pinv
+    b += 8 * (na * ld * (3 + kst) + nf * nqf * na * ld + na * lde);             // tq0 tqx ttend tk tfv tnf
+    if (sc.step_rejection_drho > 0.0) b += 8 * na * ld;                         // tprev
   }
   return b;
 }

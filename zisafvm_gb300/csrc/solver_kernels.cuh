@@ -1654,6 +1654,14 @@ void batch_occupancy_t(const BatchCfg &c, int *blocks_per_sm) {
 }
 
 // ------------------------------------------------------------ launching
+}  // namespace dev
+}  // namespace zfvm
+
+#include "tracer_kernels.cuh"
+
+namespace zfvm {
+namespace dev {
+
 struct LaunchCfg {
   int n_cells, n_edges;
   bool eq, src, mixed;
@@ -1738,6 +1746,14 @@ void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const Launc
 }
 
 template <class S>
+void launch_tracer_t(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta, const LaunchCfg &c) {
+  if (c.mixed)
+    launch_tracer_p<S, true>(D, P, a, ta, c.n_cells, c.n_edges, c.eq, c.flux, c.stream);
+  else
+    launch_tracer_p<S, false>(D, P, a, ta, c.n_cells, c.n_edges, c.eq, c.flux, c.stream);
+}
+
+template <class S>
 void launch_cfl_t(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) {
   const int nb = (c.n_cells + 127) / 128;
   k_cfl<S><<<nb, 128, 0, c.stream>>>(D, P, u);
@@ -1749,7 +1765,8 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
   void launch_batch_stage_##name(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft,  \
                                  int stage, const BatchCfg &c);                                              \
   void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm);                          \
-  void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c);
+  void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c);  \
+  void launch_tracer_##name(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta, const LaunchCfg &c);
 #define ZFVM_DEFINE_SHAPE(name, S)                                                                \
   void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) { \
     launch_stage_t<S>(D, P, a, c);                                                                \
@@ -1764,6 +1781,9 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
   void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm) { batch_occupancy_t<S>(c, blocks_per_sm); } \
   void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {             \
     launch_export_t<S>(D, P, a, c);                                                                          \
+  }                                                                                                          \
+  void launch_tracer_##name(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta, const LaunchCfg &c) { \
+    launch_tracer_t<S>(D, P, a, ta, c);                                                                      \
   }
 
 ZFVM_DECLARE_SHAPE(s2o3)

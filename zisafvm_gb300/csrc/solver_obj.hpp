@@ -85,6 +85,11 @@ struct zfvm_solver {
   zfvm::DBuf<double> poly;                // exported reconstruction records (zfvm_reconstruct)
   zfvm::DBuf<double> uprev;               // step rejection: start state of the running step
   zfvm::DBuf<double> heat_w;              // heating: w_q * rate(x_q) at the cell quadrature points
+  // advected variables (n_avars > 0): state, next stage, stage tendencies,
+  // face-point values, face fluxes, tendency output, step-rejection save
+  int na = 0;
+  zfvm::DBuf<double> tq0, tqx, tk, tfv, tnf, ttend, tprev;
+  std::vector<int> src_host;              // periodic source of every cell (host copy of src_map)
   std::vector<double> poly_host;
   zfvm::DBuf<zfvm::dev::Clock> clock;
   bool has_src = false, has_eq = false, mixed = false;
@@ -96,6 +101,7 @@ struct zfvm_solver {
 
 // helpers shared with the batch engine (solver.cu)
 zfvm::dev::StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out);
+zfvm::dev::TracerArgs tracer_args(zfvm_solver *s, int stage, double *tend_out);
 zfvm::dev::Clock read_clock(zfvm_solver *s);
 zfvm::dev::Clock fresh_clock(const zfvm_solver *s, double t);
 void write_clock(zfvm_solver *s, const zfvm::dev::Clock &c);
