@@ -56,7 +56,9 @@ def test_adaptors_match_python_binding(tmp_path, zlib):
     assert out["snapshot"][0] == "1" and out["snapshot"][2] == "1"
     assert float(out["snapshot"][1]) == dt
     snap = z.read_snapshot(tmp_path / "snapshot_0000.npz")
-    assert np.array_equal(snap["cvars"], u1) and np.array_equal(snap["avars"], q1) and snap["n_steps"] == 1
+    assert np.array_equal(snap["cvars"], u1) and snap["n_steps"] == 1
+    # the example forms its tracer's centroids in another order: last-bit differences
+    assert np.abs(snap["avars"] - q1).max() <= 1e-13 * np.abs(q1).max()
     cell = int(out["cell"][0])
     s.set_state(u0)
     s.reconstruct()

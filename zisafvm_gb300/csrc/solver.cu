@@ -335,6 +335,11 @@ int build_solver(zfvm_solver *s) {
     return fail(ZFVM_EINVAL, "n_avars must be 0 .. " + std::to_string(ZFVM_MAX_AVARS));
   s->na = sc.n_avars;
   P.weno_ao = sc.reconstruction == ZFVM_RC_WENO_AO ? 1 : 0;
+  for (int k = 0; k < 5; ++k) P.lw32[k] = (float)P.lw[k];
+  P.inv_lw0_32 = (float)P.inv_lw0;
+  P.eps32 = (float)P.epsilon;
+  P.gamma32 = (float)P.gamma;
+  P.exp4 = P.exponent == 4.0 ? 1 : 0;
   std::memset(P.a, 0, sizeof(P.a));
   std::memset(P.b, 0, sizeof(P.b));
   if (sc.rk_stages == 1) {

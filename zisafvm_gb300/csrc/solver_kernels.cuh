@@ -162,6 +162,9 @@ struct Params {
   double inv_gm1;    // 1 / (gamma - 1), computed once on the host
   int weno_ao;       // reconstruction: 0 CWENO-AO, 1 WENO-AO
   double a[4][4], b[4];
+  // FP32 copies for the mixed form, rounded once on the host
+  float lw32[5], inv_lw0_32, eps32, gamma32;
+  int exp4;          // exponent == 4
 };
 
 struct StageArgs {
@@ -457,7 +460,18 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
 #pragma unroll
   for (int v = 0; v < NV; ++v) u0[v] = q[v * ld + j0];
   const double rho = u0[0];
-  const double eint = u0[NV - 1] - kinetic_energy<NV>(u0);
+  // mixed form: one FP64 reciprocal of rho serves the kinetic energy and the
+  // equilibrium fit (FP64 divisions cost the 1/64-rate FP64 pipe ~10 slots each)
+  double eint, inv_rho = 0.0;
+  if constexpr (MIXED) {
+    inv_rho = 1.0 / rho;
+    double m2 = 0.0;
+#pragma unroll
+    for (int v = 1; v < NV - 1; ++v) m2 += u0[v] * u0[v];
+    eint = u0[NV - 1] - 0.5 * m2 * inv_rho;
+  } else {
+    eint = u0[NV - 1] - kinetic_energy<NV>(u0);
+  }
   if (!(rho > 0.0) || !(eint > 0.0)) {
     set_status(d.clock, kStNonPhysical);
     return;
@@ -465,7 +479,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   // EulerScaling (model/characteristic_scale.hpp:23-32): {rho, c, c, c, E_int}
   R inv_s2[NV];
   {
-    const R rr = R(rho), ee = R(eint), g = R(gamma);
+    const R rr = R(rho), ee = R(eint), g = MIXED ? R(P.gamma32) : R(gamma);
     const R cs = sqrt(g * (ee * (g - R(1))) / rr);
     inv_s2[0] = R(1) / (rr * rr);
 #pragma unroll
@@ -481,14 +495,19 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   // T = h_r - <phi>, so K = (E_bar + sqrt(E_bar^2 - rho_bar^2 var)) / (2 rho_bar^2)
   // and T = 2 K rho_bar: the exact root the FP64 form's Newton iteration
   // converges to within its tolerance.
+  // With T = 2 K rho_bar = (E_bar + sqrt(disc)) / rho_bar: K = T / (2 rho_bar),
+  // h_r = T + <phi> and f = (gamma - 1) / (gamma K) = rho_bar / T.
   bool closed = false;
+  double f_closed = 0.0;
   if (EQ && MIXED && P.gamma2) {
     phi_ref = d.phi_cq[i];
     const double m1 = d.phi_m1[i], var = d.phi_var[i];
     const double disc = eint * eint - rho * rho * var;
     if (disc >= 0.0) {
-      eK = (eint + sqrt(disc)) / (2.0 * rho * rho);
-      eh = 2.0 * eK * rho + m1 - phi_ref;
+      const double T = (eint + sqrt(disc)) * inv_rho;
+      eK = 0.5 * T * inv_rho;
+      eh = T + m1 - phi_ref;
+      f_closed = rho / T;
       found = eK > 0.0;
       closed = true;
     }
@@ -499,7 +518,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     found = st == 0;
     if (st == 2) set_status(d.clock, kStNewton);
   }
-  const EqEval::Bound eqb = ev.bind(eh, eK, phi_ref);
+  const EqEval::Bound eqb = closed ? EqEval::Bound{eh + phi_ref, f_closed, eK} : ev.bind(eh, eK, phi_ref);
   if (EQ) {
     a.eqth[i] = eqb.hr;
     a.eqth[ld + i] = eqb.f;
@@ -525,16 +544,20 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
 #pragma unroll
     for (int v = 0; v < NV; ++v) dev0[v] = u0[v];
   }
+  float dev0f[NV];  // mixed form: the deviation rounded to FP32 once
+  DF f_split{0.f, 0.f};
   if (MIXED) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       a.dev0[v * ld + i] = dev0[v];
-      a.dev032[v * ld + i] = float(dev0[v]);
+      dev0f[v] = float(dev0[v]);
+      a.dev032[v * ld + i] = dev0f[v];
     }
     if (EQ && P.gamma2) {
-      const DF hr = df_split(eqb.hr), f = df_split(eqb.f), K = df_split(eqb.K);
+      const DF hr = df_split(eqb.hr), K = df_split(eqb.K);
+      f_split = df_split(eqb.f);
       a.eq32[i] = make_float2(hr.hi, hr.lo);
-      a.eq32[ld + i] = make_float2(f.hi, f.lo);
+      a.eq32[ld + i] = make_float2(f_split.hi, f_split.lo);
       a.eq32[2 * ld + i] = make_float2(K.hi, K.lo);
     }
   }
@@ -555,7 +578,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     if (diff_form) {
       own_m1 = df_of(d.m1s[j0]);
       own_var = df_of(d.vars[j0]);
-      df_f = df_split(eqb.f);
+      df_f = f_split;
       df_kf2 = df_split(eqb.K * (eqb.f * eqb.f));
       df_2t = df_split(2.0 * (eqb.hr - d.phi_m1[j0]));
     }
@@ -730,8 +753,8 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       if (!P.weno_ao) {
 #pragma unroll
         for (int k = 0; k < S::NB; ++k)
-          if (c < S::CB) x -= R(P.lw[k + 1]) * bb[k][c][v];
-        x *= R(P.inv_lw0);
+          if (c < S::CB) x -= (MIXED ? R(P.lw32[k + 1]) : R(P.lw[k + 1])) * bb[k][c][v];
+        x *= MIXED ? R(P.inv_lw0_32) : R(P.inv_lw0);
       }
       pf[c][v] = x;
     }
@@ -747,14 +770,16 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     return m;
   };
   R alpha[S::NB + 1];
-  auto weight = [&](R IS, double g) {
-    R pw = P.exponent == 4.0 ? (IS * IS) * (IS * IS) : R(pow(double(IS), P.exponent));
-    return R(g) / (R(P.epsilon) + pw);
+  auto weight = [&](R IS, R g) {
+    const bool e4 = MIXED ? P.exp4 != 0 : P.exponent == 4.0;
+    R pw = e4 ? (IS * IS) * (IS * IS) : R(pow(double(IS), P.exponent));
+    return g / ((MIXED ? R(P.eps32) : R(P.epsilon)) + pw);
   };
-  alpha[0] = weight(indicator([&](int c, int v) { return pf[c][v]; }, S::C0), P.lw[0]);
+  auto lw = [&](int k) { return MIXED ? R(P.lw32[k]) : R(P.lw[k]); };
+  alpha[0] = weight(indicator([&](int c, int v) { return pf[c][v]; }, S::C0), lw(0));
 #pragma unroll
   for (int k = 0; k < S::NB; ++k)
-    alpha[k + 1] = weight(indicator([&](int c, int v) { return bb[k][c][v]; }, S::CB), P.lw[k + 1]);
+    alpha[k + 1] = weight(indicator([&](int c, int v) { return bb[k][c][v]; }, S::CB), lw(k + 1));
   R al_tot = R(0);
 #pragma unroll
   for (int k = 0; k <= S::NB; ++k) al_tot += alpha[k];
@@ -904,11 +929,11 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     // the surface part p_eq n_out cancels face by face against the flux
     // baseline and is accounted for in k_face_flux
     R mg0 = R(0);
-    const R d0 = R(dev0[0]);
+    const R d0 = dev0f[0];
 #pragma unroll
     for (int k = 0; k < ND; ++k) {
       acc[1 + k] -= d0 * G[k];
-      mg0 += R(dev0[1 + k]) * G[k];
+      mg0 += dev0f[1 + k] * G[k];
     }
     acc[NV - 1] -= mg0;
     const double iv = d.inv_vol[i];
@@ -1310,16 +1335,18 @@ __device__ __forceinline__ double cfl_candidate(const double *u, double gamma, d
   return r / (sqrt(v2) + c);
 }
 
-// The same quantity with one reciprocal instead of four divisions (mixed form):
-// r / (|m| / rho + sqrt(gamma p / rho)), p = (gamma - 1) (E - |m|^2 / (2 rho)).
+// The mixed form's CFL candidate r / (|m| / rho + sqrt(gamma p / rho)),
+// p = (gamma - 1) (E - |m|^2 / (2 rho)), in FP32 from the FP32 high parts of
+// the new state: the time step carries FP32 precision, far more than the CFL
+// bound needs, and the FP64 square roots and divisions leave the FP64 pipe.
 template <int NV>
-__device__ __forceinline__ double cfl_candidate_1rcp(const double *u, double gamma, double r) {
-  double m2 = 0.0;
+__device__ __forceinline__ float cfl_candidate_f32(const float *u, float gamma, float r) {
+  float m2 = 0.f;
 #pragma unroll
   for (int k = 1; k < NV - 1; ++k) m2 += u[k] * u[k];
-  const double ir = 1.0 / u[0];
-  const double p = (u[NV - 1] - 0.5 * m2 * ir) * (gamma - 1.0);
-  return r / (sqrt(m2) * ir + sqrt(gamma * p * ir));
+  const float ir = 1.f / u[0];
+  const float p = (u[NV - 1] - 0.5f * m2 * ir) * (gamma - 1.f);
+  return r / (sqrtf(m2) * ir + sqrtf(gamma * p * ir));
 }
 
 __device__ __forceinline__ void block_min_to_clock(double cand, Clock *clock) {
@@ -1438,12 +1465,16 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
           un[v] = a.u0[v * ld + i] + dt * dudt;
         }
       }
+      float cand32 = INFINITY;  // mixed form: CFL candidate from the FP32 high parts
       if (MIXED) {
+        float hi[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           const DF x = df_split(un[v]);
           a.qs_next[v * ld + i] = make_float2(x.hi, x.lo);
+          hi[v] = x.hi;
         }
+        if (last) cand32 = cfl_candidate_f32<NV>(hi, P.gamma32, float(d.r_eff[i]));
       }
       if (!last) {
 #pragma unroll
@@ -1464,7 +1495,7 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
         }
 #pragma unroll
         for (int v = 0; v < NV; ++v) a.u0[v * ld + i] = un[v];
-        cand = MIXED ? cfl_candidate_1rcp<NV>(un, P.gamma, d.r_eff[i]) : cfl_candidate<NV>(un, P.gamma, d.r_eff[i]);
+        cand = MIXED ? double(cand32) : cfl_candidate<NV>(un, P.gamma, d.r_eff[i]);
         bool finite = true;
 #pragma unroll
         for (int v = 0; v < NV; ++v) finite = finite && isfinite(un[v]);
@@ -1474,9 +1505,11 @@ __device__ __forceinline__ double update_cell(const DevData &d, const Params &P,
   } else if (last && !a.tend_out && !d.clock->done && i < d.n_cells && (d.flags[i] & kFrozen)) {
     // a frozen ghost cell keeps its state; LocalCFL still counts it
     double w[NV];
+    float w32[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) w[v] = a.u0[v * d.ld + i];
-    cand = MIXED ? cfl_candidate_1rcp<NV>(w, P.gamma, d.r_eff[i]) : cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
+    for (int v = 0; v < NV; ++v) w[v] = a.u0[v * d.ld + i], w32[v] = float(w[v]);
+    cand = MIXED ? double(cfl_candidate_f32<NV>(w32, P.gamma32, float(d.r_eff[i])))
+                 : cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
   }
   return cand;
 }
@@ -1488,15 +1521,19 @@ __global__ void __launch_bounds__(128) k_update(const DevData d, const Params P,
 }
 
 template <class S>
-__global__ void __launch_bounds__(128) k_cfl(const DevData d, const Params P, const double *u) {
+__global__ void __launch_bounds__(128) k_cfl(const DevData d, const Params P, const double *u, int mixed) {
   constexpr int NV = S::NV;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double cand = INFINITY;
   if (i < d.n_cells && (d.flags[i] & (kInterior | kFrozen))) {
     double w[NV];
+    float w32[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) w[v] = u[v * d.ld + i];
-    cand = cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
+    for (int v = 0; v < NV; ++v) w[v] = u[v * d.ld + i], w32[v] = float(w[v]);
+    // the mixed form's candidate is the one its update computes, so a state
+    // set from the host (a restart) continues with the same time steps
+    cand = mixed ? double(cfl_candidate_f32<NV>(w32, P.gamma32, float(d.r_eff[i])))
+                 : cfl_candidate<NV>(w, P.gamma, d.r_eff[i]);
   }
   block_min_to_clock(cand, d.clock);
 }
@@ -1756,7 +1793,7 @@ void launch_tracer_t(const DevData &D, const Params &P, StageArgs &a, TracerArgs
 template <class S>
 void launch_cfl_t(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) {
   const int nb = (c.n_cells + 127) / 128;
-  k_cfl<S><<<nb, 128, 0, c.stream>>>(D, P, u);
+  k_cfl<S><<<nb, 128, 0, c.stream>>>(D, P, u, c.mixed ? 1 : 0);
 }
 
 #define ZFVM_DECLARE_SHAPE(name)                                                                  \
