@@ -89,6 +89,9 @@ typedef struct {
   int64_t n_cells, n_interior_cells, n_edges, n_interior_edges;
   int32_t n_cell_qp, n_face_qp, n_moments;
   double min_inradius, max_circum_radius, total_volume;
+  /* wall time of zfvm_mesh_create's phases: geometry and quadrature, stencil
+   * families, least-squares pseudo-inverses */
+  double setup_geometry_s, setup_stencils_s, setup_lsq_s;
 } zfvm_mesh_info;
 int zfvm_mesh_get_info(const zfvm_mesh *m, zfvm_mesh_info *info);
 

@@ -60,7 +60,8 @@ class _MeshInfo(C.Structure):
     _fields_ = [("n_dims", C.c_int32), ("n_cells", C.c_int64), ("n_interior_cells", C.c_int64),
                 ("n_edges", C.c_int64), ("n_interior_edges", C.c_int64), ("n_cell_qp", C.c_int32),
                 ("n_face_qp", C.c_int32), ("n_moments", C.c_int32), ("min_inradius", C.c_double),
-                ("max_circum_radius", C.c_double), ("total_volume", C.c_double)]
+                ("max_circum_radius", C.c_double), ("total_volume", C.c_double),
+                ("setup_geometry_s", C.c_double), ("setup_stencils_s", C.c_double), ("setup_lsq_s", C.c_double)]
 
 
 class _ServerDesc(C.Structure):

@@ -1,6 +1,7 @@
 // C ABI: mesh generation, mesh set-up (geometry, stencils, LSQ operators) and
 // initial data.  All of it is host work done once per mesh.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -126,6 +127,9 @@ extern "C" int zfvm_mesh_create(const zfvm_mesh_desc *d, zfvm_mesh **out) {
   }
   if (m->quad.moments >= 0 && m->quad.moments < max_order - 1)
     return fail(ZFVM_EINVAL, "quadrature.moments must be at least the polynomial degree");
+  using Clk = std::chrono::steady_clock;
+  auto secs = [](Clk::time_point a, Clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+  const auto t0 = Clk::now();
   m->grid = build_grid(d->n_dims, std::move(v), std::move(vi), m->quad);
   if (d->ghost) {
     std::vector<uint8_t> g(d->ghost, d->ghost + d->n_cells);
@@ -144,7 +148,9 @@ extern "C" int zfvm_mesh_create(const zfvm_mesh_desc *d, zfvm_mesh **out) {
     }
   }
   for (int64_t i = 0; i < d->n_cells; ++i) m->n_interior += (m->grid.flags[i] & kInterior) ? 1 : 0;
+  const auto t1 = Clk::now();
   m->fam = compute_stencil_families(m->grid, m->sparams);
+  const auto t2 = Clk::now();
   const index_t n = m->grid.n_cells;
   m->pinv.resize(n * kMaxStencils);
   m->pinv_rows.assign(n * kMaxStencils, 0);
@@ -166,6 +172,10 @@ extern "C" int zfvm_mesh_create(const zfvm_mesh_desc *d, zfvm_mesh **out) {
       m->pinv_cols[i * kMaxStencils + k] = cols;
     }
   }
+  const auto t3 = Clk::now();
+  m->t_geometry = secs(t0, t1);
+  m->t_stencils = secs(t1, t2);
+  m->t_lsq = secs(t2, t3);
   *out = m.release();
   return ZFVM_OK;
   ZFVM_GUARD_END
@@ -196,6 +206,9 @@ extern "C" int zfvm_mesh_get_info(const zfvm_mesh *m, zfvm_mesh_info *info) {
   info->min_inradius = rmin;
   info->max_circum_radius = rmax;
   info->total_volume = vol;
+  info->setup_geometry_s = m->t_geometry;
+  info->setup_stencils_s = m->t_stencils;
+  info->setup_lsq_s = m->t_lsq;
   return ZFVM_OK;
 }
 

@@ -5,7 +5,6 @@
 
 #include <algorithm>
 #include <map>
-#include <unordered_map>
 
 namespace zfvm {
 
@@ -162,6 +161,7 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
   auto V = [&](index_t i, int k) -> const Vec3 & { return g.vertices[g.vertex_indices[i * nb + k]]; };
 
   // standard vertex order
+#pragma omp parallel for schedule(static)
   for (index_t i = 0; i < n; ++i) {
     if (n_dims == 2) {
       Vec3 c = cross(V(i, 1) - V(i, 0), V(i, 2) - V(i, 0));
@@ -181,46 +181,49 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
     }
   }
 
-  // neighbours across each face
+  // neighbours across each face: every (cell, local face) goes into an
+  // open-addressing table keyed by the face's sorted vertex ids, in cell order;
+  // a face meets the first earlier unmatched entry with the same vertices
+  // (consumed entries stay as tombstones, so equal keys are met in insertion
+  // order)
   g.neighbours.assign(n * nb, -1);
   {
     const int fv = n_dims;  // vertices per face
-    std::unordered_map<uint64_t, std::vector<std::pair<index_t, int>>> faces;
-    faces.reserve((size_t)(n * nb));
-    auto key = [&](index_t i, int k) {
-      index_t a[3];
+    auto sorted_face = [&](index_t i, int k, index_t *a) {
       for (int r = 0; r < fv; ++r) a[r] = g.vertex_indices[i * nb + face_vertex(n_dims, k, r)];
       std::sort(a, a + fv);
-      uint64_t h = 1469598103934665603ull;
-      for (int r = 0; r < fv; ++r) h = (h ^ (uint64_t)a[r]) * 1099511628211ull;
-      return h;
     };
-    auto same = [&](index_t i, int k, index_t j, int l) {
-      index_t a[3], b[3];
-      for (int r = 0; r < fv; ++r) {
-        a[r] = g.vertex_indices[i * nb + face_vertex(n_dims, k, r)];
-        b[r] = g.vertex_indices[j * nb + face_vertex(n_dims, l, r)];
-      }
-      std::sort(a, a + fv);
-      std::sort(b, b + fv);
-      for (int r = 0; r < fv; ++r)
-        if (a[r] != b[r]) return false;
-      return true;
-    };
+    size_t cap = 16;
+    while (cap < 2 * (size_t)(n * nb)) cap <<= 1;
+    const size_t mask = cap - 1;
+    constexpr int64_t kEmpty = -1, kConsumed = -2;
+    std::vector<int64_t> table(cap, kEmpty);  // i * nb + k of a face still waiting for its partner
     for (index_t i = 0; i < n; ++i)
       for (int k = 0; k < nb; ++k) {
-        auto &bucket = faces[key(i, k)];
-        bool matched = false;
-        for (auto &e : bucket) {
-          if (e.first >= 0 && same(i, k, e.first, e.second)) {
-            g.neighbours[i * nb + k] = e.first;
-            g.neighbours[e.first * nb + e.second] = i;
-            e.first = -1;
-            matched = true;
+        index_t a[3];
+        sorted_face(i, k, a);
+        uint64_t h = 1469598103934665603ull;
+        for (int r = 0; r < fv; ++r) h = (h ^ (uint64_t)a[r]) * 1099511628211ull;
+        for (size_t s = (size_t)(h ^ (h >> 29)) & mask;; s = (s + 1) & mask) {
+          const int64_t e = table[s];
+          if (e == kEmpty) {
+            table[s] = i * nb + k;
+            break;
+          }
+          if (e == kConsumed) continue;
+          index_t b[3];
+          const index_t j = e / nb;
+          const int l = (int)(e % nb);
+          sorted_face(j, l, b);
+          bool same = true;
+          for (int r = 0; r < fv; ++r) same = same && a[r] == b[r];
+          if (same) {
+            g.neighbours[i * nb + k] = j;
+            g.neighbours[j * nb + l] = i;
+            table[s] = kConsumed;
             break;
           }
         }
-        if (!matched) bucket.push_back({i, k});
       }
   }
 
@@ -268,6 +271,7 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
   g.inradii.resize(n);
   g.circum_radii.resize(n);
   g.char_length.resize(n);
+#pragma omp parallel for schedule(static)
   for (index_t i = 0; i < n; ++i) {
     if (n_dims == 2) {
       const Vec3 &A = V(i, 0), &B = V(i, 1), &C = V(i, 2);
@@ -300,6 +304,7 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
   g.cell_qw.resize(n * g.n_cell_qp);
   g.cell_qx.resize(n * g.n_cell_qp);
   g.cell_centers.resize(n);
+#pragma omp parallel for schedule(static)
   for (index_t i = 0; i < n; ++i) {
     Vec3 v[4];
     for (int k = 0; k < nb; ++k) v[k] = V(i, k);
@@ -318,6 +323,8 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
   g.face_normal.resize(g.n_edges);
   g.face_t1.resize(g.n_edges);
   g.face_t2.resize(g.n_edges);
+  // every face is set up once, by its lower-numbered cell
+#pragma omp parallel for schedule(static)
   for (index_t i = 0; i < n; ++i)
     for (int k = 0; k < nb; ++k) {
       index_t j = g.neighbours[i * nb + k];
@@ -350,8 +357,11 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
   const int nmq = (int)mrule.w.size();
   g.n_moments = poly_dof(mdeg, n_dims);
   g.moments.assign(n * g.n_moments, 0.0);
+#pragma omp parallel
+  {
   std::vector<double> mw(nmq);
   std::vector<Vec3> mx(nmq);
+#pragma omp for schedule(static)
   for (index_t i = 0; i < n; ++i) {
     Vec3 v[4];
     for (int k = 0; k < nb; ++k) v[k] = V(i, k);
@@ -383,6 +393,7 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
       }
       len_d *= len;
     }
+  }
   }
 
   g.flags.assign(n, kInterior);

@@ -17,6 +17,7 @@ struct zfvm_mesh {
   std::vector<std::vector<double>> pinv;
   std::vector<int> pinv_rows, pinv_cols;
   zfvm::index_t n_interior = 0;
+  double t_geometry = 0.0, t_stencils = 0.0, t_lsq = 0.0;  // set-up phase wall times (s)
 };
 
 struct zfvm_rawmesh {

@@ -3,8 +3,11 @@
 // lsq_solver.cpp:139-403 of ZisaFVM.
 #include <algorithm>
 #include <cfloat>
+#include <cstdint>
 #include <numeric>
 #include <random>
+#include <utility>
+#include <vector>
 
 #include "grid.hpp"
 
@@ -193,14 +196,46 @@ struct Region {
   }
 };
 
+// Open-addressing set of cell ids for one candidate search (a few hundred
+// entries at most); grows by rehashing if a search ever exceeds it.
+struct SmallSet {
+  std::vector<index_t> slot = std::vector<index_t>(1024, -1);
+  size_t count = 0;
+  static size_t hash(index_t c) { return (size_t)((uint64_t)c * 0x9E3779B97F4A7C15ull >> 20); }
+  bool contains(index_t c) const {
+    const size_t mask = slot.size() - 1;
+    for (size_t h = hash(c) & mask;; h = (h + 1) & mask) {
+      if (slot[h] == c) return true;
+      if (slot[h] < 0) return false;
+    }
+  }
+  void insert(index_t c) {
+    if (2 * (count + 1) > slot.size()) {
+      std::vector<index_t> old;
+      old.swap(slot);
+      slot.assign(2 * old.size(), -1);
+      count = 0;
+      for (index_t x : old)
+        if (x >= 0) insert(x);
+    }
+    const size_t mask = slot.size() - 1;
+    size_t h = hash(c) & mask;
+    while (slot[h] >= 0 && slot[h] != c) h = (h + 1) & mask;
+    if (slot[h] < 0) slot[h] = c, ++count;
+  }
+};
+
 struct Selector {
   const Grid &g;
   RefRule query;  // highest-degree cell rule (stencil.cpp:178-190)
   explicit Selector(const Grid &grid)
       : g(grid), query(grid.n_dims == 2 ? triangle_rule(-1) : tetra_rule(-1)) {}
 
+  // A cell is in the region when any of the query points or its centre is
+  // (the centre, one test, is tried first; the answer is the same).
   bool cell_in_region(index_t c, const Region &reg) const {
     if (reg.kind == 0) return true;
+    if (reg.inside(g.cell_centers[c])) return true;
     const int nb = g.max_nb;
     Vec3 v[4];
     for (int k = 0; k < nb; ++k) v[k] = g.vertex(c, k);
@@ -209,20 +244,26 @@ struct Selector {
       for (int k = 1; k < nb; ++k) x = x + query.bary[q][k] * v[k];
       if (reg.inside(x)) return true;
     }
-    return reg.inside(g.cell_centers[c]);
+    return false;
   }
 
+  // Breadth-first candidates in discovery order; `seen` answers "already a
+  // candidate?" in O(1) instead of a scan of the list.
   std::vector<index_t> candidates(index_t i, index_t n_points, const Region &reg) const {
     index_t max_points = 5 * n_points;
     std::vector<index_t> cand{i};
+    SmallSet seen;
+    seen.insert(i);
     for (index_t p = 0; p < max_points; ++p) {
       if (p >= (index_t)cand.size()) break;
       index_t j = cand[p];
       for (int k = 0; k < g.max_nb; ++k) {
         index_t c = g.neighbours[j * g.max_nb + k];
         if (c < 0) continue;
-        if (std::find(cand.begin(), cand.end(), c) == cand.end() && cell_in_region(c, reg))
+        if (!seen.contains(c) && cell_in_region(c, reg)) {
           cand.push_back(c);
+          seen.insert(c);
+        }
       }
     }
     return cand;
@@ -231,11 +272,17 @@ struct Selector {
   std::vector<index_t> region_stencil(index_t i, index_t n_points, const Region &reg) const {
     auto cand = candidates(i, n_points, reg);
     const Vec3 xc = g.cell_centers[i];
-    // std::sort by distance in the reference; ties broken by candidate order here
-    std::stable_sort(cand.begin(), cand.end(), [&](index_t a, index_t b) {
-      return norm(g.cell_centers[a] - xc) < norm(g.cell_centers[b] - xc);
-    });
-    if ((index_t)cand.size() > n_points) cand.resize(n_points);
+    // std::sort by distance in the reference; ties broken by candidate order
+    // here.  The distances are computed once, not in every comparison.
+    std::vector<std::pair<double, index_t>> key(cand.size());
+    for (size_t r = 0; r < cand.size(); ++r) key[r] = {norm(g.cell_centers[cand[r]] - xc), cand[r]};
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<double, index_t> &a, const std::pair<double, index_t> &b) {
+                       return a.first < b.first;
+                     });
+    const size_t keep = std::min(cand.size(), (size_t)n_points);
+    cand.resize(keep);
+    for (size_t r = 0; r < keep; ++r) cand[r] = key[r].second;
     return cand;
   }
 
