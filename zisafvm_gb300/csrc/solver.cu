@@ -27,6 +27,22 @@ namespace dev {
 // mode 0: open a step; mode 1: close the last step only
 __global__ void k_clock(Clock *c, double cfl, int mode) { clock_step(c, cfl, mode); }
 
+// The whole clock from the host, passed by value as a launch argument: stream
+// ordered like a copy, but with no host buffer to keep alive and no implicit
+// synchronisation (a copy from pageable memory waits for the stream).
+__global__ void k_clock_set(Clock *c, Clock v) { *c = v; }
+
+// A new run's end condition, set on the device so no host round trip is needed.
+__global__ void k_clock_reset(Clock *c, long long n_steps, double t_end, double fixed_dt, double reject_drho) {
+  c->done = 0;
+  c->started = 0;
+  c->step = 0;
+  c->n_steps = n_steps;
+  c->t_end = t_end;
+  c->fixed_dt = fixed_dt;
+  c->reject_drho = reject_drho;
+}
+
 // state AoS (n x 5) <-> SoA (NV x ld); the 2D layout drops the third momentum
 __global__ void k_aos_to_soa(const double *aos, double *soa, int n, int ld, int nv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -252,7 +268,8 @@ Clock read_clock(zfvm_solver *s) {
 }
 
 void write_clock(zfvm_solver *s, const Clock &c) {
-  CK(cudaMemcpyAsync(s->clock.p, &c, sizeof(Clock), cudaMemcpyHostToDevice, s->stream));
+  k_clock_set<<<1, 1, 0, s->stream>>>(s->clock.p, c);
+  CK(cudaGetLastError());
 }
 
 namespace {
@@ -488,6 +505,7 @@ int build_solver(zfvm_solver *s) {
   }
 
   CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming));
   s->flags.upload(h_flags);
   s->bloc.upload(h_bloc);
   s->l2g.upload(h_l2g);
@@ -704,16 +722,10 @@ int cuda_fail(const CudaError &e) {
 }  // namespace
 
 void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt) {
-  Clock c = read_clock(s);
-  c.done = 0;
-  c.started = 0;
-  c.step = 0;
-  c.n_steps = n_steps;
-  c.t_end = t_end;
-  c.fixed_dt = fixed_dt;
   // step rejection belongs to the time loop (TimeLoop), not to a single step
-  c.reject_drho = fixed_dt > 0.0 ? 0.0 : s->scheme.step_rejection_drho;
-  write_clock(s, c);
+  const double drho = fixed_dt > 0.0 ? 0.0 : s->scheme.step_rejection_drho;
+  k_clock_reset<<<1, 1, 0, s->stream>>>(s->clock.p, (long long)n_steps, t_end, fixed_dt, drho);
+  CK(cudaGetLastError());
 }
 
 namespace {
@@ -770,6 +782,7 @@ extern "C" int zfvm_solver_destroy(zfvm_solver *s) {
     cudaStreamSynchronize(s->stream);
     cudaStreamDestroy(s->stream);
   }
+  if (s->ev_in) cudaEventDestroy(s->ev_in);
   delete s;
   return ZFVM_OK;
 }
@@ -779,6 +792,7 @@ extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
   SOLVER_GUARD_BEGIN
   const size_t n = s->n_cells;
   CK(cudaMemcpyAsync(s->aos.p, cvars, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaEventRecord(s->ev_in, s->stream));
   k_aos_to_soa<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->aos.p, s->u0.p, (int)n, s->ld, s->nv);
   CK(cudaGetLastError());
   // the stage state starts as a copy: the update writes interior cells only, so
@@ -793,7 +807,9 @@ extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
   Clock c = fresh_clock(s, t);
   write_clock(s, c);
   launch_cfl(s);
-  CK(cudaStreamSynchronize(s->stream));
+  // return once the caller's buffer has been read; the layout and CFL kernels
+  // run on, ordered before the solver's next work on its stream
+  CK(cudaEventSynchronize(s->ev_in));
   return ZFVM_OK;
   SOLVER_GUARD_END
 }
