@@ -91,3 +91,47 @@ def test_batch_autotune_keeps_results(zlib):
     x, _ = s_tuned.get_state()
     y, _ = s_plain.get_state()
     assert np.array_equal(x, y)
+
+
+def test_batch_with_tracers_and_step_rejection(zlib):
+    """Slots with advected variables and with step rejection, next to plain
+    ones, give the single-solve results: FP64 bit for bit (cvars, avars, time
+    and accepted steps)."""
+    from problems import tracers
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-1)
+    rej = z.Scheme(**{**scheme.__dict__, "step_rejection_drho": 2.4e-3, "step_rejection_max_exponent": 6})
+    tr = z.Scheme(**{**scheme.__dict__, "n_avars": 2})
+    both = z.Scheme(**{**rej.__dict__, "n_avars": 1})
+    rawv, meshv, schv, uv = vortex_2d(n=16, halo=3)
+    trv = z.Scheme(**{**schv.__dict__, "n_avars": 1})
+    cases = [(mesh, scheme, u0, None), (mesh, rej, u0, None), (mesh, tr, u0, tracers(mesh, u0, 2)),
+             (mesh, both, u0, tracers(mesh, u0, 1)), (meshv, trv, uv, tracers(meshv, uv, 1))]
+    b = z.Batch(8)
+    solvers, slots = [], []
+    for m, sc, u, q in cases:
+        s = z.Solver(m, sc)
+        s.set_state(u)
+        if q is not None:
+            s.set_avars(q)
+        solvers.append(s)
+        slots.append(b.add(s, n_steps=12))
+    for _ in range(20):
+        if b.advance(4) == 0:
+            break
+    for k, (m, sc, u, q) in enumerate(cases):
+        st = b.status(slots[k])
+        assert st["done"] and st["steps"] == 12
+        b.remove(slots[k])
+        u_b, t_b = solvers[k].get_state()
+        a = z.Solver(m, sc)
+        a.set_state(u)
+        if q is not None:
+            a.set_avars(q)
+        t_a, n_a = a.advance(n_steps=12)
+        u_a, _ = a.get_state()
+        assert n_a == 12 and t_b == t_a, (k, t_b, t_a)
+        assert np.array_equal(u_b, u_a), (k, np.abs(u_b - u_a).max())
+        if q is not None:
+            assert np.array_equal(solvers[k].get_avars(), a.get_avars())
+        if sc.step_rejection_drho > 0:
+            assert a.step_rejections() > 0

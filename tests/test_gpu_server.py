@@ -149,3 +149,25 @@ def test_close_with_requests_in_every_phase(zlib):
     u, t, steps, _ = srv.wait(srv.submit(mesh, scheme, u0, n_steps=n, t_end=t_end), timeout_s=120)
     srv.close()
     assert steps == n and np.isfinite(u).all()
+
+
+def test_step_rejection_request(zlib):
+    """A request with RejectLargeDensityChange runs in the server's batch and
+    returns exactly what the solver's own time loop gives (FP64)."""
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-1)
+    scheme.step_rejection_drho = 2.4e-3
+    scheme.step_rejection_max_exponent = 6
+    a = z.Solver(mesh, scheme)
+    a.set_state(u0)
+    t_a, n_a = a.advance(n_steps=12)
+    u_a, _ = a.get_state()
+    assert n_a == 12 and a.step_rejections() > 0
+    srv = z.Server(max_slots=4, steps_per_round=3)
+    mesh2, scheme2, u2, n2, t2 = _requests()[1]
+    other = srv.submit(mesh2, scheme2, u2, n_steps=n2, t_end=t2)
+    rid = srv.submit(mesh, scheme, u0, n_steps=12)
+    u, t, steps, _ = srv.wait(rid, timeout_s=120)
+    srv.wait(other, timeout_s=120)
+    srv.close()
+    assert steps == 12 and t == t_a
+    assert np.array_equal(u, u_a)

@@ -97,11 +97,19 @@ void enqueue_batch_step(zfvm_batch *b) {
   if (b->n_clock == 0) return;
   k_clock_multi<<<(b->n_clock + 127) / 128, 128, 0, b->stream>>>(b->clock_ptrs.p, b->cfls.p, b->n_clock, 0);
   CK(cudaGetLastError());
+  // slots with step rejection put back the start of a rejected step
+  for (zfvm_solver *s : b->slots)
+    if (s && s->uprev.p) solver_restore_on(s, b->stream);
   int stages = 0;
   for (auto &kv : b->groups) stages = std::max(stages, kv.second->key.stages);
-  for (int st = 0; st < stages; ++st)
+  for (int st = 0; st < stages; ++st) {
     for (auto &kv : b->groups)
       if (kv.second->n_ct > 0 && st < kv.second->key.stages) launch_group_stage(b, *kv.second, st);
+    // advected variables: the slot's own three kernels after the stage, which
+    // read the stage's face states before the next stage overwrites them
+    for (zfvm_solver *s : b->slots)
+      if (s && s->na && st < s->P.n_stages) solver_tracers_on(s, st, b->stream);
+  }
 }
 
 // Rebuild the device tables of every group from the current slots.
@@ -223,10 +231,6 @@ extern "C" int zfvm_batch_destroy(zfvm_batch *b) {
 extern "C" int zfvm_batch_add(zfvm_batch *b, zfvm_solver *s, int64_t n_steps, double t_end, int32_t *slot) {
   if (!b || !s) return fail(ZFVM_EINVAL, "null argument");
   if (n_steps <= 0 && !(t_end > 0.0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > 0");
-  if (s->scheme.step_rejection_drho > 0.0)
-    return fail(ZFVM_EINVAL, "step rejection is not supported in batches (advance the solver by itself)");
-  if (s->na > 0)
-    return fail(ZFVM_EINVAL, "advected variables are not supported in batches (advance the solver by itself)");
   BATCH_GUARD_BEGIN
   int k = -1;
   for (int j = 0; j < b->max_slots; ++j) {
@@ -249,15 +253,10 @@ extern "C" int zfvm_batch_remove(zfvm_batch *b, int32_t slot) {
   BATCH_GUARD_BEGIN
   CK(cudaStreamSynchronize(b->stream));
   zfvm_solver *s = b->slots[slot];
-  // close the slot's last step so its clock reads the final time
-  Clock c = read_clock(s);
-  if (c.started) {
-    c.t += c.dt;
-    c.step += 1;
-    c.started = 0;
-    write_clock(s, c);
-    CK(cudaStreamSynchronize(s->stream));
-  }
+  // close the slot's last step so its clock reads the final time (and a
+  // rejected last step is put back), as zfvm_advance does
+  solver_close_step(s);
+  CK(cudaStreamSynchronize(s->stream));
   b->slots[slot] = nullptr;
   b->dirty = true;
   return ZFVM_OK;

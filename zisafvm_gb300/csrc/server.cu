@@ -381,8 +381,8 @@ extern "C" int zfvm_server_submit(zfvm_server *S, zfvm_mesh *mesh, const zfvm_sc
                                   const double *cvars, double t0, int64_t n_steps, double t_end, int64_t *id) {
   if (!S || !mesh || !scheme || !cvars || !id) return fail(ZFVM_EINVAL, "null argument");
   if (n_steps <= 0 && !(t_end > t0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > t0");
-  if (scheme->n_avars != 0 || scheme->step_rejection_drho > 0.0)
-    return fail(ZFVM_EINVAL, "the server runs batched solves: no advected variables, no step rejection");
+  if (scheme->n_avars != 0)
+    return fail(ZFVM_EINVAL, "server requests carry no advected variables (zfvm_server_submit takes cvars only)");
   const int64_t bytes = solver_footprint(mesh, *scheme);
   if (bytes < 0) return fail(ZFVM_EINVAL, "the mesh has fewer than two stencils");
   if (bytes > S->desc.hbm_budget_bytes)

@@ -176,10 +176,11 @@ void dispatch_stage(zfvm_solver *s, StageArgs &a, cudaEvent_t *ev = nullptr) {
 }
 
 // the advected variables' three kernels of a stage, after the stage's own
-void dispatch_tracers(zfvm_solver *s, StageArgs &a, double *tend_out) {
+void dispatch_tracers(zfvm_solver *s, StageArgs &a, double *tend_out, cudaStream_t stream = nullptr) {
   if (!s->na) return;
   TracerArgs ta = tracer_args(s, a.stage, tend_out);
-  const LaunchCfg c = launch_cfg(s);
+  LaunchCfg c = launch_cfg(s);
+  if (stream) c.stream = stream;
   switch (s->shape_id) {
     case 0: launch_tracer_s2o3(s->D, s->P, a, ta, c); break;
     case 1: launch_tracer_s2o2(s->D, s->P, a, ta, c); break;
@@ -202,15 +203,16 @@ void launch_cfl(zfvm_solver *s) {
 
 // after every clock launch when step rejection is on: put back the start of a
 // rejected step (a no-op launch otherwise)
-void enqueue_restore(zfvm_solver *s) {
+void enqueue_restore(zfvm_solver *s, cudaStream_t stream = nullptr) {
   if (!s->uprev.p) return;
+  if (!stream) stream = s->stream;
   const int nb = (s->n_cells + 127) / 128;
   if (s->nv == 4)
-    k_restore<4><<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
+    k_restore<4><<<nb, 128, 0, stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
   else
-    k_restore<5><<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
+    k_restore<5><<<nb, 128, 0, stream>>>(s->clock.p, s->flags.p, s->uprev.p, s->u0.p, s->qsplit.p, s->n_cells, s->ld);
   if (s->na)
-    k_tracer_restore<<<nb, 128, 0, s->stream>>>(s->clock.p, s->flags.p, s->tprev.p, s->tq0.p, s->n_cells, s->ld, s->na);
+    k_tracer_restore<<<nb, 128, 0, stream>>>(s->clock.p, s->flags.p, s->tprev.p, s->tq0.p, s->n_cells, s->ld, s->na);
   CK(cudaGetLastError());
 }
 
@@ -232,6 +234,15 @@ void enqueue_step(zfvm_solver *s) {
 }
 
 }  // namespace
+
+void solver_restore_on(zfvm_solver *s, cudaStream_t stream) { enqueue_restore(s, stream); }
+
+void solver_tracers_on(zfvm_solver *s, int stage, cudaStream_t stream) {
+  StageArgs a = stage_args(s, stage, nullptr);
+  dispatch_tracers(s, a, nullptr, stream);
+}
+
+void solver_close_step(zfvm_solver *s) { close_step(s); }
 
 int status_to_code(int st, std::string &msg) {
   if (st & kStNewton) {

@@ -103,6 +103,12 @@ struct zfvm_solver {
 // helpers shared with the batch engine (solver.cu)
 zfvm::dev::StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out);
 zfvm::dev::TracerArgs tracer_args(zfvm_solver *s, int stage, double *tend_out);
+// per-solver launches the batch engine adds on its own stream: the restore of
+// a rejected step (after the clock), the advected variables' kernels of a
+// stage (after the stage), and the close of a solver's last step
+void solver_restore_on(zfvm_solver *s, cudaStream_t stream);
+void solver_tracers_on(zfvm_solver *s, int stage, cudaStream_t stream);
+void solver_close_step(zfvm_solver *s);
 zfvm::dev::Clock read_clock(zfvm_solver *s);
 zfvm::dev::Clock fresh_clock(const zfvm_solver *s, double t);
 void write_clock(zfvm_solver *s, const zfvm::dev::Clock &c);
