@@ -1,6 +1,6 @@
 """Mixed FP32/FP64 form against the FP64 form (and the oracle).
 
-Bars (north-star): relative L1 error of the conserved variables versus FP64
+Bars of the mixed form: relative L1 error of the conserved variables versus FP64
 <= 1e-6 after N steps; well-balanced residual on the unperturbed equilibrium
 <= 1e-10 (max |du/dt| and drift after N steps, relative).
 """

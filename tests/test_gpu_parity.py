@@ -1,6 +1,6 @@
 """GPU solver vs the CPU oracle, through the C ABI.
 
-FP64 parity bar (the benchmark spec's tolerance): relative L1 and Linf of the
+FP64 parity bar: relative L1 and Linf of the
 conserved variables within 1e-12 after N steps; single right-hand-side
 evaluations and CFL steps within 1e-13.
 """
