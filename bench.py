@@ -311,8 +311,9 @@ def pinned(shape):
 
 
 def e2e_single(solver, mesh, u0, steps, pg):
-    """Public-API loop with host buffers: upload the state from pinned memory,
-    advance one CFL step, read the new state back."""
+    """Public-API loop with host buffers (Solver.step_host, zfvm_step_host):
+    upload the state from pinned memory, advance one CFL step, read the new
+    state back into pinned memory, one call per step."""
     host, host_out = pinned((mesh.n_cells, 5)), pinned((mesh.n_cells, 5))
     solver.set_state(u0)
     solver.advance(n_steps=1)
@@ -322,9 +323,7 @@ def e2e_single(solver, mesh, u0, steps, pg):
         pg.barrier()
     t0 = time.perf_counter()
     for _ in range(steps):
-        solver.set_state(host)
-        solver.advance(n_steps=1)
-        solver.get_state(out=host_out)
+        solver.step_host(host, n_steps=1, out=host_out)
         host, host_out = host_out, host
     return time.perf_counter() - t0
 
@@ -390,7 +389,7 @@ def run_single_mesh(args, rank, world, local, pg):
         "config": {**desc, "precision": args.precision, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 for c2/c3 (state, operators and face data > 129 MB)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-                "path": "Solver.set_state / advance(1) / get_state with pinned host buffers"},
+                "path": "Solver.step_host (zfvm_step_host: upload, one CFL step, download) with pinned host buffers"},
         "roofline": roof,
         "gpu_launches": solver.launches_per_step() * args.steps,
         "clocks": clk.summary(),

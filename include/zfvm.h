@@ -164,6 +164,14 @@ int zfvm_solver_destroy(zfvm_solver *s);
 /* Upload / download the state (n_cells x 5 AoS host doubles) and the time. */
 int zfvm_set_state(zfvm_solver *s, const double *cvars, double t);
 int zfvm_get_state(zfvm_solver *s, double *cvars, double *t);
+/* set_state + advance + get_state in one call with one host synchronisation:
+ * upload cvars_in (n_cells x 5) at time t, run n_steps steps (or to t_end;
+ * with fixed_dt > 0 every step is fixed_dt long instead of the CFL step),
+ * download the result into cvars_out (may be cvars_in) and its time and step
+ * count.  The host-driven loop of RungeKutta::compute_step / TimeLoop with
+ * host states (ode/runge_kutta.cpp:146-171, fvm_loops/time_loop.cpp:47-81). */
+int zfvm_step_host(zfvm_solver *s, const double *cvars_in, double t, int64_t n_steps, double t_end,
+                   double fixed_dt, double *cvars_out, double *t_out, int64_t *steps_out);
 /* Upload / download the advected variables (AllVariables::avars: mass-weighted
  * tracers mq, n_cells x n_avars row-major).  A solver with n_avars > 0 starts
  * with them zero.  They are reconstructed like the conserved variables but each

@@ -202,9 +202,16 @@ class GpuRungeKutta : public TimeIntegrationBase {
                                              double dt) override {
     // the reference keeps u0 for reuse and returns its other buffer
     if (!ux_ || ux_ == u0) ux_ = std::make_shared<AllVariables>(*u0);
-    s_->set(*u0, t);
-    check(zfvm_step(s_->get(), dt));
-    s_->get_into(*ux_);
+    if (s_->n_avars()) {
+      s_->set(*u0, t);
+      check(zfvm_step(s_->get(), dt));
+      s_->get_into(*ux_);
+    } else {
+      // upload, one step of dt, download: one call, one synchronisation
+      double t_new;
+      int64_t steps;
+      check(zfvm_step_host(s_->get(), cvars_data(*u0), t, 1, 0.0, dt, cvars_data(*ux_), &t_new, &steps));
+    }
     auto out = ux_;
     ux_ = u0;
     return out;

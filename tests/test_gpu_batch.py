@@ -135,3 +135,52 @@ def test_batch_with_tracers_and_step_rejection(zlib):
             assert np.array_equal(solvers[k].get_avars(), a.get_avars())
         if sc.step_rejection_drho > 0:
             assert a.step_rejections() > 0
+
+
+def test_set_state_then_batch_advance(zlib):
+    """A state uploaded into a solver that sits in a batch is what the next
+    batch advance steps, even with no synchronisation in between (the batch
+    stream waits for the solver's stream): every step uploads, advances the
+    batch by one step and reads back, and matches the same sequence on a
+    solver by itself, bit for bit in FP64."""
+    probs = [polytrope_2d(n_rings=r, amplitude=1e-2, seed=r) for r in (20, 26)]
+    b = z.Batch(4)
+    solvers = []
+    for raw, mesh, scheme, u0 in probs:
+        s = z.Solver(mesh, scheme)
+        s.set_state(u0)
+        solvers.append(s)
+        b.add(s, n_steps=1000)
+    states = [u0.copy() for _, _, _, u0 in probs]
+    for _ in range(4):
+        for s, u in zip(solvers, states):
+            s.set_state(u)
+        b.advance(1)
+        states = [s.get_state()[0] for s in solvers]
+    for (raw, mesh, scheme, u0), u_b in zip(probs, states):
+        a = z.Solver(mesh, scheme)
+        u = u0.copy()
+        for _ in range(4):
+            a.set_state(u)
+            a.advance(n_steps=1)
+            u, _ = a.get_state()
+        assert np.array_equal(u_b, u), np.abs(u_b - u).max()
+
+
+def test_step_host_matches_separate_calls(zlib):
+    """zfvm_step_host (upload, steps, download in one call) gives what
+    set_state + advance + get_state give, for CFL steps and a fixed dt."""
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=20, amplitude=1e-2, seed=4)
+    a = z.Solver(mesh, scheme)
+    a.set_state(u0, 0.1)
+    t_a, n_a = a.advance(n_steps=3)
+    u_a, _ = a.get_state()
+    b = z.Solver(mesh, scheme)
+    u_b, t_b, n_b = b.step_host(u0, t=0.1, n_steps=3)
+    assert (t_b, n_b) == (t_a, n_a) and np.array_equal(u_b, u_a)
+    a.set_state(u0)
+    a.step(1e-3)
+    u_a, _ = a.get_state()
+    out = u0.copy()
+    u_b, t_b, n_b = b.step_host(out, n_steps=1, fixed_dt=1e-3, out=out)  # in place
+    assert n_b == 1 and abs(t_b - 1e-3) < 1e-18 and np.array_equal(u_b, u_a)

@@ -148,6 +148,7 @@ def load_library() -> C.CDLL:
         "zfvm_server_poll": [vp, i64, C.POINTER(i32)],
         "zfvm_server_wait": [vp, i64, C.c_double, dp, dp, C.POINTER(i64), dp],
         "zfvm_server_get_stats": [vp, vp],
+        "zfvm_step_host": [vp, dp, C.c_double, i64, C.c_double, C.c_double, dp, dp, C.POINTER(i64)],
         "zfvm_set_avars": [vp, dp],
         "zfvm_get_avars": [vp, dp],
         "zfvm_rate_of_change_all": [vp, dp, dp],
@@ -401,6 +402,19 @@ class Solver:
         t = C.c_double()
         _check(load_library().zfvm_get_state(self._h, _dp(a), C.byref(t)))
         return a, t.value
+
+    def step_host(self, cvars: np.ndarray, t: float = 0.0, n_steps: int = 1, t_end: float = 0.0,
+                  fixed_dt: float = 0.0, out: np.ndarray | None = None) -> tuple[np.ndarray, float, int]:
+        """Upload `cvars`, advance, download into `out` (e.g. pinned memory) in
+        one call with one host synchronisation: (state, t, steps)."""
+        a = np.ascontiguousarray(cvars, dtype=np.float64)
+        assert a.shape == (self.mesh.n_cells, 5)
+        o = out if out is not None else np.empty((self.mesh.n_cells, 5))
+        assert o.shape == (self.mesh.n_cells, 5) and o.dtype == np.float64 and o.flags.c_contiguous
+        tt, st = C.c_double(), C.c_int64()
+        _check(load_library().zfvm_step_host(self._h, _dp(a), t, n_steps, t_end, fixed_dt, _dp(o), C.byref(tt),
+                                             C.byref(st)))
+        return o, tt.value, st.value
 
     def set_avars(self, avars: np.ndarray) -> None:
         """Advected variables (mass-weighted tracers), n_cells x n_avars."""

@@ -177,6 +177,17 @@ void ensure_graph(zfvm_batch *b, int steps) {
   b->graph_steps = steps;
 }
 
+// Work a caller queued on a slot's own stream (the layout and CFL kernels of
+// zfvm_set_state, which returns once its host buffer is read) comes before the
+// batch's next launch on the batch stream.
+void wait_for_slots(zfvm_batch *b) {
+  for (zfvm_solver *s : b->slots)
+    if (s) {
+      CK(cudaEventRecord(s->ev_sync, s->stream));
+      CK(cudaStreamWaitEvent(b->stream, s->ev_sync, 0));
+    }
+}
+
 int running_count(zfvm_batch *b) {
   if (b->n_clock == 0) return 0;
   CK(cudaMemsetAsync(b->running.p, 0, sizeof(int), b->stream));
@@ -268,6 +279,7 @@ extern "C" int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_r
   BATCH_GUARD_BEGIN
   const int chunk = std::min(max_steps, 8);
   ensure_graph(b, chunk);
+  wait_for_slots(b);
   int done_steps = 0;
   while (done_steps < max_steps) {
     CK(cudaGraphLaunch(b->graph, b->stream));
@@ -287,6 +299,7 @@ extern "C" int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *m
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  wait_for_slots(b);
   CK(cudaStreamSynchronize(b->stream));
   CK(cudaEventRecord(e0, b->stream));
   for (int k = 0; k < n_steps; k += chunk) CK(cudaGraphLaunch(b->graph, b->stream));
@@ -306,6 +319,7 @@ extern "C" int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *be
   if (!b || trial_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
   BATCH_GUARD_BEGIN
   if (b->dirty) rebuild(b);
+  wait_for_slots(b);
   float overall = 0.0f;
   for (auto &kv : b->groups) {
     Group &g = *kv.second;
@@ -358,6 +372,7 @@ extern "C" int zfvm_batch_kernel_times(zfvm_batch *b, int32_t n_steps, float *ms
   if (!b || !ms || n_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
   BATCH_GUARD_BEGIN
   if (b->dirty) rebuild(b);
+  wait_for_slots(b);
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;

@@ -43,14 +43,7 @@ __global__ void k_clock_reset(Clock *c, long long n_steps, double t_end, double 
   c->reject_drho = reject_drho;
 }
 
-// state AoS (n x 5) <-> SoA (NV x ld); the 2D layout drops the third momentum
-__global__ void k_aos_to_soa(const double *aos, double *soa, int n, int ld, int nv) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int v = 0; v < nv - 1; ++v) soa[v * ld + i] = aos[i * 5 + v];
-  soa[(nv - 1) * ld + i] = aos[i * 5 + 4];
-}
-
+// state SoA (NV x ld) -> AoS (n x 5); the 2D layout drops the third momentum
 __global__ void k_soa_to_aos(const double *soa, double *aos, int n, int ld, int nv, const int *src) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -69,14 +62,22 @@ __global__ void k_tracer_restore(const Clock *clock, const uint8_t *flags, const
   for (int t = 0; t < na; ++t) u0[(size_t)t * ld + i] = uprev[(size_t)t * ld + i];
 }
 
-// FP64 state -> FP32 (hi, lo) pairs (mixed form), for a state set from the host
-__global__ void k_split(const double *soa, float2 *pairs, int n, int ld, int nv) {
+// A state from the host in one pass: AoS rows -> the step state u0 and the
+// stage state ux (SoA), and in the mixed form the FP32 (hi, lo) pairs of both.
+__global__ void k_state_in(const double *aos, double *u0, double *ux, float2 *pairs, int n, int ld, int nv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const size_t half = (size_t)nv * ld;
   for (int v = 0; v < nv; ++v) {
-    const double x = soa[(size_t)v * ld + i];
-    const float hi = __double2float_rn(x);
-    pairs[(size_t)v * ld + i] = make_float2(hi, __double2float_rn(x - (double)hi));
+    const double x = aos[i * 5 + (v == nv - 1 ? 4 : v)];
+    u0[(size_t)v * ld + i] = x;
+    ux[(size_t)v * ld + i] = x;
+    if (pairs) {
+      const float hi = __double2float_rn(x);
+      const float2 p = make_float2(hi, __double2float_rn(x - (double)hi));
+      pairs[(size_t)v * ld + i] = p;
+      pairs[half + (size_t)v * ld + i] = p;
+    }
   }
 }
 
@@ -517,6 +518,7 @@ int build_solver(zfvm_solver *s) {
 
   CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming));
+  CK(cudaEventCreateWithFlags(&s->ev_sync, cudaEventDisableTiming));
   s->flags.upload(h_flags);
   s->bloc.upload(h_bloc);
   s->l2g.upload(h_l2g);
@@ -794,30 +796,64 @@ extern "C" int zfvm_solver_destroy(zfvm_solver *s) {
     cudaStreamDestroy(s->stream);
   }
   if (s->ev_in) cudaEventDestroy(s->ev_in);
+  if (s->ev_sync) cudaEventDestroy(s->ev_sync);
   delete s;
   return ZFVM_OK;
 }
 
-extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
-  if (!s || !cvars) return fail(ZFVM_EINVAL, "null argument");
-  SOLVER_GUARD_BEGIN
+namespace {
+
+// Upload a host state and open a fresh clock at time t, all stream-ordered;
+// ev_in is recorded once the host buffer has been read.
+void upload_state(zfvm_solver *s, const double *cvars, double t) {
   const size_t n = s->n_cells;
   CK(cudaMemcpyAsync(s->aos.p, cvars, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
   CK(cudaEventRecord(s->ev_in, s->stream));
-  k_aos_to_soa<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->aos.p, s->u0.p, (int)n, s->ld, s->nv);
-  CK(cudaGetLastError());
   // the stage state starts as a copy: the update writes interior cells only, so
   // frozen ghost cells carry their values into every stage from here
-  CK(cudaMemcpyAsync(s->ux.p, s->u0.p, s->u0.n * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
-  if (s->qsplit.p) {
-    const size_t half = (size_t)s->nv * s->ld;
-    k_split<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->qsplit.p, (int)n, s->ld, s->nv);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(s->qsplit.p + half, s->qsplit.p, half * sizeof(float2), cudaMemcpyDeviceToDevice, s->stream));
-  }
+  k_state_in<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->aos.p, s->u0.p, s->ux.p, s->qsplit.p, (int)n, s->ld,
+                                                            s->nv);
+  CK(cudaGetLastError());
   Clock c = fresh_clock(s, t);
   write_clock(s, c);
   launch_cfl(s);
+}
+
+// Download the step state into host rows (no synchronisation).
+void download_state(zfvm_solver *s, double *cvars) {
+  const size_t n = s->n_cells;
+  k_soa_to_aos<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->aos.p, (int)n, s->ld, s->nv, s->src_map.p);
+  CK(cudaGetLastError());
+  if (cvars) CK(cudaMemcpyAsync(cvars, s->aos.p, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+}
+
+// The time loop on the device: graph-replayed chunks of steps until the
+// clock is done, then the close of the last step.  Polls the clock only when
+// the end is a time or steps may be rejected.
+void run_steps(zfvm_solver *s, int64_t n_steps, double t_end, double fixed_dt) {
+  reset_clock_for_run(s, n_steps, t_end, fixed_dt);
+  const int chunk = n_steps > 0 ? (int)std::min<int64_t>(n_steps, 16) : 16;
+  build_graph(s, chunk);
+  int64_t launched = 0;
+  const bool rejecting = s->uprev.p != nullptr;  // rejected steps do not count
+  while (true) {
+    CK(cudaGraphLaunch(s->graph, s->stream));
+    launched += chunk;
+    if (n_steps > 0 && launched >= n_steps && !rejecting) break;
+    if (launched % (chunk * 8) == 0 || n_steps <= 0 || rejecting) {
+      Clock c = read_clock(s);
+      if (c.done) break;
+    }
+  }
+  close_step(s);
+}
+
+}  // namespace
+
+extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
+  if (!s || !cvars) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
+  upload_state(s, cvars, t);
   // return once the caller's buffer has been read; the layout and CFL kernels
   // run on, ordered before the solver's next work on its stream
   CK(cudaEventSynchronize(s->ev_in));
@@ -825,13 +861,30 @@ extern "C" int zfvm_set_state(zfvm_solver *s, const double *cvars, double t) {
   SOLVER_GUARD_END
 }
 
+extern "C" int zfvm_step_host(zfvm_solver *s, const double *cvars_in, double t, int64_t n_steps, double t_end,
+                              double fixed_dt, double *cvars_out, double *t_out, int64_t *steps_out) {
+  if (!s || !cvars_in || !cvars_out) return fail(ZFVM_EINVAL, "null argument");
+  if (n_steps <= 0 && !(t_end > t)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > t");
+  if (fixed_dt < 0.0) return fail(ZFVM_EINVAL, "negative fixed_dt");
+  SOLVER_GUARD_BEGIN
+  upload_state(s, cvars_in, t);
+  run_steps(s, n_steps, t_end, fixed_dt);
+  // cvars_out may be cvars_in: the upload has read it before the download lands
+  download_state(s, cvars_out);
+  const Clock c = read_clock(s);  // the one synchronisation of the call
+  if (t_out) *t_out = c.t;
+  if (steps_out) *steps_out = c.step;
+  std::string msg;
+  const int code = status_to_code(c.status, msg);
+  if (code) return fail(code, msg);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
+}
+
 extern "C" int zfvm_get_state(zfvm_solver *s, double *cvars, double *t) {
   if (!s) return fail(ZFVM_EINVAL, "null argument");
   SOLVER_GUARD_BEGIN
-  const size_t n = s->n_cells;
-  k_soa_to_aos<<<(int)((n + 127) / 128), 128, 0, s->stream>>>(s->u0.p, s->aos.p, (int)n, s->ld, s->nv, s->src_map.p);
-  CK(cudaGetLastError());
-  if (cvars) CK(cudaMemcpyAsync(cvars, s->aos.p, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  download_state(s, cvars);
   Clock c = read_clock(s);
   if (t) *t = c.t;
   return ZFVM_OK;
@@ -994,21 +1047,7 @@ extern "C" int zfvm_advance(zfvm_solver *s, int64_t n_steps, double t_end, doubl
   if (!s) return fail(ZFVM_EINVAL, "null solver");
   if (n_steps <= 0 && !(t_end > 0.0)) return fail(ZFVM_EINVAL, "need n_steps > 0 or t_end > 0");
   SOLVER_GUARD_BEGIN
-  reset_clock_for_run(s, n_steps, t_end, 0.0);
-  const int chunk = n_steps > 0 ? (int)std::min<int64_t>(n_steps, 16) : 16;
-  build_graph(s, chunk);
-  int64_t launched = 0;
-  const bool rejecting = s->uprev.p != nullptr;  // rejected steps do not count
-  while (true) {
-    CK(cudaGraphLaunch(s->graph, s->stream));
-    launched += chunk;
-    if (n_steps > 0 && launched >= n_steps && !rejecting) break;
-    if (launched % (chunk * 8) == 0 || n_steps <= 0 || rejecting) {
-      Clock c = read_clock(s);
-      if (c.done) break;
-    }
-  }
-  close_step(s);
+  run_steps(s, n_steps, t_end, 0.0);
   Clock c = read_clock(s);
   if (t_out) *t_out = c.t;
   if (steps_out) *steps_out = c.step;

@@ -69,7 +69,8 @@ struct zfvm_solver {
   int n_cells = 0, n_edges = 0;
   int shape_id = -1;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev_in = nullptr;  // recorded after a host upload
+  cudaEvent_t ev_in = nullptr;    // recorded after a host upload
+  cudaEvent_t ev_sync = nullptr;  // recorded by a batch before it uses the solver
   zfvm::dev::Params P{};
   zfvm::dev::DevData D{};
   // device buffers
