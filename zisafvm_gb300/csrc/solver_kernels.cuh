@@ -295,32 +295,38 @@ __device__ int solve_equilibrium(const EqEval &ev, const Params &P, const DevDat
   const double h0 = gamma / ev.gm1 * p_g / rho_bar;
   const double K0 = p_g / powd(rho_bar, gamma);
   const double atol0 = 1e-13 * h0, atol1 = 1e-13 * K0;
-  auto f = [&](double h, double K, double &f0, double &f1) {
+  // EqEval::bind's factor (gamma - 1) / (gamma K), in bind's own operation
+  // order: it depends on K only, so the evaluations that vary h reuse it
+  auto factor = [&](double K) { return 1.0 / K * ev.gm1 / ev.gamma; };
+  auto f = [&](double h, double K, double fk, double &f0, double &f1) {
     double rb, Eb;
-    eq_cell_average<NQC>(ev, P, d, ev.bind(h, K, phi_ref), i, rb, Eb);
+    eq_cell_average<NQC>(ev, P, d, EqEval::Bound{h + phi_ref, fk, K}, i, rb, Eb);
     f0 = rho_bar - rb;
     f1 = E_bar - Eb;
   };
   double x0 = h0, x1 = K0, fx0, fx1;
-  f(x0, x1, fx0, fx1);
+  double fk = factor(x1);
+  f(x0, x1, fk, fx0, fx1);
   double dx0 = 2.0 * atol0 + 1.0, dx1 = 2.0 * atol1 + 1.0;
   double hist0[3] = {0, 0, 0}, hist1[3] = {0, 0, 0};
   int iter = 0;
   while (!(fabs(dx0) <= atol0 && fabs(dx1) <= atol1) && iter < 20) {
     double eps0 = 1e-6 * fabs(x0), eps1 = 1e-6 * fabs(x1);
     double a0, a1, b0, b1;
-    f(x0 + 0.5 * eps0, x1, a0, a1);
-    f(x0 - 0.5 * eps0, x1, b0, b1);
+    f(x0 + 0.5 * eps0, x1, fk, a0, a1);
+    f(x0 - 0.5 * eps0, x1, fk, b0, b1);
     double d00 = (a0 - b0) / eps0, d01 = (a1 - b1) / eps0;
-    f(x0, x1 + 0.5 * eps1, a0, a1);
-    f(x0, x1 - 0.5 * eps1, b0, b1);
+    const double k_up = x1 + 0.5 * eps1, k_dn = x1 - 0.5 * eps1;
+    f(x0, k_up, factor(k_up), a0, a1);
+    f(x0, k_dn, factor(k_dn), b0, b1);
     double d10 = (a0 - b0) / eps1, d11 = (a1 - b1) / eps1;
     double inv_det = 1.0 / (d00 * d11 - d01 * d10);
     dx0 = inv_det * (d11 * fx0 - d10 * fx1);
     dx1 = inv_det * (-d01 * fx0 + d00 * fx1);
     x0 -= dx0;
     x1 -= dx1;
-    f(x0, x1, fx0, fx1);
+    fk = factor(x1);
+    f(x0, x1, fk, fx0, fx1);
     hist0[0] = hist0[1], hist0[1] = hist0[2], hist0[2] = dx0;
     hist1[0] = hist1[1], hist1[1] = hist1[2], hist1[2] = dx1;
     if (iter >= 4) {
