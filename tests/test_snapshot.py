@@ -83,3 +83,43 @@ def test_refusals(zlib, tmp_path):
     np.savez(tmp_path / "e.npz", time=0.0, n_steps=0, n_avars=0, **{k: v for k, v in ds.items() if k != "E"})
     with pytest.raises(z.ZfvmError, match='"E"'):
         z.read_snapshot(tmp_path / "e.npz")
+
+
+def test_reader_survives_corrupted_files(zlib, tmp_path):
+    """The reader parses files it did not write: truncations, bit flips and
+    overwritten header fields must give an error (or, for a flip in the data
+    only, a successful read), never a crash."""
+    u, q = _state(23, 2, seed=7)
+    good = tmp_path / "good.npz"
+    z.write_snapshot(good, u, t=1.0, n_steps=2, avars=q)
+    data = bytearray(good.read_bytes())
+    rng = np.random.default_rng(11)
+    bad = tmp_path / "bad.npz"
+    trials = 0
+    for cut in list(range(0, len(data), max(1, len(data) // 97))) + [len(data) - 1, len(data) - 23]:
+        bad.write_bytes(bytes(data[:cut]))
+        with pytest.raises(z.ZfvmError):
+            z.read_snapshot(bad)
+        trials += 1
+    for _ in range(400):
+        d = bytearray(data)
+        for _ in range(int(rng.integers(1, 6))):
+            pos = int(rng.integers(0, len(d)))
+            d[pos] = int(rng.integers(0, 256)) if rng.random() < 0.5 else d[pos] ^ (1 << int(rng.integers(0, 8)))
+        bad.write_bytes(bytes(d))
+        try:
+            r = z.read_snapshot(bad)
+            assert r["cvars"].shape == (23, 5)
+        except z.ZfvmError:
+            pass
+        trials += 1
+    # hostile header values: huge sizes, counts and offsets in the zip records
+    end = len(data) - 22
+    for off, val in ((end + 10, 0xFFFF), (end + 12, 0xFFFFFFFF), (end + 16, 0xFFFFFFFF)):
+        d = bytearray(data)
+        d[off:off + (2 if val == 0xFFFF else 4)] = val.to_bytes(2 if val == 0xFFFF else 4, "little")
+        bad.write_bytes(bytes(d))
+        with pytest.raises(z.ZfvmError):
+            z.read_snapshot(bad)
+        trials += 1
+    assert trials > 400

@@ -170,7 +170,7 @@ def load_library() -> C.CDLL:
 
 def _check(code: int) -> None:
     if code != 0:
-        msg = load_library().zfvm_last_error().decode()
+        msg = load_library().zfvm_last_error().decode(errors="replace")
         raise ZfvmError(code, msg)
 
 

@@ -19,6 +19,7 @@
 // and renamed, so a crash mid-write never leaves a truncated snapshot behind.
 // The reader accepts uncompressed .npz files written by numpy.savez as well
 // (including their zip64 records); compressed members are refused.
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -294,14 +295,18 @@ bool parse_npy(Archive &A, const std::string &name, uint64_t off, uint64_t size,
   while (p < shape.size()) {
     while (p < shape.size() && (shape[p] == ' ' || shape[p] == ',')) ++p;
     if (p >= shape.size()) break;
+    uint64_t v = 0;
     size_t e = p;
-    while (e < shape.size() && shape[e] >= '0' && shape[e] <= '9') ++e;
-    if (e == p) {
+    for (; e < shape.size() && shape[e] >= '0' && shape[e] <= '9'; ++e) {
+      if (v > (1ull << 40)) break;  // no dataset here is that long
+      v = 10 * v + (uint64_t)(shape[e] - '0');
+    }
+    if (e == p || v > (1ull << 40) || (e < shape.size() && shape[e] != ',' && shape[e] != ' ')) {
       A.error = name + ": bad shape (" + shape + ")";
       return false;
     }
-    ds.n *= std::stoull(shape.substr(p, e - p));
-    ++dims;
+    ds.n *= v;
+    if (++dims > 1) break;
     p = e;
   }
   ds.scalar = dims == 0;
@@ -309,8 +314,10 @@ bool parse_npy(Archive &A, const std::string &name, uint64_t off, uint64_t size,
     A.error = name + ": only one-dimensional datasets are read";
     return false;
   }
-  const uint64_t item = descr.size() >= 3 ? std::stoull(descr.substr(2)) : 0;
-  if (item == 0 || start + hl + ds.n * item > size) {
+  // item size from the type code ('<f8' -> 8); only 1, 2, 4 and 8 are types
+  const char c = descr.size() == 3 ? descr[2] : '0';
+  const uint64_t item = (c == '1' || c == '2' || c == '4' || c == '8') ? (uint64_t)(c - '0') : 0;
+  if (item == 0 || ds.n > (size - start - hl) / item) {
     A.error = name + ": data shorter than its shape";
     return false;
   }
@@ -358,6 +365,10 @@ bool open_archive(Archive &A, const std::string &path) {
     cd_size = get64(z + 40);
     cd_off = get64(z + 48);
   }
+  if (cd_off > (uint64_t)flen || cd_size > (uint64_t)flen - cd_off || n_entries > cd_size / 46 + 1) {
+    A.error = path + ": bad central directory";
+    return false;
+  }
   std::vector<unsigned char> cd(cd_size);
   if (!A.read_at(cd_off, cd.data(), cd_size)) {
     A.error = path + ": cannot read the central directory";
@@ -378,14 +389,19 @@ bool open_archive(Archive &A, const std::string &path) {
       return false;
     }
     std::string fname((const char *)&cd[p + 46], nlen);
+    // names from the file go into error messages: printable ASCII only
+    for (char &ch : fname)
+      if (ch < 0x20 || ch > 0x7e) ch = '?';
     // zip64 extra field (id 1): the 64-bit values of the saturated fields, in order
-    for (size_t q = p + 46 + nlen; q + 4 <= p + 46 + nlen + xlen;) {
+    const size_t xend = p + 46 + nlen + xlen;  // inside cd, checked above
+    for (size_t q = p + 46 + nlen; q + 4 <= xend;) {
       const uint32_t id = get16(&cd[q]), len = get16(&cd[q + 2]);
+      const size_t fend = std::min(q + 4 + len, xend);
       if (id == 1) {
         size_t r = q + 4;
-        if (usize == 0xFFFFFFFFu && r + 8 <= q + 4 + len) usize = get64(&cd[r]), r += 8;
-        if (csize == 0xFFFFFFFFu && r + 8 <= q + 4 + len) csize = get64(&cd[r]), r += 8;
-        if (loff == 0xFFFFFFFFu && r + 8 <= q + 4 + len) loff = get64(&cd[r]), r += 8;
+        if (usize == 0xFFFFFFFFu && r + 8 <= fend) usize = get64(&cd[r]), r += 8;
+        if (csize == 0xFFFFFFFFu && r + 8 <= fend) csize = get64(&cd[r]), r += 8;
+        if (loff == 0xFFFFFFFFu && r + 8 <= fend) loff = get64(&cd[r]), r += 8;
       }
       q += 4 + len;
     }
@@ -394,6 +410,10 @@ bool open_archive(Archive &A, const std::string &path) {
     const std::string name = fname.substr(0, fname.size() - 4);
     if (method != 0 || csize != usize) {
       A.error = path + ": member " + fname + " is compressed; write snapshots with numpy.savez, not savez_compressed";
+      return false;
+    }
+    if (loff > (uint64_t)flen || usize > (uint64_t)flen) {
+      A.error = path + ": member " + fname + " lies outside the file";
       return false;
     }
     unsigned char lh[30];
@@ -437,7 +457,12 @@ bool read_scalar(Archive &A, const std::string &name, double *d, int64_t *i) {
   }
   unsigned char b[8] = {0};
   const std::string &t = ds->descr;
-  if (ds->n != 1 || t.size() != 3 || (t[0] != '<' && t[0] != '|') || !A.read_at(ds->data_off, b, t[2] - '0')) {
+  const bool known = t == "<f8" || t == "<i8" || t == "<u8" || t == "<i4" || t == "<u4";
+  if (!known) {
+    A.error = A.path + ": dataset \"" + name + "\" has unsupported type " + t;
+    return false;
+  }
+  if (ds->n != 1 || !A.read_at(ds->data_off, b, (size_t)(t[2] - '0'))) {
     A.error = A.path + ": dataset \"" + name + "\" is not a scalar";
     return false;
   }
@@ -445,13 +470,10 @@ bool read_scalar(Archive &A, const std::string &name, double *d, int64_t *i) {
     const double x = get_f64(b);
     if (d) *d = x;
     if (i) *i = (int64_t)x;
-  } else if (t == "<i8" || t == "<u8" || t == "<i4" || t == "<u4") {
+  } else {
     int64_t x = t[2] == '8' ? (int64_t)get64(b) : (t[1] == 'i' ? (int64_t)(int32_t)get32(b) : (int64_t)get32(b));
     if (d) *d = (double)x;
     if (i) *i = x;
-  } else {
-    A.error = A.path + ": dataset \"" + name + "\" has unsupported type " + t;
-    return false;
   }
   return true;
 }
@@ -481,16 +503,23 @@ extern "C" int zfvm_snapshot_write(const char *path, int64_t n_cells, const doub
 
 extern "C" int zfvm_snapshot_info(const char *path, int64_t *n_cells, int32_t *n_avars, int32_t *has_clock) {
   if (!path) return fail(ZFVM_EINVAL, "null argument");
+  try {
   Archive A;
   if (!open_archive(A, path)) return fail(ZFVM_EINVAL, A.error.empty() ? "cannot read " + A.path : A.error);
   const Dataset *rho = A.find("rho");
   if (!rho || rho->scalar) return fail(ZFVM_EINVAL, A.path + " has no dataset \"rho\"");
   int64_t na = 0;
   if (A.find("n_avars") && !read_scalar(A, "n_avars", nullptr, &na)) return fail(ZFVM_EINVAL, A.error);
+  if (na < 0 || na > (1 << 20)) return fail(ZFVM_EINVAL, A.path + ": bad n_avars");
   if (n_cells) *n_cells = (int64_t)rho->n;
   if (n_avars) *n_avars = (int32_t)na;
   if (has_clock) *has_clock = A.find("time") && A.find("n_steps");
   return ZFVM_OK;
+  } catch (const std::bad_alloc &) {
+    return fail(ZFVM_ENOMEM, "zfvm_snapshot_info: host allocation failed");
+  } catch (const std::exception &e) {
+    return fail(ZFVM_EINVAL, std::string("zfvm_snapshot_info: ") + e.what());
+  }
 }
 
 extern "C" int zfvm_snapshot_read(const char *path, int64_t n_cells, double *cvars, int32_t n_avars, double *avars,
