@@ -122,3 +122,23 @@ def test_rejects_bad_descriptions(zlib):
     assert e.value.code == 1
     with pytest.raises(z.ZfvmError):
         z.Mesh(raw, z.StencilSpec([3, 2], [0, 1], [2.0, 1.5]), quad=(3, 3, 1))
+
+
+def test_rejects_degenerate_cells(zlib):
+    """Cells that repeat a vertex (whose faces would match each other) or have
+    no volume, and non-finite coordinates, are refused with an error."""
+    z = zlib
+    raw = z.RawMesh.generate("periodic_square", n=4, halo=0, jitter=0.0, seed=1)
+    rep = z.RawMesh(raw.n_dims, raw.vertices, raw.vertex_indices.copy())
+    rep.vertex_indices[3, 2] = rep.vertex_indices[3, 0]
+    with pytest.raises(z.ZfvmError, match="repeats a vertex"):
+        z.Mesh(rep, z.StencilSpec.cweno(3, 2))
+    flat = z.RawMesh(raw.n_dims, raw.vertices.copy(), raw.vertex_indices.copy())
+    a, b, c = flat.vertex_indices[5]
+    flat.vertices[c] = 0.5 * (flat.vertices[a] + flat.vertices[b])  # collinear: zero area
+    with pytest.raises(z.ZfvmError, match="no volume"):
+        z.Mesh(flat, z.StencilSpec.cweno(3, 2))
+    nan = z.RawMesh(raw.n_dims, raw.vertices.copy(), raw.vertex_indices.copy())
+    nan.vertices[2, 0] = np.nan
+    with pytest.raises(z.ZfvmError, match="non-finite"):
+        z.Mesh(nan, z.StencilSpec.cweno(3, 2))

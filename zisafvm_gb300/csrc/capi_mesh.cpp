@@ -115,6 +115,14 @@ extern "C" int zfvm_mesh_create(const zfvm_mesh_desc *d, zfvm_mesh **out) {
   std::vector<index_t> vi(d->vertex_indices, d->vertex_indices + d->n_cells * nb);
   for (auto x : vi)
     if (x < 0 || x >= d->n_vertices) return fail(ZFVM_EINVAL, "vertex index out of range");
+  for (int64_t i = 0; i < d->n_cells; ++i)
+    for (int a = 0; a < nb; ++a)
+      for (int b = a + 1; b < nb; ++b)
+        if (vi[i * nb + a] == vi[i * nb + b])
+          return fail(ZFVM_EINVAL, "cell " + std::to_string(i) + " repeats a vertex");
+  for (const Vec3 &x : v)
+    if (!std::isfinite(x.x) || !std::isfinite(x.y) || !std::isfinite(x.z))
+      return fail(ZFVM_EINVAL, "non-finite vertex coordinate");
   auto m = std::make_unique<zfvm_mesh>();
   m->quad = {d->quad_edge, d->quad_volume, d->quad_moments};
   int max_order = 1;
@@ -131,6 +139,9 @@ extern "C" int zfvm_mesh_create(const zfvm_mesh_desc *d, zfvm_mesh **out) {
   auto secs = [](Clk::time_point a, Clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
   const auto t0 = Clk::now();
   m->grid = build_grid(d->n_dims, std::move(v), std::move(vi), m->quad);
+  for (int64_t i = 0; i < d->n_cells; ++i)
+    if (!(m->grid.volumes[i] > 0.0) || !std::isfinite(m->grid.volumes[i]))
+      return fail(ZFVM_EINVAL, "cell " + std::to_string(i) + " has no volume (degenerate or flat)");
   if (d->ghost) {
     std::vector<uint8_t> g(d->ghost, d->ghost + d->n_cells);
     mask_ghost_cells(m->grid, g);

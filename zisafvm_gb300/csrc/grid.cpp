@@ -248,7 +248,7 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
         int kj = -1;
         for (int l = 0; l < nb; ++l)
           if (g.neighbours[j * nb + l] == i) kj = l;
-        if (kj < 0) throw SetupError(1, "inconsistent neighbours");
+        if (kj < 0 || g.edge_indices[j * nb + kj] < 0) throw SetupError(1, "inconsistent neighbours");
         g.edge_indices[i * nb + k] = g.edge_indices[j * nb + kj];
       }
     }
