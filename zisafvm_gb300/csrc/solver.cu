@@ -572,6 +572,7 @@ int build_solver(zfvm_solver *s) {
     // FP32 copies: face frames, moments, scaled offsets of the quadrature points
     s->frame32.upload(std::vector<float>(h_frame.begin(), h_frame.end()));
     s->mom32.upload(std::vector<float>(h_mom.begin(), h_mom.end()));
+    s->fqw32.upload(std::vector<float>(h_fqw.begin(), h_fqw.end()));
     std::vector<float> hxf((size_t)nf * nqf * nd * ld, 0.f), hxc((size_t)nqc * nd * ld, 0.f);
     for (index_t i = 0; i < n; ++i) {
       const double il = 1.0 / g.char_length[i];
@@ -624,8 +625,10 @@ int build_solver(zfvm_solver *s) {
       };
       s->m1s.upload(pairs(h_phi_m1));
       s->vars.upload(pairs(h_phi_var));
-      s->eq32.alloc((size_t)3 * ld);
-      s->eq32.zero(s->stream);
+      // (h_r, f, K) pairs; K = -1 until a cell's equilibrium is found
+      std::vector<float2> h_eq((size_t)3 * ld, make_float2(0.f, 0.f));
+      for (size_t i = 2 * (size_t)ld; i < h_eq.size(); ++i) h_eq[i] = make_float2(-1.f, 0.f);
+      s->eq32.upload(h_eq);
       std::vector<float2> hp((size_t)nqf * lde, make_float2(0.f, 0.f));
       for (size_t k = 0; k < hp.size(); ++k) {
         const float hi = (float)h_phi_fq[k];
@@ -680,6 +683,7 @@ int build_solver(zfvm_solver *s) {
   D.xfq32 = s->xfq32.p;
   D.xcq32 = s->xcq32.p;
   D.mom32 = s->mom32.p;
+  D.fqw32 = s->fqw32.p;
   D.gphi_w = s->gphi_w.p;
   D.wg32 = s->wg32.p;
   D.m1s = s->m1s.p;
@@ -715,7 +719,7 @@ int build_solver(zfvm_solver *s) {
   add(s->flags.n + s->bloc.n + s->fkL.n + s->fkR.n + s->factive.n);
   add(4 * (s->l2g.n + s->cface.n + s->fL.n + s->fR.n + s->src_map.n));
   add(4 * (s->pinv32.n + s->fv32.n + s->frame32.n + s->xfq32.n + s->xcq32.n + s->mom32.n + s->wg32.n + s->g32.n +
-           s->mL32.n + s->mR32.n + s->src32.n + s->kbuf32.n));
+           s->mL32.n + s->mR32.n + s->src32.n + s->kbuf32.n + s->fqw32.n));
   add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n + s->eq32.n + s->phi_fq2.n));
   add(4 * s->dev032.n);
   add(8 * s->uprev.n);
@@ -1173,7 +1177,7 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
   if (sc.step_rejection_drho > 0.0) b += 8 * nv * ld;                            // uprev
   if (sc.heating_rate != 0.0 && has_src) b += 8 * nqc * ld;                       // heat_w
   if (mixed) {
-    b += 4 * (NP * ld + nd * nd * lde + NC * ld + nf * nqf * nd * ld + nqc * nd * ld);  // pinv32 frame32 mom32 xfq32 xcq32
+    b += 4 * (NP * ld + nd * nd * lde + NC * ld + nf * nqf * nd * ld + nqc * nd * ld + nqf * lde);  // pinv32 frame32 mom32 xfq32 xcq32 fqw32
     b += 4 * (nv * lde + 2 * nd * lde + kst * nv * ld + nf * nqf * nv * ld);          // g32 mL32 mR32 kbuf32 fv32
     b += 8 * nv * ld;                                                                   // dev0
     b += 8 * 2 * nv * ld + 4 * nv * ld;                                                 // qsplit dev032

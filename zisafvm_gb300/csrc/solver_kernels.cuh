@@ -139,6 +139,7 @@ struct DevData {
   const float *xfq32;    // [NF*NQF][ND][ld] scaled offsets (x - x_c) / l of the cell's face points
   const float *xcq32;    // [NQC][ND][ld] scaled offsets of the cell's quadrature points
   const float *mom32;    // [NC][ld]
+  const float *fqw32;    // [NQF][lde] face quadrature weights
   const double *gphi_w;  // [ND][ld] sum_q w_q grad phi(x_q) over the cell
   const float *wg32;     // [NQC][ND][ld] w_q grad phi(x_q)
   const float2 *m1s;     // [ld] phi_m1 as an FP32 (hi, lo) pair
@@ -564,7 +565,9 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       f_split = df_split(eqb.f);
       a.eq32[i] = make_float2(hr.hi, hr.lo);
       a.eq32[ld + i] = make_float2(f_split.hi, f_split.lo);
-      a.eq32[2 * ld + i] = make_float2(K.hi, K.lo);
+      // K > 0 whenever the equilibrium was found; -1 marks a cell without one,
+      // so the face kernel tells them apart with one FP32 comparison
+      a.eq32[2 * ld + i] = found ? make_float2(K.hi, K.lo) : make_float2(-1.f, 0.f);
     }
   }
   // dev_j - dev_0 for a stencil cell j.  In the mixed form with gamma = 2 the
@@ -1136,7 +1139,8 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         to_face<NV, ND>(uL, d.frame, lde, e, wL);
         to_face<NV, ND>(uR, d.frame, lde, e, wR);
         numerical_flux<NV, FLUX>(wL, wR, P.gamma, f);
-      } else if (EQ && eq_found(a, ld, L) && eq_found(a, ld, R)) {
+      } else if (EQ && (P.gamma2 ? (a.eq32[2 * ld + L].x >= 0.f && a.eq32[2 * ld + R].x >= 0.f)
+                                 : (eq_found(a, ld, L) && eq_found(a, ld, R)))) {
         // perturbation form around the left cell's equilibrium at the point:
         // F = (0, p_w n, 0) + [F32(w + dL, w + dR) - F32(w)] in the face frame
         // base w = the left equilibrium at the point; the right side carries
@@ -1179,7 +1183,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         }
         to_face32<NV, ND>(cL, d.frame32, lde, e, dL);
         to_face32<NV, ND>(cR, d.frame32, lde, e, dR);
-        const float gamma32 = float(P.gamma);
+        const float gamma32 = P.gamma32;
         if (FLUX == 0)
           hllc_flux_dev<NV>(dL, dR, rwL, EwL, gamma32, df);
         else
@@ -1187,7 +1191,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         from_face32<NV, ND>(df, d.frame32, lde, e);
         // the baseline p_wL n cancels the left cell's own surface source term
         // exactly; the right cell keeps (p_wL - p_eqR) n
-        const float wq = float(d.fqw[qq * lde + e]);
+        const float wq = d.fqw32[qq * lde + e];
         const float dpn = -dE * (gamma32 - 1.f) * wq;
 #pragma unroll
         for (int v = 0; v < NV; ++v) g32[v] += wq * df[v];
@@ -1204,9 +1208,9 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         }
         to_face32<NV, ND>(uL, d.frame32, lde, e, wL);
         to_face32<NV, ND>(uR, d.frame32, lde, e, wR);
-        numerical_flux<NV, FLUX>(wL, wR, float(P.gamma), f32);
+        numerical_flux<NV, FLUX>(wL, wR, P.gamma32, f32);
         from_face32<NV, ND>(f32, d.frame32, lde, e);
-        const float wq = float(d.fqw[qq * lde + e]);
+        const float wq = d.fqw32[qq * lde + e];
 #pragma unroll
         for (int v = 0; v < NV; ++v) g32[v] += wq * f32[v];
         continue;
@@ -1226,7 +1230,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
         numerical_flux<NV, FLUX>(wL, wR, P.gamma, f);
         // surface source terms of the sides that have an equilibrium
         double rq, Eq;
-        const float wq32 = float(d.fqw[qq * lde + e]);
+        const float wq32 = d.fqw32[qq * lde + e];
         if (eq_found(a, ld, L)) {
           eq_bound(a, ld, L).at(ev, phi, rq, Eq);
 #pragma unroll
