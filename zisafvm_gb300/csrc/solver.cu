@@ -12,7 +12,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -296,6 +298,8 @@ int build_solver(zfvm_solver *s) {
   s->nf = g.n_dims + 1;
   s->nqf = g.n_face_qp;
   s->nqc = g.n_cell_qp;
+  if (g.n_cells >= INT32_MAX / 64 || g.n_edges >= INT32_MAX / 64)
+    return fail(ZFVM_EINVAL, "mesh too large for one solver; split it into instances of a batch");
   s->n_cells = (int)g.n_cells;
   s->n_edges = (int)g.n_edges;
   s->ld = (int)((g.n_cells + 31) / 32 * 32);
@@ -331,6 +335,18 @@ int build_solver(zfvm_solver *s) {
     return fail(ZFVM_EINVAL, "unsupported stencil / quadrature shape for the GPU kernels");
   const int R0 = key.R0, C0 = key.C0, NB = key.NB, RB = key.RB, CB = key.CB;
   const int NC = std::max(C0, CB), NP = R0 * C0 + NB * RB * CB, MAXL = R0 + 1 + NB * RB;
+  // The kernels form 32-bit offsets row * ld + i into the per-cell tables (and
+  // row * lde + e into the per-face ones); the tallest per-cell table is the
+  // pseudo-inverses (NP rows) or the exported polynomial records.
+  {
+    const int64_t rows = std::max<int64_t>({(int64_t)NP, (int64_t)MAXL, (int64_t)nf * s->nqf * nv,
+                                            (int64_t)s->nqc * nd, (int64_t)nv + (int64_t)NC * nv + nd + NC + 6});
+    const int64_t face_rows = std::max<int64_t>({(int64_t)s->nqf * nd, (int64_t)nd * nd, (int64_t)nv});
+    if (rows * ld >= INT32_MAX || face_rows * lde >= INT32_MAX)
+      return fail(ZFVM_EINVAL, "mesh of " + std::to_string(g.n_cells) + " cells exceeds the kernels' 32-bit table offsets (" +
+                                   std::to_string(INT32_MAX / rows) + " cells at most for this stencil shape); "
+                                   "split it into instances of a batch");
+  }
 
   // ---- scheme parameters
   if (sc.rk_stages < 1 || sc.rk_stages > 3) return fail(ZFVM_EINVAL, "rk_stages must be 1, 2 or 3");
