@@ -298,7 +298,9 @@ int build_solver(zfvm_solver *s) {
   s->nf = g.n_dims + 1;
   s->nqf = g.n_face_qp;
   s->nqc = g.n_cell_qp;
-  if (g.n_cells >= INT32_MAX / 64 || g.n_edges >= INT32_MAX / 64)
+  // the counts and padded lengths below are ints; the table check further down
+  // sets the real limit
+  if (g.n_cells >= INT32_MAX - 64 || g.n_edges >= INT32_MAX - 64)
     return fail(ZFVM_EINVAL, "mesh too large for one solver; split it into instances of a batch");
   s->n_cells = (int)g.n_cells;
   s->n_edges = (int)g.n_edges;
