@@ -1,6 +1,8 @@
 """The C-ABI library loads and exports every entry point include/*.h declares."""
 import ctypes
 import re
+
+import pytest
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parent.parent
@@ -46,3 +48,28 @@ def test_solver_footprint_without_device(zlib):
     assert 0 < f32 < f64 < f64_big
     per_cell = f64_big / mesh2.n_cells
     assert 500 < per_cell < 5000
+
+
+def test_solver_validation_runs_before_cuda(zlib):
+    """zfvm_solver_create checks its configuration before any CUDA call:
+    invalid schemes are refused with ZFVM_EINVAL on any host; on a host
+    without a GPU a valid one gets as far as the first CUDA call."""
+    import sys
+    sys.path.insert(0, str(ROOT / "tests"))
+    from problems import polytrope_2d
+    from conftest import gpu_available
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=10)
+    bad = [dict(steps_per_recompute=2), dict(rk_stages=4), dict(reconstruction=7), dict(n_avars=-1),
+           dict(n_avars=1000), dict(heating_rate=1.0, gravity=z.GRAVITY_NONE, equilibrium=z.EQ_NONE,
+                                    flux_bc=z.FLUX_BC_NONE), dict(step_rejection_drho=-1.0)]
+    for change in bad:
+        sc = z.Scheme(**{**scheme.__dict__, **change})
+        with pytest.raises(z.ZfvmError) as e:
+            z.Solver(mesh, sc)
+        assert e.value.code == 1, (change, e.value)
+    if not gpu_available():
+        for prec in (z.FP64, z.MIXED):
+            with pytest.raises(z.ZfvmError) as e:
+                z.Solver(mesh, z.Scheme(**{**scheme.__dict__, "precision": prec}))
+            assert e.value.code == 6  # ZFVM_ECUDA: validation passed

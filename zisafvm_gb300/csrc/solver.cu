@@ -378,6 +378,7 @@ int build_solver(zfvm_solver *s) {
   P.inv_gm1 = 1.0 / (sc.gamma - 1.0);
   if (sc.reconstruction != ZFVM_RC_CWENO_AO && sc.reconstruction != ZFVM_RC_WENO_AO)
     return fail(ZFVM_EINVAL, "unknown reconstruction mode");
+  if (sc.step_rejection_drho < 0.0) return fail(ZFVM_EINVAL, "negative step_rejection_drho");
   if (sc.n_avars < 0 || sc.n_avars > ZFVM_MAX_AVARS)
     return fail(ZFVM_EINVAL, "n_avars must be 0 .. " + std::to_string(ZFVM_MAX_AVARS));
   s->na = sc.n_avars;
@@ -662,7 +663,6 @@ int build_solver(zfvm_solver *s) {
   if (!s->mixed) s->nfb.alloc((size_t)nv * lde);
   s->tend.alloc((size_t)nv * ld);
   s->aos.alloc((size_t)5 * n);
-  if (sc.step_rejection_drho < 0.0) return fail(ZFVM_EINVAL, "negative step_rejection_drho");
   if (sc.step_rejection_drho > 0.0) {
     s->uprev.alloc((size_t)nv * ld);
     s->uprev.zero(s->stream);
