@@ -811,15 +811,7 @@ extern "C" int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *sc, zfvm
 }
 
 extern "C" int zfvm_solver_destroy(zfvm_solver *s) {
-  if (!s) return ZFVM_OK;
-  if (s->graph) cudaGraphExecDestroy(s->graph);
-  if (s->stream) {
-    cudaStreamSynchronize(s->stream);
-    cudaStreamDestroy(s->stream);
-  }
-  if (s->ev_in) cudaEventDestroy(s->ev_in);
-  if (s->ev_sync) cudaEventDestroy(s->ev_sync);
-  delete s;
+  delete s;  // ~zfvm_solver waits for the solver's stream, then frees everything
   return ZFVM_OK;
 }
 

@@ -98,6 +98,20 @@ struct zfvm_solver {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   int64_t device_bytes = 0;
+  zfvm_solver() = default;
+  zfvm_solver(const zfvm_solver &) = delete;
+  zfvm_solver &operator=(const zfvm_solver &) = delete;
+  // Also runs when zfvm_solver_create fails part-way: the work on the stream
+  // ends before the buffers (members, freed after this body) go away.
+  ~zfvm_solver() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_sync) cudaEventDestroy(ev_sync);
+  }
 };
 
 
