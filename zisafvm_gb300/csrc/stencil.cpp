@@ -197,31 +197,51 @@ struct Region {
 };
 
 // Open-addressing set of cell ids for one candidate search (a few hundred
-// entries at most); grows by rehashing if a search ever exceeds it.
+// entries at most).  The table is per thread and reused: a slot belongs to the
+// current search when its stamp equals the search's epoch, so a new search
+// clears nothing.  It grows by rehashing if a search ever fills half of it.
 struct SmallSet {
-  std::vector<index_t> slot = std::vector<index_t>(1024, -1);
+  struct Table {
+    std::vector<index_t> key = std::vector<index_t>(1024, -1);
+    std::vector<uint32_t> stamp = std::vector<uint32_t>(1024, 0);
+    uint32_t epoch = 0;
+  };
+  Table &t;
   size_t count = 0;
+  static Table &table() {
+    static thread_local Table tab;
+    return tab;
+  }
+  SmallSet() : t(table()) {
+    if (++t.epoch == 0) {  // stamps wrapped: start over
+      std::fill(t.stamp.begin(), t.stamp.end(), 0u);
+      t.epoch = 1;
+    }
+  }
   static size_t hash(index_t c) { return (size_t)((uint64_t)c * 0x9E3779B97F4A7C15ull >> 20); }
   bool contains(index_t c) const {
-    const size_t mask = slot.size() - 1;
+    const size_t mask = t.key.size() - 1;
     for (size_t h = hash(c) & mask;; h = (h + 1) & mask) {
-      if (slot[h] == c) return true;
-      if (slot[h] < 0) return false;
+      if (t.stamp[h] != t.epoch) return false;
+      if (t.key[h] == c) return true;
     }
   }
   void insert(index_t c) {
-    if (2 * (count + 1) > slot.size()) {
-      std::vector<index_t> old;
-      old.swap(slot);
-      slot.assign(2 * old.size(), -1);
-      count = 0;
-      for (index_t x : old)
-        if (x >= 0) insert(x);
-    }
-    const size_t mask = slot.size() - 1;
+    if (2 * (count + 1) > t.key.size()) grow();
+    const size_t mask = t.key.size() - 1;
     size_t h = hash(c) & mask;
-    while (slot[h] >= 0 && slot[h] != c) h = (h + 1) & mask;
-    if (slot[h] < 0) slot[h] = c, ++count;
+    while (t.stamp[h] == t.epoch && t.key[h] != c) h = (h + 1) & mask;
+    if (t.stamp[h] != t.epoch) t.stamp[h] = t.epoch, t.key[h] = c, ++count;
+  }
+  void grow() {
+    std::vector<index_t> live;
+    for (size_t h = 0; h < t.key.size(); ++h)
+      if (t.stamp[h] == t.epoch) live.push_back(t.key[h]);
+    t.key.assign(2 * t.key.size(), -1);
+    t.stamp.assign(t.key.size(), 0u);
+    t.epoch = 1;
+    count = 0;
+    for (index_t x : live) insert(x);
   }
 };
 
@@ -251,7 +271,9 @@ struct Selector {
   // candidate?" in O(1) instead of a scan of the list.
   std::vector<index_t> candidates(index_t i, index_t n_points, const Region &reg) const {
     index_t max_points = 5 * n_points;
-    std::vector<index_t> cand{i};
+    std::vector<index_t> cand;
+    cand.reserve((size_t)(max_points + 1) * g.max_nb);
+    cand.push_back(i);
     SmallSet seen;
     seen.insert(i);
     for (index_t p = 0; p < max_points; ++p) {
