@@ -295,17 +295,16 @@ struct Selector {
     auto cand = candidates(i, n_points, reg);
     const Vec3 xc = g.cell_centers[i];
     // std::sort by distance in the reference; ties broken by candidate order
-    // here.  The distances are computed once, not in every comparison.
+    // here, so the key is (distance, position in the candidate list), a total
+    // order.  The distances are computed once, not in every comparison, and
+    // only the nearest n_points are ordered.
     std::vector<std::pair<double, index_t>> key(cand.size());
-    for (size_t r = 0; r < cand.size(); ++r) key[r] = {norm(g.cell_centers[cand[r]] - xc), cand[r]};
-    std::stable_sort(key.begin(), key.end(),
-                     [](const std::pair<double, index_t> &a, const std::pair<double, index_t> &b) {
-                       return a.first < b.first;
-                     });
+    for (size_t r = 0; r < cand.size(); ++r) key[r] = {norm(g.cell_centers[cand[r]] - xc), (index_t)r};
     const size_t keep = std::min(cand.size(), (size_t)n_points);
-    cand.resize(keep);
-    for (size_t r = 0; r < keep; ++r) cand[r] = key[r].second;
-    return cand;
+    std::partial_sort(key.begin(), key.begin() + keep, key.end());
+    std::vector<index_t> out(keep);
+    for (size_t r = 0; r < keep; ++r) out[r] = cand[key[r].second];
+    return out;
   }
 
   Region cone(index_t i, const Vec3 &apex, int k) const {
