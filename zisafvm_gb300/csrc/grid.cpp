@@ -4,6 +4,9 @@
 #include "grid.hpp"
 
 #include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <map>
 
 namespace zfvm {
@@ -181,90 +184,167 @@ Grid build_grid(int n_dims, std::vector<Vec3> vertices, std::vector<index_t> vi,
     }
   }
 
-  // neighbours across each face: every (cell, local face) goes into an
-  // open-addressing table keyed by the face's sorted vertex ids, in cell order;
-  // a face meets the first earlier unmatched entry with the same vertices
-  // (consumed entries stay as tombstones, so equal keys are met in insertion
-  // order)
+  // neighbours across each face: every (cell, local face) is keyed by the
+  // face's sorted vertex ids; a face meets the earlier unmatched entry with
+  // the same vertices, if there is one, else waits for a later one (so with
+  // more than two equal faces, consecutive ones pair up in cell order).  The
+  // entries are split by hash into buckets, each matched on its own in cell
+  // order by an open-addressing table with tombstones for consumed entries;
+  // equal faces share a bucket, so the pairing is the serial one.
   g.neighbours.assign(n * nb, -1);
   {
     const int fv = n_dims;  // vertices per face
     auto sorted_face = [&](index_t i, int k, index_t *a) {
       for (int r = 0; r < fv; ++r) a[r] = g.vertex_indices[i * nb + face_vertex(n_dims, k, r)];
-      std::sort(a, a + fv);
+      if (a[0] > a[1]) std::swap(a[0], a[1]);
+      if (fv == 3) {
+        if (a[1] > a[2]) std::swap(a[1], a[2]);
+        if (a[0] > a[1]) std::swap(a[0], a[1]);
+      }
     };
-    size_t cap = 16;
-    while (cap < 2 * (size_t)(n * nb)) cap <<= 1;
-    const size_t mask = cap - 1;
-    constexpr int64_t kEmpty = -1, kConsumed = -2;
-    std::vector<int64_t> table(cap, kEmpty);  // i * nb + k of a face still waiting for its partner
+    const index_t total = n * nb;
+    std::vector<uint64_t> hv(total);
+#pragma omp parallel for schedule(static)
     for (index_t i = 0; i < n; ++i)
       for (int k = 0; k < nb; ++k) {
-        index_t a[3];
+        index_t a[3] = {0, 0, 0};
         sorted_face(i, k, a);
         uint64_t h = 1469598103934665603ull;
         for (int r = 0; r < fv; ++r) h = (h ^ (uint64_t)a[r]) * 1099511628211ull;
-        for (size_t s = (size_t)(h ^ (h >> 29)) & mask;; s = (s + 1) & mask) {
-          const int64_t e = table[s];
-          if (e == kEmpty) {
-            table[s] = i * nb + k;
-            break;
+        hv[i * nb + k] = h;
+      }
+    constexpr int kBucketBits = 10, kBuckets = 1 << kBucketBits;
+    auto bucket_of = [](uint64_t h) { return (int)((h * 0x9E3779B97F4A7C15ull) >> (64 - kBucketBits)); };
+    // stable counting sort of the entries by bucket
+    std::vector<index_t> order(total), start(kBuckets + 1, 0);
+    int max_threads = 1;
+#ifdef _OPENMP
+    max_threads = omp_get_max_threads();
+#endif
+    std::vector<index_t> cnt((size_t)max_threads * kBuckets, 0);
+#pragma omp parallel
+    {
+      int t = 0, T = 1;
+#ifdef _OPENMP
+      t = omp_get_thread_num(), T = omp_get_num_threads();
+#endif
+      const index_t lo = total * t / T, hi = total * (t + 1) / T;
+      index_t *c = &cnt[(size_t)t * kBuckets];
+      for (index_t e = lo; e < hi; ++e) ++c[bucket_of(hv[e])];
+#pragma omp barrier
+#pragma omp single
+      {
+        index_t off = 0;
+        for (int b = 0; b < kBuckets; ++b) {
+          start[b] = off;
+          for (int u = 0; u < T; ++u) {
+            const index_t m = cnt[(size_t)u * kBuckets + b];
+            cnt[(size_t)u * kBuckets + b] = off;
+            off += m;
           }
-          if (e == kConsumed) continue;
-          index_t b[3];
-          const index_t j = e / nb;
-          const int l = (int)(e % nb);
-          sorted_face(j, l, b);
-          bool same = true;
-          for (int r = 0; r < fv; ++r) same = same && a[r] == b[r];
-          if (same) {
-            g.neighbours[i * nb + k] = j;
-            g.neighbours[j * nb + l] = i;
-            table[s] = kConsumed;
-            break;
+        }
+        start[kBuckets] = off;
+      }
+      for (index_t e = lo; e < hi; ++e) order[c[bucket_of(hv[e])]++] = e;
+    }
+    constexpr int64_t kEmpty = -1, kConsumed = -2;
+#pragma omp parallel
+    {
+      std::vector<int64_t> table;  // entry i * nb + k of a face still waiting for its partner
+#pragma omp for schedule(dynamic, 8)
+      for (int bk = 0; bk < kBuckets; ++bk) {
+        size_t cap = 16;
+        while (cap < 2 * (size_t)(start[bk + 1] - start[bk])) cap <<= 1;
+        const size_t mask = cap - 1;
+        table.assign(cap, kEmpty);
+        for (index_t o = start[bk]; o < start[bk + 1]; ++o) {
+          const index_t ent = order[o];
+          const index_t i = ent / nb;
+          const int k = (int)(ent % nb);
+          index_t a[3] = {0, 0, 0};
+          sorted_face(i, k, a);
+          const uint64_t h = hv[ent];
+          for (size_t s = (size_t)(h ^ (h >> 29)) & mask;; s = (s + 1) & mask) {
+            const int64_t e = table[s];
+            if (e == kEmpty) {
+              table[s] = ent;
+              break;
+            }
+            if (e == kConsumed || hv[e] != h) continue;
+            index_t b[3] = {0, 0, 0};
+            const index_t j = e / nb;
+            const int l = (int)(e % nb);
+            sorted_face(j, l, b);
+            bool same = true;
+            for (int r = 0; r < fv; ++r) same = same && a[r] == b[r];
+            if (same) {
+              g.neighbours[i * nb + k] = j;
+              g.neighbours[j * nb + l] = i;
+              table[s] = kConsumed;
+              break;
+            }
           }
         }
       }
+    }
   }
 
-  // interior-first edge numbering (grid/grid.cpp:385-413)
-  index_t n_int = 0;
-  for (index_t i = 0; i < n; ++i)
-    for (int k = 0; k < nb; ++k) {
-      index_t j = g.neighbours[i * nb + k];
-      if (j >= 0 && i < j) ++n_int;
+  // interior-first edge numbering (grid/grid.cpp:385-413): interior faces in
+  // the order of their lower cell, then boundary faces in cell order; the
+  // numbers come from per-cell prefix counts, so every cell is numbered on
+  // its own
+  {
+    std::vector<index_t> int_off(n + 1, 0), ext_off(n + 1, 0);
+#pragma omp parallel for schedule(static)
+    for (index_t i = 0; i < n; ++i) {
+      index_t ni = 0, ne = 0;
+      for (int k = 0; k < nb; ++k) {
+        const index_t j = g.neighbours[i * nb + k];
+        ni += (j >= 0 && i < j);
+        ne += (j < 0);
+      }
+      int_off[i + 1] = ni;
+      ext_off[i + 1] = ne;
     }
-  g.n_interior_edges = n_int;
-  g.edge_indices.assign(n * nb, -1);
-  index_t next_int = 0, next_ext = n_int;
-  for (index_t i = 0; i < n; ++i)
-    for (int k = 0; k < nb; ++k) {
-      index_t j = g.neighbours[i * nb + k];
-      if (j < 0) {
-        g.edge_indices[i * nb + k] = next_ext++;
-      } else if (i < j) {
-        g.edge_indices[i * nb + k] = next_int++;
-      } else {
+    for (index_t i = 0; i < n; ++i) int_off[i + 1] += int_off[i], ext_off[i + 1] += ext_off[i];
+    const index_t n_int = int_off[n];
+    g.n_interior_edges = n_int;
+    g.n_edges = n_int + ext_off[n];
+    g.edge_indices.assign(n * nb, -1);
+    g.left.assign(g.n_edges, -1);
+    g.right.assign(g.n_edges, -1);
+#pragma omp parallel for schedule(static)
+    for (index_t i = 0; i < n; ++i) {
+      index_t next_int = int_off[i], next_ext = n_int + ext_off[i];
+      for (int k = 0; k < nb; ++k) {
+        const index_t j = g.neighbours[i * nb + k];
+        if (j < 0) {
+          g.edge_indices[i * nb + k] = next_ext;
+          g.left[next_ext++] = i;
+        } else if (i < j) {
+          g.edge_indices[i * nb + k] = next_int;
+          g.left[next_int] = i;
+          g.right[next_int++] = j;
+        }
+      }
+    }
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (index_t i = 0; i < n; ++i)
+      for (int k = 0; k < nb; ++k) {
+        const index_t j = g.neighbours[i * nb + k];
+        if (j < 0 || i < j) continue;
         int kj = -1;
         for (int l = 0; l < nb; ++l)
           if (g.neighbours[j * nb + l] == i) kj = l;
-        if (kj < 0 || g.edge_indices[j * nb + kj] < 0) throw SetupError(1, "inconsistent neighbours");
+        if (kj < 0 || g.edge_indices[j * nb + kj] < 0) {
+          bad = 1;
+          continue;
+        }
         g.edge_indices[i * nb + k] = g.edge_indices[j * nb + kj];
       }
-    }
-  g.n_edges = next_ext;
-  g.left.assign(g.n_edges, -1);
-  g.right.assign(g.n_edges, -1);
-  for (index_t i = 0; i < n; ++i)
-    for (int k = 0; k < nb; ++k) {
-      index_t e = g.edge_indices[i * nb + k], j = g.neighbours[i * nb + k];
-      if (j < 0) {
-        g.left[e] = i;
-      } else if (i < j) {
-        g.left[e] = i;
-        g.right[e] = j;
-      }
-    }
+    if (bad) throw SetupError(1, "inconsistent neighbours");
+  }
 
   // cell measures
   g.volumes.resize(n);
