@@ -142,3 +142,49 @@ def test_rejects_degenerate_cells(zlib):
     nan.vertices[2, 0] = np.nan
     with pytest.raises(z.ZfvmError, match="non-finite"):
         z.Mesh(nan, z.StencilSpec.cweno(3, 2))
+
+
+_SETUP_DIGEST = r"""
+import hashlib, sys
+import numpy as np
+import zisafvm_gb300 as z
+h = hashlib.sha256()
+cases = [("cube", dict(n=6, jitter=0.1, seed=2), 3, (2, 2, 2)),
+         ("cube", dict(n=5, jitter=0.0, seed=1), 3, (2, 2, 2)),
+         ("disk", dict(n=14, radius=1.0, jitter=0.2, seed=3), 3, (3, 3, 2)),
+         ("periodic_square", dict(n=10, halo=3, jitter=0.0, seed=1), 3, (3, 3, 2))]
+for kind, kw, order, quad in cases:
+    raw = z.RawMesh.generate(kind, **kw)
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(order, raw.n_dims), quad=quad)
+    info = mesh.info
+    h.update(repr([info["n_cells"], info["n_edges"], info["n_interior_edges"]]).encode())
+    for v in mesh.geometry().values():
+        h.update(np.ascontiguousarray(v).tobytes())
+    st = mesh.stencils()
+    for k in sorted(st):
+        h.update(st[k].tobytes())
+    for i in range(mesh.n_cells):
+        for s in range(int(st["n_stencils"][i])):
+            if st["order"][i, s] >= 2:
+                h.update(mesh.pinv(i, s).tobytes())
+print(h.hexdigest())
+"""
+
+
+def test_setup_does_not_depend_on_the_thread_count(zlib):
+    """The set-up runs its per-cell and per-face loops with OpenMP (face
+    matching in hash buckets, edge numbers from prefix counts, stencils and
+    pseudo-inverses per cell): geometry, neighbours, stencils and operators
+    must be bit for bit the same on one thread and on several."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    digests = []
+    for threads in ("1", "5"):
+        env = dict(os.environ, OMP_NUM_THREADS=threads, PYTHONPATH=root)
+        out = subprocess.run([sys.executable, "-c", _SETUP_DIGEST], env=env, cwd=root,
+                             capture_output=True, text=True, timeout=300)
+        assert out.returncode == 0, out.stderr
+        digests.append(out.stdout.strip())
+    assert len(digests[0]) == 64 and digests[0] == digests[1]
