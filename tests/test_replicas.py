@@ -36,7 +36,7 @@ def _reduce_worker(rank, world, port, out):
 
 def test_max_and_sum_over_two_ranks():
     port = _free_port()
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_reduce_worker, args=(2, port, out), nprocs=2, join=True, start_method="spawn")
         assert out[0] == out[1] == (20.0, 3.0)
