@@ -253,8 +253,10 @@ int zfvm_step(zfvm_solver *s, double dt);
  * TimeLoop::reject_step time_loop.cpp:182-198): with step_rejection_drho > 0, a
  * step whose density changes anywhere by more than drho * rho is redone from its
  * start with half the time step; two accepted steps in a row double the factor
- * again (at most 1, at least 2^-max_exponent).  Applies to zfvm_advance; not
- * available in batches. */
+ * again (at most 1, at least 2^-max_exponent).  Applies to zfvm_advance and to
+ * batch slots (a slot steps on the solver's own clock, so the count of a batched
+ * run is read from the solver after zfvm_batch_remove); counted since the state
+ * was last set (zfvm_set_state, zfvm_step_host, a snapshot read). */
 int zfvm_step_rejections(zfvm_solver *s, int64_t *n);
 
 /* TimeLoop (fvm_loops/time_loop.cpp:36-81) without IO: steps with the CFL time
