@@ -334,7 +334,8 @@ int zfvm_server_create(const zfvm_server_desc *desc, zfvm_server **out);
 int zfvm_server_destroy(zfvm_server *srv);
 /* Queue a solve of `mesh` (kept alive by the caller until the request is
  * waited for) from cvars (n_cells x 5, copied) at time t0 until n_steps steps
- * (if > 0) or time t_end (if > t0).  ZFVM_ENOMEM if its footprint exceeds the budget. */
+ * (if > 0) or time t_end (if > t0).  ZFVM_ENOMEM if its footprint exceeds the budget;
+ * ZFVM_EINVAL for a scheme with n_avars > 0 (requests carry conserved variables only). */
 int zfvm_server_submit(zfvm_server *srv, zfvm_mesh *mesh, const zfvm_scheme_desc *scheme, const double *cvars,
                        double t0, int64_t n_steps, double t_end, int64_t *id);
 /* phase: 0 queued, 1 running, 2 done, 3 failed */
