@@ -44,8 +44,9 @@ def test_mixed_rate_of_change_matches_fp64(zlib):
     s64, s32 = _pair(mesh, scheme, u0)
     t64, t32 = s64.rate_of_change(), s32.rate_of_change()
     inner = raw.ghost == 0
-    err = np.abs(t32[inner] - t64[inner]).max(axis=0) / np.abs(t64[inner]).max(axis=0)
-    assert np.nanmax(err[[0, 1, 2, 4]]) < 1e-5, err
+    cols = [0, 1, 2, 4]  # the 2D state has no third momentum
+    err = np.abs(t32[inner][:, cols] - t64[inner][:, cols]).max(axis=0) / np.abs(t64[inner][:, cols]).max(axis=0)
+    assert err.max() < 1e-5, err
 
 
 def test_mixed_well_balanced(zlib):
