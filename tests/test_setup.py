@@ -188,3 +188,38 @@ def test_setup_does_not_depend_on_the_thread_count(zlib):
         assert out.returncode == 0, out.stderr
         digests.append(out.stdout.strip())
     assert len(digests[0]) == 64 and digests[0] == digests[1]
+
+
+def test_small_and_empty_meshes(zlib):
+    """Meshes too small for the requested stencils fall back to lower orders
+    (deduce_max_order, stencil_family.cpp; order 1 when a one-sided region
+    holds too few cells), the central stencil stays the highest-order one, and
+    every stencil index is a cell of the mesh; an empty mesh is refused."""
+    z = zlib
+    cases = [("disk", dict(n=2, radius=1.0)), ("cube", dict(n=1)), ("periodic_square", dict(n=2, halo=1))]
+    for kind, kw in cases:
+        raw = z.RawMesh.generate(kind, jitter=0.0, seed=1, **kw)
+        mesh = z.Mesh(raw, z.StencilSpec.cweno(3, raw.n_dims), quad=(3, 3, 2) if raw.n_dims == 2 else (2, 2, 2))
+        st = mesh.stencils()
+        n = raw.n_cells
+        ns = int(st["n_stencils"].max())
+        assert st["order"][:, :ns].min() >= 1 and np.all(st["k_high"] == 0)
+        assert np.all(st["order"][:, 0] >= st["order"][:, 1:ns].max(axis=1))
+        for i in range(n):
+            l2g = st["l2g"][i, :st["n_l2g"][i]]
+            assert l2g[0] == i and np.all((l2g >= 0) & (l2g < n)) and len(set(l2g)) == len(l2g)
+            for k in range(int(st["n_stencils"][i])):
+                if st["order"][i, k] >= 2:
+                    P = mesh.pinv(i, k)
+                    assert P.shape[1] == st["size"][i, k] - 1 and np.all(np.isfinite(P))
+    # the six tetrahedra of one cube: too few cells for any linear fit
+    raw = z.RawMesh.generate("cube", n=1, jitter=0.0, seed=1)
+    st = z.Mesh(raw, z.StencilSpec.cweno(3, 3), quad=(2, 2, 2)).stencils()
+    assert np.all(st["order"][:, :5] == 1)
+    # one triangle: every stencil is the cell itself
+    one = z.RawMesh(2, np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]]), np.array([[0, 1, 2]], np.int64))
+    st = z.Mesh(one, z.StencilSpec.cweno(3, 2)).stencils()
+    assert st["n_l2g"][0] == 1 and np.all(st["order"][0, :4] == 1)
+    empty = z.RawMesh(2, np.zeros((0, 3)), np.zeros((0, 3), np.int64))
+    with pytest.raises(z.ZfvmError, match="empty"):
+        z.Mesh(empty, z.StencilSpec.cweno(3, 2))
