@@ -46,6 +46,8 @@ def lib() -> C.CDLL:
         L.zfvm_oracle_equilibrium_average.argtypes = [C.c_double, C.c_int, C.c_double, dp, dp, dp, C.c_int, dp]
         L.zfvm_oracle_rk_ode_error.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double]
         L.zfvm_oracle_rk_ode_error.restype = C.c_double
+        L.zfvm_oracle_eos_roundtrips.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, dp]
+        L.zfvm_oracle_quasi_newton_problem.argtypes = [C.c_int, dp]
         L.zfvm_oracle_last_error.restype = C.c_char_p
         _LIB = L
     return _LIB
@@ -203,3 +205,17 @@ def equilibrium_average(gamma, gravity_kind, g, theta, x_ref, tri, quad_deg):
 
 def rk_ode_error(stages: int, ode: int, dt: float, t_final: float = 3.0) -> float:
     return lib().zfvm_oracle_rk_ode_error(stages, ode, dt, t_final)
+
+
+def eos_roundtrips(gamma: float, R: float, rho: float, E: float) -> np.ndarray:
+    """(rho, E) through (h, K) and back, and through (rho, p) and back: 2 x 2."""
+    out = np.zeros(4)
+    _check(lib().zfvm_oracle_eos_roundtrips(gamma, R, rho, E, _dp(out)))
+    return out.reshape(2, 2)
+
+
+def quasi_newton_problem(which: int):
+    """The oracle's quasi_newton on a known problem: (solution, status)."""
+    x = np.zeros(2)
+    st = lib().zfvm_oracle_quasi_newton_problem(which, _dp(x))
+    return (x[:1] if which == 0 else x), st

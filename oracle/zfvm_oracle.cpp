@@ -45,7 +45,6 @@ struct XYZ {
 static XYZ operator+(const XYZ &a, const XYZ &b) { return {{a[0] + b[0], a[1] + b[1], a[2] + b[2]}}; }
 static XYZ operator-(const XYZ &a, const XYZ &b) { return {{a[0] - b[0], a[1] - b[1], a[2] - b[2]}}; }
 static XYZ operator*(double s, const XYZ &a) { return {{s * a[0], s * a[1], s * a[2]}}; }
-static XYZ operator*(const XYZ &a, double s) { return {{a[0] * s, a[1] * s, a[2] * s}}; }
 static XYZ operator/(const XYZ &a, double s) { return {{a[0] / s, a[1] / s, a[2] / s}}; }
 static double dot(const XYZ &a, const XYZ &b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 static double norm(const XYZ &a) { return std::sqrt(dot(a, a)); }
@@ -330,6 +329,14 @@ struct EOS {
     double base = 1.0 / K * (gamma - 1.0) / gamma * h;
     return std::pow(base, 1.0 / (gamma - 1.0));
   }
+  // enthalpy_entropy(RhoE) via rhoP(RhoE) (ideal_gas_eos.hpp:74-76,131-133,146-160):
+  // h = gamma / (gamma - 1) p / rho, K = p / rho^gamma
+  std::array<double, 2> hK_rhoE(const RhoE &r) const {
+    double p = pressure_rhoE(r[1]);
+    return {gamma / (gamma - 1.0) * p / r[0], p / std::pow(r[0], gamma)};
+  }
+  // rhoE(RhoP) (ideal_gas_eos.hpp:104-106): E = p / (gamma - 1)
+  RhoE rhoE_rhoP(double rho, double p) const { return {rho, p / (gamma - 1.0)}; }
   // rhoE(EnthalpyEntropy)  (ideal_gas_eos.hpp:86-91,162-168,184-187)
   RhoE rhoE_hK(double h, double K) const {
     double rho = rho_hK(h, K);
@@ -446,8 +453,59 @@ struct Gravity {
   }
 };
 
+// quasi_newton (math/quasi_newton.hpp:12-50): x -= inv_df(x)(f(x)) until every
+// |dx_k| <= atol_k, at most max_iter steps.  From the fifth step on, the step
+// must be converging in the sense of RollingConvergenceRate::is_converging(0)
+// (math/rolling_convergence_rate.hpp): the last step within atol (compared
+// signed, as there), or every component's rate log(|c| / |b|) / log(|b| / |a|)
+// over the last three steps at least 0.  Returns 0 when converged; 2 when not
+// converging (the reference logs an error); 1 when max_iter steps end more than
+// 1000 atol away (the reference warns).  On 1 and 2, x is put back to its start.
+template <size_t N, class F, class IDF>
+static int quasi_newton(const F &f, const IDF &inv_df, std::array<double, N> &x, const std::array<double, N> &atol,
+                        int max_iter = 20) {
+  const std::array<double, N> x0 = x;
+  std::array<double, N> fx = f(x), dx;
+  for (size_t k = 0; k < N; ++k) dx[k] = 2.0 * atol[k] + 1.0;
+  auto within = [&](double factor) {
+    for (size_t k = 0; k < N; ++k)
+      if (!(std::fabs(dx[k]) <= factor * atol[k])) return false;
+    return true;
+  };
+  std::vector<std::array<double, N>> hist;
+  int iter = 0;
+  while (!within(1.0) && iter < max_iter) {
+    dx = inv_df(x, fx);
+    for (size_t k = 0; k < N; ++k) x[k] -= dx[k];
+    fx = f(x);
+    hist.push_back(dx);
+    if (iter >= 4) {
+      const auto &a = hist[hist.size() - 3], &b = hist[hist.size() - 2], &c = hist[hist.size() - 1];
+      bool conv = true;
+      for (size_t k = 0; k < N; ++k) conv = conv && c[k] <= atol[k];
+      if (!conv) {
+        bool ok = true;
+        for (size_t k = 0; k < N; ++k) {
+          double r = std::log(std::fabs(c[k]) / std::fabs(b[k])) / std::log(std::fabs(b[k]) / std::fabs(a[k]));
+          ok = ok && r >= 0.0;
+        }
+        if (!ok) {
+          x = x0;
+          return 2;
+        }
+      }
+    }
+    ++iter;
+  }
+  if (iter == max_iter && !within(1000.0)) {
+    x = x0;
+    return 1;
+  }
+  return 0;
+}
+
 // IsentropicEquilibrium + LocalEquilibriumBase (model/isentropic_equilibrium.hpp,
-// local_equilibrium_impl.hpp:40-94,160-186) and quasi_newton (math/quasi_newton.hpp).
+// local_equilibrium_impl.hpp:40-94,160-186), solved by quasi_newton.
 struct LocalEq {
   const EOS *eos = nullptr;
   const Gravity *grav = nullptr;
@@ -476,61 +534,29 @@ struct LocalEq {
   // returns 0 ok, 1 not found (warning), 2 diverging (the reference aborts)
   int solve(const RhoE &rbar, const QR &cell) {
     x_ref = cell.x[0];
-    double p = eos->pressure_rhoE(rbar[1]);
-    double h0 = eos->gamma / (eos->gamma - 1.0) * p / rbar[0];
-    double K0 = p / std::pow(rbar[0], eos->gamma);
-    auto f = [&](double hh, double KK) {
-      RhoE avg = average<RhoE>(cell, [&](const XYZ &x) { return extrapolate_theta(hh, KK, x_ref, x); });
+    const auto guess = eos->hK_rhoE(rbar);  // full_extra_variables(rhoE_bar): (h, s)
+    auto f = [&](const std::array<double, 2> &t) {
+      RhoE avg = average<RhoE>(cell, [&](const XYZ &x) { return extrapolate_theta(t[0], t[1], x_ref, x); });
       return RhoE{rbar[0] - avg[0], rbar[1] - avg[1]};
     };
-    double atol[2] = {1e-13 * h0, 1e-13 * K0};
-    double x[2] = {h0, K0};
-    RhoE fx = f(x[0], x[1]);
-    double dx[2] = {2.0 * atol[0] + 1.0, 2.0 * atol[1] + 1.0};
-    std::vector<std::array<double, 2>> hist;
-    int iter = 0;
-    int status = 0;
-    while (!(std::fabs(dx[0]) <= atol[0] && std::fabs(dx[1]) <= atol[1]) && iter < 20) {
+    // central differences of f with step 1e-6 |x_dir|, and the 2 x 2 inverse
+    auto inv_df = [&](const std::array<double, 2> &x, const RhoE &fx) {
       double df[2][2];
       for (int dir = 0; dir < 2; ++dir) {
         double eps = 1e-6 * std::fabs(x[dir]);
-        double xp[2] = {x[0], x[1]}, xm[2] = {x[0], x[1]};
+        std::array<double, 2> xp = x, xm = x;
         xp[dir] = x[dir] + 0.5 * eps * 1.0;
         xm[dir] = x[dir] - 0.5 * eps * 1.0;
-        RhoE a = f(xp[0], xp[1]), b = f(xm[0], xm[1]);
+        RhoE a = f(xp), b = f(xm);
         df[dir][0] = (a[0] - b[0]) / eps;
         df[dir][1] = (a[1] - b[1]) / eps;
       }
       double inv_det = 1.0 / (df[0][0] * df[1][1] - df[0][1] * df[1][0]);
-      dx[0] = inv_det * (df[1][1] * fx[0] - df[1][0] * fx[1]);
-      dx[1] = inv_det * (-df[0][1] * fx[0] + df[0][0] * fx[1]);
-      x[0] -= dx[0];
-      x[1] -= dx[1];
-      fx = f(x[0], x[1]);
-      hist.push_back({dx[0], dx[1]});
-      if (iter >= 4) {
-        auto &c = hist[hist.size() - 1];
-        bool conv = c[0] <= atol[0] && c[1] <= atol[1];
-        if (!conv) {
-          auto &a = hist[hist.size() - 3], &b = hist[hist.size() - 2];
-          bool ok = true;
-          for (int k = 0; k < 2; ++k) {
-            double r = std::log(std::fabs(c[k]) / std::fabs(b[k])) / std::log(std::fabs(b[k]) / std::fabs(a[k]));
-            ok = ok && r >= 0.0;
-          }
-          if (!ok) {
-            status = 2;
-            x[0] = h0, x[1] = K0;
-            break;
-          }
-        }
-      }
-      ++iter;
-    }
-    if (status == 0 && iter == 20 && !(std::fabs(dx[0]) <= 1000.0 * atol[0] && std::fabs(dx[1]) <= 1000.0 * atol[1])) {
-      status = 1;
-      x[0] = h0, x[1] = K0;
-    }
+      return std::array<double, 2>{inv_det * (df[1][1] * fx[0] - df[1][0] * fx[1]),
+                                   inv_det * (-df[0][1] * fx[0] + df[0][0] * fx[1])};
+    };
+    std::array<double, 2> x = guess;
+    const int status = quasi_newton(f, inv_df, x, std::array<double, 2>{1e-13 * guess[0], 1e-13 * guess[1]});
     found = status == 0;
     h = x[0];
     K = x[1];
@@ -969,7 +995,6 @@ static Poly hybrid_poly(const Problem &pr, idx i, const std::vector<Cv> &ul);
 // LocalReconstruction::compute + CWENO_AO::reconstruct_impl + HybridWENO
 static int local_reconstruct(Problem &pr, idx i, std::vector<Cv> &ul) {
   auto &rc = pr.rc[i];
-  const auto &g = pr.g;
   int st = 0;
   // recompute_equilibrium (local_reconstruction.hpp:87-100)
   if (rc.steps_since % pr.s.steps_per_recompute == 0) {
@@ -1891,6 +1916,49 @@ double zfvm_oracle_rk_ode_error(int stages, int ode, double dt, double t_final) 
   double err = 0.0;
   for (int i = 0; i < n; ++i) err = std::max(err, std::fabs(u[i] - exact));
   return err;
+}
+
+// The EOS round trips of test/zisa/unit_test/model/eos.cpp:7-23 at (rho, E):
+// out = {rhoE(enthalpy_entropy(rhoE)), rhoE(rhoP(rhoE))}, four numbers.
+int zfvm_oracle_eos_roundtrips(double gamma, double R, double rho, double E, double *out) {
+  EOS eos;
+  eos.gamma = gamma;
+  eos.R = R;
+  const RhoE r{rho, E};
+  const auto hK = eos.hK_rhoE(r);
+  const RhoE a = eos.rhoE_hK(hK[0], hK[1]);
+  const RhoE b = eos.rhoE_rhoP(r[0], eos.pressure_rhoE(r[1]));
+  out[0] = a[0], out[1] = a[1], out[2] = b[0], out[3] = b[1];
+  return 0;
+}
+
+// The problems of test/zisa/unit_test/math/quasi_newton.cpp:9-54 solved by the
+// quasi_newton above.  which 0: x^2 - 1.2345^2 from 1.9 with the Newton
+// inverse fx / (2 x0), atol 1e-10; which 1: f(h, K) = (h K + h - K, K) from
+// (0.2, -0.4) with its exact inverse Jacobian at the current point, atol 1e-10
+// (root (0, 0)).  x gets the result (one or two numbers); returns
+// quasi_newton's status.
+int zfvm_oracle_quasi_newton_problem(int which, double *x) {
+  if (which == 0) {
+    const double root = 1.2345;
+    auto f = [root](const std::array<double, 1> &v) { return std::array<double, 1>{v[0] * v[0] - root * root}; };
+    auto inv_df = [](const std::array<double, 1> &v, const std::array<double, 1> &fx) {
+      return std::array<double, 1>{fx[0] / (2.0 * v[0])};
+    };
+    std::array<double, 1> v{1.9};
+    const int st = quasi_newton(f, inv_df, v, std::array<double, 1>{1e-10});
+    x[0] = v[0];
+    return st;
+  }
+  auto f = [](const std::array<double, 2> &t) { return std::array<double, 2>{t[0] * t[1] + t[0] - t[1], t[1]}; };
+  auto inv_df = [](const std::array<double, 2> &t, const std::array<double, 2> &fx) {
+    const double h = t[0], K = t[1], inv_det = 1.0 / (K + 1.0);
+    return std::array<double, 2>{inv_det * (fx[0] + (-h + 1.0) * fx[1]), inv_det * ((K + 1.0) * fx[1])};
+  };
+  std::array<double, 2> v{0.2, -0.4};
+  const int st = quasi_newton(f, inv_df, v, std::array<double, 2>{1e-10, 1e-10});
+  x[0] = v[0], x[1] = v[1];
+  return st;
 }
 
 }  // extern "C"

@@ -77,6 +77,23 @@ def test_local_equilibrium(olib):
     assert np.allclose(approx2, exact2, rtol=1e-9)
 
 
+def test_eos_round_trips(olib):
+    # test/zisa/unit_test/model/eos.cpp:7-23: IdealGasEOS(1.2, 0.9), (rho, E) = (1, 2)
+    # through (h, K) and back, and through (rho, p) and back, within 1e-10
+    via_hK, via_p = olib.eos_roundtrips(1.2, 0.9, 1.0, 2.0)
+    assert np.allclose(via_hK, [1.0, 2.0], rtol=1e-10, atol=0.0)
+    assert np.allclose(via_p, [1.0, 2.0], rtol=1e-10, atol=0.0)
+
+
+def test_quasi_newton_problems(olib):
+    # test/zisa/unit_test/math/quasi_newton.cpp:9-54, solved by the quasi-Newton
+    # iteration the equilibrium solve uses: converged, within 10 atol = 1e-9
+    x, st = olib.quasi_newton_problem(0)
+    assert st == 0 and abs(x[0] - 1.2345) <= 1e-9
+    x, st = olib.quasi_newton_problem(1)
+    assert st == 0 and np.all(np.abs(x) <= 1e-9)
+
+
 def _isentropic_point(gamma, g, theta, x_ref, x):
     # h(x) = h_ref + phi(x_ref) - phi(x), phi = g |x|; rho = ((gamma-1)/gamma h/K)^(1/(gamma-1))
     h = theta[0] + g * np.linalg.norm(x_ref) - g * np.linalg.norm(x)
