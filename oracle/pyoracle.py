@@ -48,6 +48,7 @@ def lib() -> C.CDLL:
         L.zfvm_oracle_rk_ode_error.restype = C.c_double
         L.zfvm_oracle_eos_roundtrips.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.zfvm_oracle_quasi_newton_problem.argtypes = [C.c_int, dp]
+        L.zfvm_oracle_rule.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), dp, dp]
         L.zfvm_oracle_last_error.restype = C.c_char_p
         _LIB = L
     return _LIB
@@ -219,3 +220,15 @@ def quasi_newton_problem(which: int):
     x = np.zeros(2)
     st = lib().zfvm_oracle_quasi_newton_problem(which, _dp(x))
     return (x[:1] if which == 0 else x), st
+
+
+def rule(kind: str, deg: int):
+    """The oracle's reference-element rule ("edge", "triangle", "tetrahedron"):
+    (weights summing to 1, points: [-1, 1] coordinates or barycentric rows)."""
+    k = {"edge": 0, "triangle": 1, "tetrahedron": 2}[kind]
+    nc = 1 if k == 0 else k + 2
+    n = C.c_int()
+    w, x = np.zeros(16), np.zeros(16 * nc)
+    _check(lib().zfvm_oracle_rule(k, deg, 16, C.byref(n), _dp(w), _dp(x)))
+    m = n.value
+    return w[:m].copy(), x[:m * nc].reshape(m, nc).copy()

@@ -1918,6 +1918,30 @@ double zfvm_oracle_rk_ode_error(int stages, int ode, double dt, double t_final) 
   return err;
 }
 
+// A reference-element rule: kind 0 edge (x: n coordinates in [-1, 1]), 1
+// triangle (x: n x 3 barycentric), 2 tetrahedron (x: n x 4 barycentric);
+// weights normalised to sum 1.  At most max_n points are written; *n gets the
+// rule's size.
+int zfvm_oracle_rule(int kind, int deg, int max_n, int *n, double *w, double *x) {
+  try {
+    const Rule r = kind == 0 ? edge_rule(deg) : (kind == 1 ? tri_rule(deg) : tet_rule(deg));
+    const int m = (int)r.w.size(), nc = kind == 0 ? 1 : kind + 2;
+    *n = m;
+    if (m > max_n) {
+      g_oracle_err = "rule larger than the buffers";
+      return 1;
+    }
+    for (int q = 0; q < m; ++q) {
+      w[q] = r.w[q];
+      for (int c = 0; c < nc; ++c) x[q * nc + c] = r.x[q][c];
+    }
+    return 0;
+  } catch (const Error &e) {
+    g_oracle_err = e.msg;
+    return e.code;
+  }
+}
+
 // The EOS round trips of test/zisa/unit_test/model/eos.cpp:7-23 at (rho, E):
 // out = {rhoE(enthalpy_entropy(rhoE)), rhoE(rhoP(rhoE))}, four numbers.
 int zfvm_oracle_eos_roundtrips(double gamma, double R, double rho, double E, double *out) {
