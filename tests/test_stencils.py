@@ -1,0 +1,88 @@
+"""The reference's stencil tests, restated for this build's host set-up on
+generated meshes (the reference's grid files are missing):
+
+- deduce_max_order (test/zisa/unit_test/reconstruction/stencil.cpp:126-145):
+  a central stencil that finds only N cells falls back to the highest order N
+  cells support at overfit 2 in 2D (1, 2, 4 -> 1; 5, 10 -> 2; 11, 18 -> 3;
+  19 -> 4), here on strips of N triangles with an order-4 request;
+- a central stencil holds the nearest cells: no cell closer than its farthest
+  member is left out (stencil.cpp:10-41, 12 points in 2D; also 3D);
+- one-sided stencils reach the requested size away from the boundary
+  (stencil.cpp:43-62);
+- stencil families: the cell first in local2global and nowhere else, no
+  repeats, for orders 1-3 central and one-sided on a cube of tetrahedra, and
+  the family order of single and mixed families (stencil_family.cpp:10-74).
+"""
+import numpy as np
+import pytest
+
+import zisafvm_gb300 as z
+
+
+def _strip(n):
+    """n triangles in a row, each sharing edges with its neighbours."""
+    m = (n + 1) // 2 + 1
+    v = np.array([[i, 0.0, 0.0] for i in range(m + 1)] + [[i + 0.5, 1.0, 0.0] for i in range(m + 1)])
+    tris = []
+    for i in range(m):
+        tris += [[i, i + 1, m + 1 + i], [i + 1, m + 2 + i, m + 1 + i]]
+    return z.RawMesh(2, v, np.array(tris[:n], np.int64))
+
+
+def test_deduce_max_order(zlib):
+    for n, order in [(1, 1), (2, 1), (4, 1), (5, 2), (10, 2), (11, 3), (18, 3), (19, 4), (28, 4)]:
+        st = z.Mesh(_strip(n), z.StencilSpec([4], [0], [2.0]), quad=(3, 5, 4)).stencils()
+        assert st["n_l2g"][0] == min(n, 19)
+        assert st["order"][0, 0] == order, (n, st["order"][0, 0])
+
+
+def _nearest_cells_check(mesh, cells):
+    st, c = mesh.stencils(), mesh.geometry()["centers"]
+    for i in cells:
+        s = st["l2g"][i, st["local"][i, 0, :st["size"][i, 0]]]
+        d = np.linalg.norm(c - c[i], axis=1)
+        nearer = np.where(d < d[s].max())[0]
+        assert set(nearer) <= set(s), (i, sorted(set(nearer) - set(s)))
+
+
+def test_central_and_one_sided_stencils_2d(zlib):
+    raw = z.RawMesh.generate("disk", n=20, radius=1.0, jitter=0.2, seed=2)
+    # order 3 at overfit 2.2: 12 points, as in the reference's test
+    mesh = z.Mesh(raw, z.StencilSpec([3, 3, 3, 3], [0, 1, 1, 1], [2.2, 2.2, 2.2, 2.2]), quad=(3, 3, 2))
+    away = np.where(np.linalg.norm(mesh.geometry()["centers"], axis=1) < 0.5)[0]
+    st = mesh.stencils()
+    assert len(away) > 500 and np.all(st["size"][away, :4] == 12)
+    _nearest_cells_check(mesh, away)
+
+
+@pytest.mark.parametrize("spec", [z.StencilSpec([3], [0], [2.2]), z.StencilSpec.cweno(2, 3), z.StencilSpec.cweno(3, 3)])
+def test_central_and_one_sided_stencils_3d(zlib, spec):
+    raw = z.RawMesh.generate("cube", n=8, jitter=0.1, seed=2)
+    mesh = z.Mesh(raw, spec, quad=(2, 2, 2))
+    away = np.where(np.linalg.norm(mesh.geometry()["centers"] - 0.5, axis=1) < 0.25)[0]
+    st = mesh.stencils()
+    ns = len(spec.orders)
+    assert len(away) > 200 and np.all(st["order"][away, :ns] == np.array(spec.orders))
+    _nearest_cells_check(mesh, away)
+
+
+def test_stencil_families_are_unique(zlib):
+    raw = z.RawMesh.generate("cube", n=3, jitter=0.1, seed=1)
+    for order in (1, 2, 3):
+        for biased in (0, 1):
+            st = z.Mesh(raw, z.StencilSpec([order], [biased], [2.0]), quad=(2, 2, 2)).stencils()
+            for i in range(raw.n_cells):
+                l2g = st["l2g"][i, :st["n_l2g"][i]]
+                assert l2g[0] == i and i not in l2g[1:] and len(set(l2g)) == len(l2g)
+
+
+def test_family_order(zlib):
+    raw = z.RawMesh.generate("cube", n=3, jitter=0.1, seed=1)
+    mesh_c = z.Mesh(raw, z.StencilSpec([3], [0], [2.0]), quad=(2, 2, 2))
+    i = int(np.argmin(np.linalg.norm(mesh_c.geometry()["centers"] - 0.5, axis=1)))  # a cell away from the boundary
+    for order in (1, 2, 3):
+        for biased in (0, 1):
+            st = z.Mesh(raw, z.StencilSpec([order], [biased], [2.0]), quad=(2, 2, 2)).stencils()
+            assert st["order"][i, st["k_high"][i]] == order
+    st = z.Mesh(raw, z.StencilSpec([3, 1, 1], [0, 1, 1], [2.0, 1.5, 1.5]), quad=(2, 2, 2)).stencils()
+    assert st["order"][i, st["k_high"][i]] == 3
