@@ -106,6 +106,18 @@ int zfvm_mesh_get_pinv(const zfvm_mesh *m, int64_t cell, int32_t k, double *P, i
 /* Geometry export: volumes[n], inradii[n], centers[n x 3], flags[n]. */
 int zfvm_mesh_get_geometry(const zfvm_mesh *m, double *volumes, double *inradii, double *centers,
                            uint8_t *flags);
+/* Connectivity export, n_cells x (n_dims + 1) each: the neighbour across local
+ * face k (-1 on the boundary) and the face's number (Grid::neighbours,
+ * Grid::edge_indices, grid/grid.cpp:385-413: interior faces first, numbered in
+ * the order of their lower cell, then boundary faces in cell order).  Local
+ * face k of a triangle joins its vertices k and k+1 (mod 3), after the
+ * counter-clockwise reordering of grid/grid.cpp:152-203.  Either pointer may be
+ * null. */
+int zfvm_mesh_get_connectivity(const zfvm_mesh *m, int64_t *neighbours, int64_t *edge_indices);
+/* Face export, n_edges entries each: left and right cell (right = -1 on the
+ * boundary; left < right inside), the unit normal out of the left cell
+ * (n_edges x 3) and the face's area (length in 2D).  Any pointer may be null. */
+int zfvm_mesh_get_faces(const zfvm_mesh *m, int64_t *left, int64_t *right, double *normals, double *areas);
 
 /* ---- initial data (cell averages with the volume quadrature) ---------------
  * kind 0: isentropic vortex (2D) / vortex tube along z (3D);

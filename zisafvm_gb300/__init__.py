@@ -115,6 +115,8 @@ def load_library() -> C.CDLL:
         "zfvm_mesh_get_stencils": [vp] + [C.c_void_p] * 8,
         "zfvm_mesh_get_pinv": [vp, i64, i32, dp, C.POINTER(i32), C.POINTER(i32)],
         "zfvm_mesh_get_geometry": [vp, dp, dp, dp, C.POINTER(C.c_uint8)],
+        "zfvm_mesh_get_connectivity": [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+        "zfvm_mesh_get_faces": [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64), dp, dp],
         "zfvm_initial_conditions": [vp, i32, dp, dp],
         "zfvm_solver_create": [vp, C.POINTER(_SchemeDesc), pp],
         "zfvm_solver_destroy": [vp],
@@ -304,6 +306,23 @@ class Mesh:
         _check(load_library().zfvm_mesh_get_geometry(self._h, _dp(vol), _dp(rin), _dp(cen),
                                                       flags.ctypes.data_as(C.POINTER(C.c_uint8))))
         return {"volumes": vol, "inradii": rin, "centers": cen, "flags": flags}
+
+    def connectivity(self) -> dict:
+        """Neighbour across every local face (-1: boundary) and the face's number,
+        n_cells x (n_dims + 1) each."""
+        n, nb = self.n_cells, int(self.info["n_dims"]) + 1
+        nbr, edge = np.zeros((n, nb), np.int64), np.zeros((n, nb), np.int64)
+        _check(load_library().zfvm_mesh_get_connectivity(self._h, _i64p(nbr), _i64p(edge)))
+        return {"neighbours": nbr, "edge_indices": edge}
+
+    def faces(self) -> dict:
+        """Left / right cell (-1: boundary), unit normal out of the left cell and
+        area of every face, interior faces first."""
+        m = int(self.info["n_edges"])
+        left, right = np.zeros(m, np.int64), np.zeros(m, np.int64)
+        normals, areas = np.zeros((m, 3)), np.zeros(m)
+        _check(load_library().zfvm_mesh_get_faces(self._h, _i64p(left), _i64p(right), _dp(normals), _dp(areas)))
+        return {"left": left, "right": right, "normals": normals, "areas": areas}
 
     def initial_conditions(self, kind: str, **p) -> np.ndarray:
         """Cell averages (n_cells x 5) of 'vortex' or 'polytrope' initial data."""

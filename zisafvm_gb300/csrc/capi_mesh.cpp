@@ -267,6 +267,31 @@ extern "C" int zfvm_mesh_get_geometry(const zfvm_mesh *m, double *volumes, doubl
   return ZFVM_OK;
 }
 
+extern "C" int zfvm_mesh_get_connectivity(const zfvm_mesh *m, int64_t *neighbours, int64_t *edge_indices) {
+  if (!m) return fail(ZFVM_EINVAL, "null mesh");
+  const auto &g = m->grid;
+  if (neighbours) std::copy(g.neighbours.begin(), g.neighbours.end(), neighbours);
+  if (edge_indices) std::copy(g.edge_indices.begin(), g.edge_indices.end(), edge_indices);
+  return ZFVM_OK;
+}
+
+extern "C" int zfvm_mesh_get_faces(const zfvm_mesh *m, int64_t *left, int64_t *right, double *normals,
+                                   double *areas) {
+  if (!m) return fail(ZFVM_EINVAL, "null mesh");
+  const auto &g = m->grid;
+  for (index_t e = 0; e < g.n_edges; ++e) {
+    if (left) left[e] = g.left[e];
+    if (right) right[e] = g.right[e];
+    if (normals) {
+      normals[3 * e] = g.face_normal[e].x;
+      normals[3 * e + 1] = g.face_normal[e].y;
+      normals[3 * e + 2] = g.face_normal[e].z;
+    }
+    if (areas) areas[e] = g.face_area[e];
+  }
+  return ZFVM_OK;
+}
+
 // Initial data as cell averages over the volume quadrature
 // (the averaging pattern of experiments/polytrope.cpp:25-53).
 extern "C" int zfvm_initial_conditions(const zfvm_mesh *m, int32_t kind, const double *p, double *cv) {
