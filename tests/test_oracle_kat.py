@@ -94,6 +94,24 @@ def test_quasi_newton_problems(olib):
     assert st == 0 and np.all(np.abs(x) <= 1e-9)
 
 
+def test_frozen_ghost_cells_keep_their_values(zlib, olib):
+    # test/zisa/unit_test/boundary/frozen_boundary_condition.cpp:9-51: ghost
+    # cells under FrozenBC keep the values they were set to, bit for bit, here
+    # through whole RK steps of the well-balanced polytrope with the reference's
+    # experiment mask (ghost cells beyond r = 0.5), each ghost cell set to
+    # distinct values
+    from problems import polytrope_2d_frozen
+    raw, mesh, scheme, u0 = polytrope_2d_frozen(n_rings=12, amplitude=1e-2)
+    ghost = np.where(raw.ghost == 1)[0]
+    assert len(ghost) > 0
+    u = u0.copy()
+    u[ghost] *= 1.0 + 1e-3 * (np.arange(len(ghost)) % 7)[:, None]
+    o = olib.Oracle(raw, mesh.stencils(), scheme.oracle_vector(), quad=mesh.quad, threads=2)
+    out, t, n = o.run(u, n_steps=3)
+    assert n == 3 and np.array_equal(out[ghost], u[ghost])
+    assert not np.array_equal(out[raw.ghost == 0], u[raw.ghost == 0])
+
+
 def _isentropic_point(gamma, g, theta, x_ref, x):
     # h(x) = h_ref + phi(x_ref) - phi(x), phi = g |x|; rho = ((gamma-1)/gamma h/K)^(1/(gamma-1))
     h = theta[0] + g * np.linalg.norm(x_ref) - g * np.linalg.norm(x)
