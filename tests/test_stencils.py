@@ -11,7 +11,9 @@ generated meshes (the reference's grid files are missing):
   (stencil.cpp:43-62);
 - stencil families: the cell first in local2global and nowhere else, no
   repeats, for orders 1-3 central and one-sided on a cube of tetrahedra, and
-  the family order of single and mixed families (stencil_family.cpp:10-74).
+  the family order of single and mixed families (stencil_family.cpp:10-74);
+- every stencil in use has a full-rank least-squares operator
+  (hybrid_weno.hpp:360-405).
 """
 import numpy as np
 import pytest
@@ -86,3 +88,27 @@ def test_family_order(zlib):
             assert st["order"][i, st["k_high"][i]] == order
     st = z.Mesh(raw, z.StencilSpec([3, 1, 1], [0, 1, 1], [2.0, 1.5, 1.5]), quad=(2, 2, 2)).stencils()
     assert st["order"][i, st["k_high"][i]] == 3
+
+
+@pytest.mark.parametrize("nd,order", [(2, 3), (3, 2), (3, 3)])
+def test_used_stencils_have_full_rank_operators(zlib, nd, order):
+    """test_hybrid_weno_matrices (hybrid_weno.hpp:360-405): the least-squares
+    matrix of every stencil a cell uses (interior cells and the first ghost
+    layer) has full column rank, here as a pseudo-inverse of full row rank."""
+    if nd == 2:
+        raw = z.RawMesh.generate("periodic_square", n=8, halo=3, jitter=0.2, seed=4)
+        mesh = z.Mesh(raw, z.StencilSpec.cweno(order, 2), quad=(3, 3, 2))
+    else:
+        raw = z.RawMesh.generate("cube", n=4, jitter=0.1, seed=4)
+        mesh = z.Mesh(raw, z.StencilSpec.cweno(order, 3), quad=(2, 2, 2))
+    st = mesh.stencils()
+    checked = 0
+    for i in range(mesh.n_cells):
+        for k in range(int(st["n_stencils"][i])):
+            if st["order"][i, k] < 2:
+                continue
+            P = mesh.pinv(i, k)
+            s = np.linalg.svd(P, compute_uv=False)
+            assert P.shape[0] <= P.shape[1] and np.all(np.isfinite(P)) and s.min() > 1e-10 * s.max(), (i, k)
+            checked += 1
+    assert checked > mesh.n_cells
