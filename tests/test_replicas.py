@@ -8,7 +8,6 @@ import subprocess
 import sys
 from pathlib import Path
 
-import pytest
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
