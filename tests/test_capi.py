@@ -28,6 +28,15 @@ def test_library_exports_every_symbol(zlib):
     assert not missing, missing
 
 
+def test_python_bindings_cover_the_header(zlib):
+    """Every declared entry point has argument types in the bindings' table
+    (zfvm_last_error, which takes none, is set up on its own)."""
+    src = (ROOT / "zisafvm_gb300" / "__init__.py").read_text()
+    bound = set(re.findall(r'"(zfvm_\w+)"\s*:', src))
+    assert [n for n in declared_symbols() if n not in bound and n != "zfvm_last_error"] == []
+    assert sorted(bound - set(declared_symbols())) == []
+
+
 def test_error_reporting_without_compute(zlib):
     z = zlib
     lib = z.load_library()

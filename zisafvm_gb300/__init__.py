@@ -123,6 +123,7 @@ def load_library() -> C.CDLL:
         "zfvm_set_state": [vp, dp, C.c_double],
         "zfvm_get_state": [vp, dp, dp],
         "zfvm_rate_of_change": [vp, dp],
+        "zfvm_rate_of_change_noalloc": [vp, dp],
         "zfvm_cfl_dt": [vp, dp],
         "zfvm_step": [vp, C.c_double],
         "zfvm_advance": [vp, i64, C.c_double, dp, C.POINTER(i64)],
