@@ -28,7 +28,15 @@ NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fope
              "--expt-relaxed-constexpr"]
 
 HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp", "snapshot.cpp"]
-CUDA_SOURCES = ["solver.cu", "batch.cu", "server.cu", "noalloc.cu", "inst_s2o3.cu", "inst_s2o2.cu", "inst_s3o3.cu", "inst_s3o2.cu"]
+CUDA_SOURCES = ["solver.cu", "batch.cu", "server.cu", "noalloc.cu"]
+# inst_shape.cu compiled once per stencil shape x precision x (single solver,
+# batch): (object name, -D flags)
+SHAPES = {"s2o3": "S2o3", "s2o2": "S2o2", "s3o3": "S3o3", "s3o2": "S3o2"}
+SHAPE_UNITS = [
+    (f"inst_{name}_{'mix' if mixed else 'f64'}{'_batch' if batch else ''}",
+     [f"-DZFVM_SHAPE_NAME={name}", f"-DZFVM_SHAPE={cls}", f"-DZFVM_MIXED={mixed}", f"-DZFVM_BATCH={batch}"])
+    for name, cls in SHAPES.items() for mixed in (0, 1) for batch in (0, 1)
+]
 
 
 def _headers() -> list[Path]:
@@ -61,13 +69,17 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         objs.append(obj)
         if force or _stale(obj, src, deps):
             jobs.append(["g++", *CXXFLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)])
-    for name in CUDA_SOURCES:
-        src, obj = CSRC / name, BUILD / (name + ".o")
+    units = [(name, CSRC / name, []) for name in CUDA_SOURCES]
+    units += [(name + ".cu", CSRC / "inst_shape.cu", defs) for name, defs in SHAPE_UNITS]
+    for name, src, defs in units:
+        obj = BUILD / (name + ".o")
         objs.append(obj)
         if force or _stale(obj, src, deps):
-            jobs.append([NVCC, *NVCCFLAGS, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)])
+            jobs.append([NVCC, *NVCCFLAGS, *defs, "-I", str(INCLUDE), "-c", str(src), "-o", str(obj)])
     workers = max(1, min(len(jobs), os.cpu_count() or 4))
     if jobs:
+        # the slowest units first, so they do not start last
+        jobs.sort(key=lambda cmd: 0 if "-DZFVM_SHAPE_NAME=s3o2" in cmd or "-DZFVM_SHAPE_NAME=s3o3" in cmd else 1)
         with ThreadPoolExecutor(max_workers=workers) as ex:
             for cmd, _ in zip(jobs, ex.map(_run, jobs)):
                 if verbose:

@@ -1680,32 +1680,17 @@ void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_c
   if (c.ev) cudaEventRecord(c.ev[3], c.stream);
 }
 
-template <class S>
-void launch_batch_stage_t(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft, int stage,
-                          const BatchCfg &c) {
-  if (c.mixed)
-    launch_batch_stage_p<S, true>(inst, ct, n_ct, ft, n_ft, stage, c);
-  else
-    launch_batch_stage_p<S, false>(inst, ct, n_ct, ft, n_ft, stage, c);
-}
-
 // Occupancy-limited block counts of the three batch kernels (for the autotuner).
-template <class S>
-void batch_occupancy_t(const BatchCfg &c, int *blocks_per_sm) {
+template <class S, bool MIXED>
+void batch_occupancy_p(int *blocks_per_sm) {
   auto occ = [](const void *k, size_t smem = 0) {
     int b = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 128, smem);
     return b;
   };
-  if (c.mixed) {
-    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, true>(), recon_smem_bytes<S, 1, true>(128));
-    blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, true>);
-    blocks_per_sm[2] = occ((const void *)km_update<S, true>);
-  } else {
-    blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, false>());
-    blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, false>);
-    blocks_per_sm[2] = occ((const void *)km_update<S, false>);
-  }
+  blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, MIXED>(), recon_smem_bytes<S, 1, MIXED>(128));
+  blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, MIXED>);
+  blocks_per_sm[2] = occ((const void *)km_update<S, MIXED>);
 }
 
 // ------------------------------------------------------------ launching
@@ -1785,61 +1770,68 @@ void launch_export_p(const DevData &D, const Params &P, StageArgs &a, const Laun
 }
 
 template <class S>
-void launch_export_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
-  if (c.mixed)
-    launch_export_p<S, true>(D, P, a, c);
-  else
-    launch_export_p<S, false>(D, P, a, c);
-}
-
-template <class S>
-void launch_stage_t(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {
-  if (c.mixed)
-    launch_stage_p<S, true>(D, P, a, c);
-  else
-    launch_stage_p<S, false>(D, P, a, c);
-}
-
-template <class S>
-void launch_tracer_t(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta, const LaunchCfg &c) {
-  if (c.mixed)
-    launch_tracer_p<S, true>(D, P, a, ta, c.n_cells, c.n_edges, c.eq, c.flux, c.stream);
-  else
-    launch_tracer_p<S, false>(D, P, a, ta, c.n_cells, c.n_edges, c.eq, c.flux, c.stream);
-}
-
-template <class S>
 void launch_cfl_t(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) {
   const int nb = (c.n_cells + 127) / 128;
   k_cfl<S><<<nb, 128, 0, c.stream>>>(D, P, u, c.mixed ? 1 : 0);
 }
 
-#define ZFVM_DECLARE_SHAPE(name)                                                                  \
-  void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c); \
-  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c); \
-  void launch_batch_stage_##name(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft,  \
-                                 int stage, const BatchCfg &c);                                              \
-  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm);                          \
-  void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c);  \
-  void launch_tracer_##name(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta, const LaunchCfg &c);
-#define ZFVM_DEFINE_SHAPE(name, S)                                                                \
-  void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) { \
-    launch_stage_t<S>(D, P, a, c);                                                                \
-  }                                                                                               \
-  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) { \
-    launch_cfl_t<S>(D, P, u, c);                                                                  \
-  }                                                                                               \
-  void launch_batch_stage_##name(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, int n_ft,  \
-                                 int stage, const BatchCfg &c) {                                             \
-    launch_batch_stage_t<S>(inst, ct, n_ct, ft, n_ft, stage, c);                                             \
-  }                                                                                                          \
-  void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm) { batch_occupancy_t<S>(c, blocks_per_sm); } \
-  void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {             \
-    launch_export_t<S>(D, P, a, c);                                                                          \
-  }                                                                                                          \
-  void launch_tracer_##name(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta, const LaunchCfg &c) { \
-    launch_tracer_t<S>(D, P, a, ta, c);                                                                      \
+// Instantiation: inst_shape.cu is compiled once per (shape, precision, single
+// solver or batch) so the sixteen kernel sets build in parallel; the shape-level
+// entry points below pick the precision at run time.
+#define ZFVM_DECLARE_SHAPE_PREC(name, sfx)                                                                \
+  void launch_stage_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c);  \
+  void launch_export_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c); \
+  void launch_tracer_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta,      \
+                                    const LaunchCfg &c);                                                  \
+  void launch_batch_stage_##name##_##sfx(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, \
+                                         int n_ft, int stage, const BatchCfg &c);                         \
+  void batch_occupancy_##name##_##sfx(int *blocks_per_sm);
+#define ZFVM_DECLARE_SHAPE(name)                                                                          \
+  ZFVM_DECLARE_SHAPE_PREC(name, f64)                                                                      \
+  ZFVM_DECLARE_SHAPE_PREC(name, mix)                                                                      \
+  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c);         \
+  inline void launch_stage_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {  \
+    c.mixed ? launch_stage_##name##_mix(D, P, a, c) : launch_stage_##name##_f64(D, P, a, c);              \
+  }                                                                                                       \
+  inline void launch_export_##name(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) { \
+    c.mixed ? launch_export_##name##_mix(D, P, a, c) : launch_export_##name##_f64(D, P, a, c);            \
+  }                                                                                                       \
+  inline void launch_tracer_##name(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta,       \
+                                   const LaunchCfg &c) {                                                  \
+    c.mixed ? launch_tracer_##name##_mix(D, P, a, ta, c) : launch_tracer_##name##_f64(D, P, a, ta, c);    \
+  }                                                                                                       \
+  inline void launch_batch_stage_##name(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft,  \
+                                        int n_ft, int stage, const BatchCfg &c) {                         \
+    c.mixed ? launch_batch_stage_##name##_mix(inst, ct, n_ct, ft, n_ft, stage, c)                         \
+            : launch_batch_stage_##name##_f64(inst, ct, n_ct, ft, n_ft, stage, c);                        \
+  }                                                                                                       \
+  inline void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm) {                             \
+    c.mixed ? batch_occupancy_##name##_mix(blocks_per_sm) : batch_occupancy_##name##_f64(blocks_per_sm);  \
   }
+// the single-solver kernels of one shape and precision (the FP64 unit also
+// holds the shape's CFL pass)
+#define ZFVM_DEFINE_SHAPE_SINGLE(name, S, MIXED, sfx)                                                      \
+  void launch_stage_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) {  \
+    launch_stage_p<S, MIXED>(D, P, a, c);                                                                  \
+  }                                                                                                        \
+  void launch_export_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c) { \
+    launch_export_p<S, MIXED>(D, P, a, c);                                                                 \
+  }                                                                                                        \
+  void launch_tracer_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta,       \
+                                    const LaunchCfg &c) {                                                  \
+    launch_tracer_p<S, MIXED>(D, P, a, ta, c.n_cells, c.n_edges, c.eq, c.flux, c.stream);                  \
+  }
+#define ZFVM_DEFINE_SHAPE_CFL(name, S)                                                                     \
+  void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) {          \
+    launch_cfl_t<S>(D, P, u, c);                                                                           \
+  }
+// the batched (persistent, multi-instance) kernels of one shape and precision
+#define ZFVM_DEFINE_SHAPE_BATCH(name, S, MIXED, sfx)                                                       \
+  void launch_batch_stage_##name##_##sfx(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft,  \
+                                         int n_ft, int stage, const BatchCfg &c) {                         \
+    launch_batch_stage_p<S, MIXED>(inst, ct, n_ct, ft, n_ft, stage, c);                                    \
+  }                                                                                                        \
+  void batch_occupancy_##name##_##sfx(int *blocks_per_sm) { batch_occupancy_p<S, MIXED>(blocks_per_sm); }
 
 ZFVM_DECLARE_SHAPE(s2o3)
 ZFVM_DECLARE_SHAPE(s2o2)
