@@ -158,8 +158,9 @@ typedef struct {
   int32_t flux_bc;              /* flux-bc.mode                                     */
   int32_t boundary;             /* ghost-cell boundary condition                    */
   int32_t precision;            /* zfvm_precision                                   */
-  int32_t steps_per_recompute;  /* reconstruction.steps_per_recompute (must be 1)   */
-  double recompute_threshold;
+  int32_t steps_per_recompute;  /* reconstruction.steps_per_recompute (>= 1)        */
+  double recompute_threshold;   /* reconstruction.recompute_threshold: refresh sooner
+                                   when |scaled (rho, E_int) - equilibrium average| >= it */
   int32_t reconstruction;       /* reconstruction.mode: zfvm_reconstruction           */
   double step_rejection_drho;   /* RejectLargeDensityChange drho_crit_rel; 0: RejectNothing */
   int32_t step_rejection_max_exponent; /* smallest step factor 2^-max_exponent       */
@@ -241,7 +242,8 @@ int zfvm_rate_of_change(zfvm_solver *s, double *tendency);
  *  - Every call on a device shares the one array.  Calls return only when their
  *    work is done, so calls from one thread never overlap; calls from several
  *    threads must be serialised by the caller, or they race on the GPU.
- *  - The solver's device must be current, as for the other entry points. */
+ *  - The solver's device must be current; a call made while another device is
+ *    current fails with ZFVM_EINVAL instead of handing over that device's array. */
 int zfvm_rate_of_change_noalloc(zfvm_solver *s, double *tendency);
 
 /* EulerGlobalReconstruction::compute (reconstruction/global_reconstruction_impl.hpp:100-163):

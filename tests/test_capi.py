@@ -69,7 +69,7 @@ def test_solver_validation_runs_before_cuda(zlib):
     from conftest import gpu_available
     z = zlib
     raw, mesh, scheme, u0 = polytrope_2d(n_rings=10)
-    bad = [dict(steps_per_recompute=2), dict(rk_stages=4), dict(reconstruction=7), dict(n_avars=-1),
+    bad = [dict(steps_per_recompute=0), dict(rk_stages=4), dict(reconstruction=7), dict(n_avars=-1),
            dict(n_avars=1000), dict(heating_rate=1.0, gravity=z.GRAVITY_NONE, equilibrium=z.EQ_NONE,
                                     flux_bc=z.FLUX_BC_NONE), dict(step_rejection_drho=-1.0)]
     for change in bad:
@@ -82,3 +82,19 @@ def test_solver_validation_runs_before_cuda(zlib):
             with pytest.raises(z.ZfvmError) as e:
                 z.Solver(mesh, z.Scheme(**{**scheme.__dict__, "precision": prec}))
             assert e.value.code == 6  # ZFVM_ECUDA: validation passed
+
+
+def test_equilibrium_schedule_footprint_and_validation(zlib):
+    """A refresh schedule adds the per-cell schedule state to the footprint;
+    steps_per_recompute below 1 is refused before any device work."""
+    z = zlib
+    from problems import polytrope_2d
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=12)
+    every = z.solver_footprint(mesh, scheme)
+    scheme.steps_per_recompute = 3
+    scheduled = z.solver_footprint(mesh, scheme)
+    assert scheduled > every
+    scheme.steps_per_recompute = 0
+    with pytest.raises(z.ZfvmError) as e:
+        z.Solver(mesh, scheme)
+    assert e.value.code == 1 and "steps_per_recompute" in str(e.value)

@@ -323,3 +323,48 @@ def test_error_status_nonphysical(zlib):
     # the context stays usable
     s.set_state(u0)
     s.rate_of_change()
+
+
+@pytest.mark.parametrize("spr,threshold", [(3, 1e30), (3, 1e-3), (1000, 1e-3)])
+def test_equilibrium_refresh_schedule(zlib, olib, spr, threshold):
+    """LocalReconstruction::recompute_equilibrium (local_reconstruction.hpp:87-100):
+    the equilibrium and the scaling are refreshed every steps_per_recompute
+    reconstructions, or sooner when the scaled (rho, E_int) of the cell move
+    recompute_threshold away from the equilibrium's own cell average.  Every
+    reconstruction counts (right-hand sides and RK stages alike), on the GPU
+    as in the oracle."""
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=20, amplitude=1e-2)
+    scheme.steps_per_recompute, scheme.recompute_threshold = spr, threshold
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    o = _oracle(olib, raw, mesh, scheme)
+    t_gpu, t_ref = s.rate_of_change(), o.rate_of_change(u0)
+    assert np.abs(t_gpu - t_ref).max() <= TOL_RHS * np.abs(t_ref).max()
+    s.advance(n_steps=6)
+    u_gpu, t1 = s.get_state()
+    u_ref, t_ref1, _ = o.run(u0, n_steps=6)
+    l1, linf = rel_errors(u_gpu, u_ref)
+    assert l1 < TOL_RUN and linf < TOL_RUN, (l1, linf)
+    assert abs(t1 - t_ref1) <= 1e-12 * t_ref1
+    # the schedule changes the result: a refresh at every reconstruction differs
+    every = z.Solver(mesh, z.Scheme(**{**scheme.__dict__, "steps_per_recompute": 1}))
+    every.set_state(u0)
+    every.rate_of_change()
+    every.advance(n_steps=6)
+    u_every, _ = every.get_state()
+    assert np.abs(u_every - u_gpu).max() > 1e-3 * np.abs(u_ref - u0).max()
+
+
+def test_zero_threshold_refreshes_every_reconstruction(zlib):
+    """recompute_threshold = 0 refreshes at every reconstruction whatever the
+    schedule: the same steps bit for bit as steps_per_recompute = 1."""
+    z = zlib
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-2)
+    out = []
+    for spr, thr in ((1, 0.0), (4, 0.0)):
+        s = z.Solver(mesh, z.Scheme(**{**scheme.__dict__, "steps_per_recompute": spr, "recompute_threshold": thr}))
+        s.set_state(u0)
+        s.advance(n_steps=5)
+        out.append(s.get_state()[0])
+    assert np.array_equal(out[0], out[1])

@@ -14,7 +14,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from problems import polytrope_2d, vortex_2d, vortex_tube_3d
+from problems import polytrope_2d, polytrope_2d_frozen, polytrope_3d, tracers, vortex_2d, vortex_tube_3d
 
 pytestmark = pytest.mark.gpu
 
@@ -46,11 +46,31 @@ def _assert_close(got, ref):
     assert err <= TOL_RHS, err
 
 
+def _heated_frozen(z, precision):
+    raw, mesh, scheme, u0 = polytrope_2d_frozen(n_rings=30, amplitude=1e-3, precision=precision)
+    scheme.heating_rate, scheme.heating_r0, scheme.heating_r1 = 0.3, 0.2, 0.45
+    return raw, mesh, scheme, u0
+
+
+def _with_tracers(z):
+    raw, mesh, scheme, u0 = vortex_2d(n=24, halo=3, flux=z.FLUX_HLLC)
+    scheme.n_avars = 2
+    return raw, mesh, scheme, u0
+
+
+# Each case changes which scratch pieces the call carves out of the array and
+# which of them the kernels read: FP64 or mixed face values and fluxes, the
+# equilibrium and source pieces, 2D or 3D strides, frozen ghost cells, heating.
 CASES = {
     "vortex_fp64_periodic": lambda z: vortex_2d(n=32, halo=3, flux=z.FLUX_HLLC),
     "polytrope_mixed": lambda z: polytrope_2d(n_rings=40, amplitude=1e-3, precision=z.MIXED),
     "polytrope_fp64": lambda z: polytrope_2d(n_rings=30, amplitude=1e-3),
     "tets_fp64": lambda z: vortex_tube_3d(n=10),
+    "polytrope3d_mixed": lambda z: polytrope_3d(n=8, amplitude=1e-3, precision=z.MIXED),
+    "frozen_heated_fp64": lambda z: _heated_frozen(z, z.FP64),
+    "frozen_heated_mixed": lambda z: _heated_frozen(z, z.MIXED),
+    # advected variables do not enter the conserved tendency this call returns
+    "tracers_fp64": _with_tracers,
 }
 
 
@@ -59,6 +79,8 @@ def test_two_calls_in_a_row_match_allocating_entry_point(zlib):
     for name, make in CASES.items():
         _, mesh, scheme, u0 = make(z)
         s = z.Solver(mesh, scheme)
+        if scheme.n_avars:
+            s.set_avars(tracers(mesh, u0, scheme.n_avars))
         states = [u0, _perturbed(u0, seed=len(name))]
         got = []
         for u in states:  # two calls in a row of the new entry point

@@ -24,7 +24,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CXXFLAGS = ["-std=c++17", "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
-NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
+NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "--compress-mode=size", "-Xcompiler", "-fPIC,-fopenmp,-ffp-contract=off",
              "--expt-relaxed-constexpr"]
 
 HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp", "snapshot.cpp"]

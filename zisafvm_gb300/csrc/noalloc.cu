@@ -16,7 +16,10 @@
 // library, held until the process exits).  The three stage kernels are the
 // same ones the solver's other entry points run; only their scratch pointers
 // point into this array.  The call only reads the solver's state and writes
-// its device clock (status flags), like zfvm_rate_of_change.
+// its device clock (status flags), like zfvm_rate_of_change; with an
+// equilibrium refresh schedule (steps_per_recompute > 1) it also advances the
+// schedule and keeps the equilibrium in the solver's own buffers, as every
+// reconstruction does.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -37,12 +40,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mutex;
 unsigned char *g_scratch_address[kMaxDevices] = {};
 
-// Device address of the array on the current device.  The first call on a
-// device looks it up (cudaGetSymbolAddress, which also loads this file's code
-// on that device); later calls reuse it.
-unsigned char *scratch_address() {
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
+// Device address of the array on device `dev`, which must be the current
+// device.  The first call on a device looks it up (cudaGetSymbolAddress, which
+// also loads this file's code on that device); later calls reuse it.
+unsigned char *scratch_address(int dev) {
   if (dev < 0 || dev >= kMaxDevices) throw CudaError{cudaErrorInvalidDevice, "device ordinal beyond 64"};
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
   if (!g_scratch_address[dev]) {
@@ -105,7 +106,9 @@ Layout plan(const zfvm_solver *s, unsigned char *base) {
     L.fv = c.take<double>(fpts);
     if (s->has_src) L.src = c.take<double>(nv * ld);
   }
-  if (s->has_eq) L.eqth = c.take<double>(4 * ld);
+  // with an equilibrium schedule the equilibrium outlives the call: the
+  // solver's own buffer holds it
+  if (s->has_eq && !s->sched_count.p) L.eqth = c.take<double>(4 * ld);
   L.aos = c.take<double>((size_t)5 * s->n_cells);
   L.bytes = c.used;
   return L;
@@ -121,60 +124,52 @@ __global__ void k_tendency_rows(const double *soa, double *aos, int n, int ld, i
   for (int v = 0; v < 5; ++v) aos[(size_t)i * 5 + v] = r[v];
 }
 
-void launch_stage(zfvm_solver *s, StageArgs &a) {
-  const LaunchCfg c{s->n_cells, s->n_edges, s->has_eq, s->has_src, s->mixed,
-                    s->scheme.flux == ZFVM_FLUX_HLLC ? 0 : 1, s->stream, nullptr};
-  switch (s->shape_id) {
-    case 0: launch_stage_s2o3(s->D, s->P, a, c); break;
-    case 1: launch_stage_s2o2(s->D, s->P, a, c); break;
-    case 2: launch_stage_s3o3(s->D, s->P, a, c); break;
-    case 3: launch_stage_s3o2(s->D, s->P, a, c); break;
-  }
-  CK(cudaGetLastError());
-}
-
 }  // namespace
 
 extern "C" int zfvm_rate_of_change_noalloc(zfvm_solver *s, double *tendency) {
   if (!s || !tendency) return fail(ZFVM_EINVAL, "null argument");
+  SOLVER_GUARD_BEGIN
   const Layout need = plan(s, nullptr);
   if (need.bytes > (size_t)ZFVM_NOALLOC_SCRATCH_BYTES)
     return fail(ZFVM_EINVAL, "zfvm_rate_of_change_noalloc: this solver needs " + std::to_string(need.bytes) +
                                  " bytes of stage scratch (" + std::to_string(s->n_cells) +
                                  " cells), more than the fixed " + std::to_string(ZFVM_NOALLOC_SCRATCH_BYTES) +
                                  " bytes; use zfvm_rate_of_change");
-  try {
-    const Layout L = plan(s, scratch_address());
-    Clock c = read_clock(s);
-    c.done = 0;
-    c.status = 0;
-    write_clock(s, c);
-    CK(cudaMemsetAsync(L.tend, 0, L.zero_bytes, s->stream));
-    StageArgs a = stage_args(s, 0, L.tend);
-    a.fv = L.fv;
-    a.fv32 = L.fv32;
-    a.dev0 = L.dev0;
-    a.dev032 = L.dev032;
-    a.eq32 = L.eq32;
-    a.nf = L.nf;
-    a.src = L.src;
-    a.eqth = L.eqth;
-    a.g32 = L.g32;
-    a.mL32 = L.mL32;
-    a.mR32 = L.mR32;
-    a.src32 = L.src32;
-    for (int k = 0; k < 4; ++k) a.k[k] = nullptr, a.k32[k] = nullptr;
-    launch_stage(s, a);
-    const int n = s->n_cells;
-    k_tendency_rows<<<(n + 127) / 128, 128, 0, s->stream>>>(L.tend, L.aos, n, s->ld, s->nv);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(tendency, L.aos, (size_t)n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    const Clock c2 = read_clock(s);
-    std::string msg;
-    const int code = status_to_code(c2.status, msg);
-    if (code) return fail(code, msg);
-    return ZFVM_OK;
-  } catch (const CudaError &e) {
-    return fail(ZFVM_ECUDA, e.where + ": " + cudaGetErrorString(e.err));
-  }
+  // the array handed to the kernels must be the one on the solver's device
+  int current = -1;
+  CK(cudaGetDevice(&current));
+  if (current != s->device)
+    return fail(ZFVM_EINVAL, "zfvm_rate_of_change_noalloc: the solver lives on device " + std::to_string(s->device) +
+                                 " but device " + std::to_string(current) + " is current");
+  const Layout L = plan(s, scratch_address(s->device));
+  Clock c = read_clock(s);
+  c.done = 0;
+  c.status = 0;
+  write_clock(s, c);
+  CK(cudaMemsetAsync(L.tend, 0, L.zero_bytes, s->stream));
+  StageArgs a = stage_args(s, 0, L.tend);
+  a.fv = L.fv;
+  a.fv32 = L.fv32;
+  a.dev0 = L.dev0;
+  a.dev032 = L.dev032;
+  a.eq32 = L.eq32;
+  a.nf = L.nf;
+  a.src = L.src;
+  if (L.eqth) a.eqth = L.eqth;
+  a.g32 = L.g32;
+  a.mL32 = L.mL32;
+  a.mR32 = L.mR32;
+  a.src32 = L.src32;
+  for (int k = 0; k < 4; ++k) a.k[k] = nullptr, a.k32[k] = nullptr;
+  solver_dispatch_stage(s, a);
+  const int n = s->n_cells;
+  k_tendency_rows<<<(n + 127) / 128, 128, 0, s->stream>>>(L.tend, L.aos, n, s->ld, s->nv);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(tendency, L.aos, (size_t)n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  const Clock c2 = read_clock(s);
+  std::string msg;
+  const int code = status_to_code(c2.status, msg);
+  if (code) return fail(code, msg);
+  return ZFVM_OK;
+  SOLVER_GUARD_END
 }

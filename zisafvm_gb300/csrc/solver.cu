@@ -119,6 +119,8 @@ StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out) {
   a.dev032 = s->dev032.p;
   a.eq32 = s->eq32.p;
   a.uprev = s->uprev.p;
+  a.sched_count = s->sched_count.p;
+  a.sched = s->sched.p;
   a.nf = s->nfb.p;
   a.src = s->has_src ? s->srcb.p : nullptr;
   a.eqth = s->has_eq ? s->eqth.p : nullptr;
@@ -240,6 +242,8 @@ void enqueue_step(zfvm_solver *s) {
 
 void solver_restore_on(zfvm_solver *s, cudaStream_t stream) { enqueue_restore(s, stream); }
 
+void solver_dispatch_stage(zfvm_solver *s, StageArgs &a) { dispatch_stage(s, a); }
+
 void solver_tracers_on(zfvm_solver *s, int stage, cudaStream_t stream) {
   StageArgs a = stage_args(s, stage, nullptr);
   dispatch_tracers(s, a, nullptr, stream);
@@ -352,8 +356,7 @@ int build_solver(zfvm_solver *s) {
 
   // ---- scheme parameters
   if (sc.rk_stages < 1 || sc.rk_stages > 3) return fail(ZFVM_EINVAL, "rk_stages must be 1, 2 or 3");
-  if (sc.steps_per_recompute != 1)
-    return fail(ZFVM_EINVAL, "steps_per_recompute must be 1 (the equilibrium is refreshed every stage)");
+  if (sc.steps_per_recompute < 1) return fail(ZFVM_EINVAL, "steps_per_recompute must be at least 1");
   s->has_eq = sc.equilibrium == ZFVM_EQ_ISENTROPIC;
   s->mixed = sc.precision == ZFVM_MIXED;
   s->has_src = sc.gravity != ZFVM_GRAVITY_NONE;
@@ -388,6 +391,8 @@ int build_solver(zfvm_solver *s) {
   P.eps32 = (float)P.epsilon;
   P.gamma32 = (float)P.gamma;
   P.exp4 = P.exponent == 4.0 ? 1 : 0;
+  P.steps_per_recompute = sc.steps_per_recompute;
+  P.recompute_threshold = sc.recompute_threshold;
   std::memset(P.a, 0, sizeof(P.a));
   std::memset(P.b, 0, sizeof(P.b));
   if (sc.rk_stages == 1) {
@@ -535,6 +540,7 @@ int build_solver(zfvm_solver *s) {
       for (int q = 0; q < nqf; ++q) h_phi_fq[(size_t)q * lde + e] = phi(g.face_qx[e * nqf + q]);
   }
 
+  CK(cudaGetDevice(&s->device));
   CK(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
   CK(cudaEventCreateWithFlags(&s->ev_in, cudaEventDisableTiming));
   CK(cudaEventCreateWithFlags(&s->ev_sync, cudaEventDisableTiming));
@@ -582,6 +588,13 @@ int build_solver(zfvm_solver *s) {
     if (!s->mixed) s->srcb.alloc((size_t)nv * ld);
   }
   if (s->has_eq) s->eqth.alloc((size_t)4 * ld);
+  if (s->has_eq && sc.steps_per_recompute > 1) {
+    // zero counts: the first reconstruction of every cell refreshes
+    s->sched_count.alloc(ld);
+    s->sched_count.zero(s->stream);
+    s->sched.alloc((size_t)4 * ld);
+    s->sched.zero(s->stream);
+  }
   s->u0.alloc((size_t)nv * ld);
   s->ux.alloc((size_t)nv * ld);
   if (!s->mixed) s->kbuf.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
@@ -741,6 +754,7 @@ int build_solver(zfvm_solver *s) {
   add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n + s->eq32.n + s->phi_fq2.n));
   add(4 * s->dev032.n);
   add(8 * s->uprev.n);
+  add(4 * s->sched_count.n + 8 * s->sched.n);
   add(8 * s->heat_w.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
            s->frame.n + s->farea.n + s->phi_cq.n + s->gphi_cq.n + s->cqx.n + s->cqw.n + s->phi_fq.n + s->u0.n +
@@ -748,10 +762,6 @@ int build_solver(zfvm_solver *s) {
   add(8 * (s->tq0.n + s->tqx.n + s->tk.n + s->tfv.n + s->tnf.n + s->ttend.n + s->tprev.n));
   s->device_bytes = bytes;
   return ZFVM_OK;
-}
-
-int cuda_fail(const CudaError &e) {
-  return fail(ZFVM_ECUDA, e.where + ": " + cudaGetErrorString(e.err));
 }
 
 }  // namespace
@@ -781,19 +791,6 @@ void build_graph(zfvm_solver *s, int steps) {
 }
 
 }  // namespace
-
-#define SOLVER_GUARD_BEGIN try {
-#define SOLVER_GUARD_END                                  \
-  }                                                       \
-  catch (const CudaError &e) {                            \
-    return cuda_fail(e);                                  \
-  }                                                       \
-  catch (const SetupError &e) {                           \
-    return fail(ZFVM_ESETUP, e.what());                   \
-  }                                                       \
-  catch (const std::bad_alloc &) {                        \
-    return fail(ZFVM_ENOMEM, "host allocation failed");   \
-  }
 
 extern "C" int zfvm_solver_create(zfvm_mesh *m, const zfvm_scheme_desc *sc, zfvm_solver **out) {
   if (!m || !sc || !out) return fail(ZFVM_EINVAL, "null argument");
@@ -1184,6 +1181,7 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
     if (!mixed) b += 8 * nv * ld;                                               // srcb
   }
   if (has_eq) b += 8 * 4 * ld;                                                  // eqth
+  if (has_eq && sc.steps_per_recompute > 1) b += 4 * ld + 8 * 4 * ld;           // sched_count, sched
   if (sc.step_rejection_drho > 0.0) b += 8 * nv * ld;                            // uprev
   if (sc.heating_rate != 0.0 && has_src) b += 8 * nqc * ld;                       // heat_w
   if (mixed) {

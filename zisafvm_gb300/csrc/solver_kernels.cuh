@@ -166,6 +166,12 @@ struct Params {
   // FP32 copies for the mixed form, rounded once on the host
   float lw32[5], inv_lw0_32, eps32, gamma32;
   int exp4;          // exponent == 4
+  // equilibrium refresh schedule (LocalRCParams, local_reconstruction.hpp:18-21):
+  // refresh every steps_per_recompute reconstructions, or sooner when the
+  // scaled (rho, E_int) of the cell leave its equilibrium average by
+  // recompute_threshold; 1 refreshes at every reconstruction
+  int steps_per_recompute;
+  double recompute_threshold;
 };
 
 struct StageArgs {
@@ -196,6 +202,12 @@ struct StageArgs {
   double *poly_out;
   // step rejection: the last stage saves the step's start state here [NV][ld]
   double *uprev;
+  // equilibrium refresh schedule (only with steps_per_recompute > 1): the
+  // reconstructions since the last refresh [ld], and per cell the scale
+  // (rho, E_int) and the equilibrium's own cell average (rho, E_int) of the
+  // last refresh [4][ld]; eqth then holds the equilibrium between stages
+  int *sched_count;
+  double *sched;
   double coef[4];    // RK row of this stage: a[stage + 1][.] or b[.] at the last stage
   float coef32[4];   // the same row rounded to FP32 (mixed form)
   int stage;
@@ -483,10 +495,28 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     set_status(d.clock, kStNonPhysical);
     return;
   }
+  // LocalReconstruction::recompute_equilibrium (local_reconstruction.hpp:87-100):
+  // with a schedule the equilibrium and the scaling of the last refresh stay
+  // until steps_per_recompute reconstructions have passed, or until the
+  // scaled distance of (rho, E_int) from the equilibrium's own cell average
+  // reaches recompute_threshold
+  bool refresh = true;
+  double rho_s = rho, eint_s = eint;
+  if (EQ && a.sched_count) {
+    const int cnt = a.sched_count[i];
+    if (cnt % P.steps_per_recompute != 0) {
+      rho_s = a.sched[i];
+      eint_s = a.sched[ld + i];
+      const double d0 = (rho - a.sched[2 * ld + i]) / rho_s, d1 = (eint - a.sched[3 * ld + i]) / eint_s;
+      refresh = sqrt(d0 * d0 + d1 * d1) >= P.recompute_threshold;
+      if (refresh) rho_s = rho, eint_s = eint;
+    }
+    a.sched_count[i] = refresh ? 1 : cnt + 1;
+  }
   // EulerScaling (model/characteristic_scale.hpp:23-32): {rho, c, c, c, E_int}
   R inv_s2[NV];
   {
-    const R rr = R(rho), ee = R(eint), g = MIXED ? R(P.gamma32) : R(gamma);
+    const R rr = R(rho_s), ee = R(eint_s), g = MIXED ? R(P.gamma32) : R(gamma);
     const R cs = sqrt(g * (ee * (g - R(1))) / rr);
     inv_s2[0] = R(1) / (rr * rr);
 #pragma unroll
@@ -506,7 +536,10 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   // h_r = T + <phi> and f = (gamma - 1) / (gamma K) = rho_bar / T.
   bool closed = false;
   double f_closed = 0.0;
-  if (EQ && MIXED && P.gamma2) {
+  if (EQ && !refresh) {
+    // the equilibrium of the last refresh, as it was bound then
+    phi_ref = d.phi_cq[i];
+  } else if (EQ && MIXED && P.gamma2) {
     phi_ref = d.phi_cq[i];
     const double m1 = d.phi_m1[i], var = d.phi_var[i];
     const double disc = eint * eint - rho * rho * var;
@@ -519,18 +552,34 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       closed = true;
     }
   }
-  if (EQ && !closed) {
+  if (EQ && refresh && !closed) {
     phi_ref = d.phi_cq[i];
     int st = solve_equilibrium<S::NQC>(ev, P, d, i, phi_ref, rho, eint, eh, eK);
     found = st == 0;
     if (st == 2) set_status(d.clock, kStNewton);
   }
-  const EqEval::Bound eqb = closed ? EqEval::Bound{eh + phi_ref, f_closed, eK} : ev.bind(eh, eK, phi_ref);
-  if (EQ) {
+  EqEval::Bound eqb;
+  if (EQ && !refresh) {
+    eqb = EqEval::Bound{a.eqth[i], a.eqth[ld + i], a.eqth[2 * ld + i]};
+    found = a.eqth[3 * ld + i] != 0.0;
+  } else {
+    eqb = closed ? EqEval::Bound{eh + phi_ref, f_closed, eK} : ev.bind(eh, eK, phi_ref);
+  }
+  if (EQ && refresh) {
     a.eqth[i] = eqb.hr;
     a.eqth[ld + i] = eqb.f;
     a.eqth[2 * ld + i] = eqb.K;
     a.eqth[3 * ld + i] = found ? 1.0 : 0.0;
+    if (a.sched_count) {
+      // the scale and the equilibrium's own cell average (rhoEbar_cache(0),
+      // zero when no equilibrium was found) of this refresh
+      double rc = 0.0, Ec = 0.0;
+      if (found) eq_cell_average<S::NQC>(ev, P, d, eqb, j0, rc, Ec);
+      a.sched[i] = rho_s;
+      a.sched[ld + i] = eint_s;
+      a.sched[2 * ld + i] = rc;
+      a.sched[3 * ld + i] = Ec;
+    }
   }
   // deviation of a stencil cell's average from this cell's equilibrium (FP64)
   auto load_dev = [&](int j, double *out) {

@@ -5,6 +5,7 @@
 
 #include <cuda_runtime.h>
 
+#include <new>
 #include <string>
 #include <vector>
 
@@ -68,6 +69,7 @@ struct zfvm_solver {
   int nd = 2, nv = 4, nf = 3, nqf = 2, nqc = 3, ld = 0, lde = 0;
   int n_cells = 0, n_edges = 0;
   int shape_id = -1;
+  int device = -1;  // the device current at creation, which owns every buffer and the stream
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_in = nullptr;    // recorded after a host upload
   cudaEvent_t ev_sync = nullptr;  // recorded by a batch before it uses the solver
@@ -87,6 +89,8 @@ struct zfvm_solver {
   zfvm::DBuf<double> poly;                // exported reconstruction records (zfvm_reconstruct)
   zfvm::DBuf<double> uprev;               // step rejection: start state of the running step
   zfvm::DBuf<double> heat_w;              // heating: w_q * rate(x_q) at the cell quadrature points
+  zfvm::DBuf<int> sched_count;            // equilibrium schedule: reconstructions since the last refresh
+  zfvm::DBuf<double> sched;               // equilibrium schedule: scale and own average of the last refresh [4][ld]
   // advected variables (n_avars > 0): state, next stage, stage tendencies,
   // face-point values, face fluxes, tendency output, step-rejection save
   int na = 0;
@@ -117,6 +121,10 @@ struct zfvm_solver {
 
 // helpers shared with the batch engine (solver.cu)
 zfvm::dev::StageArgs stage_args(zfvm_solver *s, int stage, double *tend_out);
+// the three kernels of one stage on the solver's stream, with the solver's
+// launch configuration (the entry point without allocation swaps the scratch
+// pointers of `a` and launches through this)
+void solver_dispatch_stage(zfvm_solver *s, zfvm::dev::StageArgs &a);
 zfvm::dev::TracerArgs tracer_args(zfvm_solver *s, int stage, double *tend_out);
 // per-solver launches the batch engine adds on its own stream: the restore of
 // a rejected step (after the clock), the advected variables' kernels of a
@@ -132,3 +140,21 @@ void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double f
 int status_to_code(int st, std::string &msg);
 // device bytes zfvm_solver_create allocates for this mesh and scheme (-1: no stencils)
 int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc);
+
+// The C ABI's error guard: every failure inside an entry point becomes a status
+// code and a zfvm_last_error message, nothing escapes the extern "C" boundary.
+inline int cuda_fail(const zfvm::CudaError &e) {
+  return zfvm::fail(ZFVM_ECUDA, e.where + ": " + cudaGetErrorString(e.err));
+}
+#define SOLVER_GUARD_BEGIN try {
+#define SOLVER_GUARD_END                                  \
+  }                                                       \
+  catch (const zfvm::CudaError &e) {                      \
+    return cuda_fail(e);                                  \
+  }                                                       \
+  catch (const zfvm::SetupError &e) {                     \
+    return zfvm::fail(ZFVM_ESETUP, e.what());             \
+  }                                                       \
+  catch (const std::bad_alloc &) {                        \
+    return zfvm::fail(ZFVM_ENOMEM, "host allocation failed"); \
+  }
