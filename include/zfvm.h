@@ -125,6 +125,11 @@ int zfvm_mesh_get_faces(const zfvm_mesh *m, int64_t *left, int64_t *right, doubl
  * kind 1: polytrope rho = rho_c - k r^2 / 4 ... for gamma = 2, K and phi = k r^2/2,
  *         plus a Gaussian pressure bump;
  *         dparams = {gamma, K, rho_c, k_phi, amplitude, width, x0, y0}
+ * kind 2: isentropic polytrope in one of the radial potentials, h(x) = h_c + phi(0) - phi(x)
+ *         with h_c the enthalpy of rho_c (for POLYTROPE_RADIAL and gamma = 2 the
+ *         Lane-Emden profile rho = rho_c sin(a r) / (a r)), plus the same bump;
+ *         dparams = {gamma, K, rho_c, amplitude, width, x0, y0, zfvm_gravity kind,
+ *                    gravity_strength, gravity_params[0..4]} (no RADIAL_TABLE)
  * Output: n_cells x 5 AoS. */
 int zfvm_initial_conditions(const zfvm_mesh *m, int32_t kind, const double *dparams,
                             double *cvars);
@@ -132,7 +137,27 @@ int zfvm_initial_conditions(const zfvm_mesh *m, int32_t kind, const double *dpar
 /* ---- scheme ---------------------------------------------------------------- */
 enum zfvm_flux { ZFVM_FLUX_HLLC = 0, ZFVM_FLUX_RUSANOV = 1 };
 enum zfvm_equilibrium { ZFVM_EQ_NONE = 0, ZFVM_EQ_ISENTROPIC = 1 };
-enum zfvm_gravity { ZFVM_GRAVITY_NONE = 0, ZFVM_GRAVITY_CONSTANT_RADIAL = 1, ZFVM_GRAVITY_HARMONIC_RADIAL = 2 };
+/* Radial potentials phi(|x|) (model/gravity_decl.hpp, gravity_impl.hpp; built by
+ * make_gravity, model/euler_factory.cpp:60-121):
+ *   CONSTANT_RADIAL        ConstantGravityRadial: phi = g r (gravity_strength g)
+ *   HARMONIC_RADIAL        phi = k r^2 / 2 (gravity_strength k; no counterpart in the reference)
+ *   POLYTROPE_RADIAL       PolytropeGravityRadial(rhoC, K, G): gravity_params {rhoC, K, G}
+ *   POLYTROPE_JUMP_RADIAL  PolytropeGravityWithJumpRadial(r_crit, rhoC, K_inner, K_outer, G):
+ *                          gravity_params {r_crit, rhoC, K_inner, K_outer, G}
+ *   POINT_MASS_RADIAL      PointMassGravityRadial(G, M, X): gravity_params {G, M, X}
+ *   RADIAL_TABLE           RadialGravity: phi linearly interpolated between the
+ *                          gravity_table_n radii gravity_table_r (increasing) and
+ *                          potentials gravity_table_phi; the solver copies the table
+ *                          at creation and refuses quadrature points beyond its last radius */
+enum zfvm_gravity {
+  ZFVM_GRAVITY_NONE = 0,
+  ZFVM_GRAVITY_CONSTANT_RADIAL = 1,
+  ZFVM_GRAVITY_HARMONIC_RADIAL = 2,
+  ZFVM_GRAVITY_POLYTROPE_RADIAL = 3,
+  ZFVM_GRAVITY_POLYTROPE_JUMP_RADIAL = 4,
+  ZFVM_GRAVITY_POINT_MASS_RADIAL = 5,
+  ZFVM_GRAVITY_RADIAL_TABLE = 6
+};
 enum zfvm_flux_bc { ZFVM_FLUX_BC_NONE = 0, ZFVM_FLUX_BC_CONSTANT = 1, ZFVM_FLUX_BC_ISENTROPIC = 2 };
 /* Ghost cells (the mesh's ghost mask) are periodic images of their interior
  * source cells, or, when a ghost cell is its own source, frozen at the values
@@ -168,6 +193,10 @@ typedef struct {
   double heating_r0, heating_r1; /* heating.lower_boundary / upper_boundary           */
   int32_t n_avars;              /* advected variables (AllVariables::avars columns,
                                    choose_n_avars); 0..ZFVM_MAX_AVARS                */
+  double gravity_params[5];     /* euler.gravity parameters of zfvm_gravity         */
+  const double *gravity_table_r;   /* RADIAL_TABLE: radii, then potentials          */
+  const double *gravity_table_phi;
+  int64_t gravity_table_n;
 } zfvm_scheme_desc;
 #define ZFVM_MAX_AVARS 64
 

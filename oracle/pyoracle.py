@@ -49,6 +49,7 @@ def lib() -> C.CDLL:
         L.zfvm_oracle_eos_roundtrips.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, dp]
         L.zfvm_oracle_quasi_newton_problem.argtypes = [C.c_int, dp]
         L.zfvm_oracle_rule.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), dp, dp]
+        L.zfvm_oracle_gravity.argtypes = [dp, C.c_int64, dp, dp, dp]
         L.zfvm_oracle_last_error.restype = C.c_char_p
         _LIB = L
     return _LIB
@@ -61,6 +62,11 @@ def _dp(a):
 def _check(code):
     if code != 0:
         raise OracleError(code, lib().zfvm_oracle_last_error().decode())
+
+
+# entries the oracle reads from a scheme vector (zfvm_oracle_create's table),
+# a gravity table's radii and potentials following
+SCHEME_VECTOR_MIN = 32
 
 
 class Oracle:
@@ -81,6 +87,8 @@ class Oracle:
         s = arr(raw.source, np.int64) if raw.source is not None else None
         st = {k: arr(x, x.dtype) for k, x in stencils.items()}
         self.scheme = arr(scheme_vector, np.float64)
+        if self.scheme.shape[0] < SCHEME_VECTOR_MIN:
+            raise ValueError(f"scheme vector of {self.scheme.shape[0]} entries; the oracle reads {SCHEME_VECTOR_MIN}")
         h = C.c_void_p()
         _check(L.zfvm_oracle_create(raw.n_dims, v.shape[0], _dp(v), vi.shape[0], vi.ctypes.data,
                                     g.ctypes.data if g is not None else None,
@@ -202,6 +210,16 @@ def equilibrium_average(gamma, gravity_kind, g, theta, x_ref, tri, quad_deg):
     th, xr, t, out = np.asarray(theta, float), np.asarray(x_ref, float), np.asarray(tri, float).ravel(), np.zeros(2)
     lib().zfvm_oracle_equilibrium_average(gamma, gravity_kind, g, _dp(th), _dp(xr), _dp(t), quad_deg, _dp(out))
     return out
+
+
+def gravity(scheme_vector, x):
+    """The oracle's potential and its gradient at points x (n x 3)."""
+    sv = np.ascontiguousarray(scheme_vector, dtype=np.float64)
+    xx = np.ascontiguousarray(np.atleast_2d(x), dtype=np.float64)
+    n = xx.shape[0]
+    phi, grad = np.zeros(n), np.zeros((n, 3))
+    _check(lib().zfvm_oracle_gravity(_dp(sv), n, _dp(xx), _dp(phi), _dp(grad)))
+    return phi, grad
 
 
 def rk_ode_error(stages: int, ode: int, dt: float, t_final: float = 3.0) -> float:

@@ -27,6 +27,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <string>
@@ -436,17 +437,88 @@ static void inv_coord_transform(Cv &u, const XYZ &n, const XYZ &t1, const XYZ &t
   u[1] = ux, u[2] = uy, u[3] = uz;
 }
 
-// Gravity<Base, RadialAlignment> (model/gravity_decl.hpp:17-88, gravity_impl.hpp)
-struct Gravity {
-  int kind = 0;  // 0 none, 1 constant radial (phi = g r), 2 harmonic radial (phi = k r^2 / 2)
-  double g = 0.0;
-  double phi(const XYZ &x) const {
-    double chi = norm(x);
-    return kind == 1 ? g * chi : (kind == 2 ? 0.5 * g * chi * chi : 0.0);
+// Gravity<Base, RadialAlignment> (model/gravity_decl.hpp:17-88, gravity_impl.hpp):
+// chi = |x|, phi(x) = base.phi(chi), dphi/dx_k = base.dphi_dx(chi) x_k / (|x| + 1e-50).
+// Bases: ConstantGravity (gravity_impl.hpp:12-19), the harmonic k chi^2 / 2 (new),
+// PolytropeGravity (:29-58), PolytropeGravityWithJump (:70-92), PointMassGravity
+// (:21-27) and SphericalGravity over NonUniformLinearInterpolation
+// (:94-101, math/linear_interpolation.hpp:14-45).
+struct PolytropeBase {
+  double rhoC = 1.0, K = 1.0, G = 1.0, eps = std::numeric_limits<double>::min();
+  double alpha() const { return std::sqrt(2.0 * M_PI * G / K); }  // gamma == 2
+  double phi(double chi) const {
+    double a = alpha();
+    double chi_eff = a * (chi + eps);
+    return -2.0 * K * rhoC * std::sin(chi_eff) / chi_eff;
   }
+  double dphi_dx(double chi) const {
+    double a = alpha();
+    double chi_eff = a * (chi + eps);
+    double dphi = (std::cos(chi_eff) - std::sin(chi_eff) / chi_eff) / chi_eff;
+    return -2.0 * K * rhoC * dphi * a;
+  }
+};
+
+struct Gravity {
+  // 0 none, 1 constant radial (phi = g r), 2 harmonic radial (phi = k r^2 / 2),
+  // 3 polytrope, 4 polytrope with a jump, 5 point mass, 6 tabulated
+  int kind = 0;
+  double g = 0.0;
+  PolytropeBase inner, outer;
+  double r_crit = 0.0;
+  double GM = 0.0, X = 0.0;
+  std::vector<double> tr, tphi;
+
+  void set_params(const double *a) {
+    if (kind == 3) inner = PolytropeBase{a[0], a[1], a[2]};
+    if (kind == 4) {
+      // PolytropeGravityWithJump::PolytropeGravityWithJump (gravity_impl.hpp:70-76)
+      r_crit = a[0];
+      inner = PolytropeBase{a[1], a[2], a[4]};
+      outer = PolytropeBase{1.0, a[3], a[4]};
+      double rhoC_outer = inner.phi(r_crit) / outer.phi(r_crit);
+      outer = PolytropeBase{rhoC_outer, a[3], a[4]};
+    }
+    if (kind == 5) GM = a[0] * a[1], X = a[2];
+  }
+  // NonUniformLinearInterpolation::index
+  size_t index(double r) const {
+    auto first_past = std::lower_bound(tr.begin(), tr.end(), r);
+    size_t i = (size_t)(first_past - tr.begin());
+    return i == 0 ? 0 : i - 1;
+  }
+  double base_phi(double chi) const {
+    switch (kind) {
+      case 1: return g * chi;
+      case 2: return 0.5 * g * chi * chi;
+      case 3: return inner.phi(chi);
+      case 4: return chi < r_crit ? inner.phi(chi) : outer.phi(chi);
+      case 5: return GM / (X + chi);
+      case 6: {
+        size_t i = index(chi);
+        double alpha = (chi - tr[i]) / (tr[i + 1] - tr[i]);
+        return (1 - alpha) * tphi[i] + alpha * tphi[i + 1];
+      }
+      default: return 0.0;
+    }
+  }
+  double base_dphi(double chi) const {
+    switch (kind) {
+      case 1: return g;
+      case 2: return g * chi;
+      case 3: return inner.dphi_dx(chi);
+      case 4: return chi < r_crit ? inner.dphi_dx(chi) : outer.dphi_dx(chi);
+      case 5: return -GM / ((X + chi) * (X + chi));
+      case 6: {
+        size_t i = index(chi);
+        return (tphi[i + 1] - tphi[i]) / (tr[i + 1] - tr[i]);
+      }
+      default: return 0.0;
+    }
+  }
+  double phi(const XYZ &x) const { return base_phi(norm(x)); }
   XYZ grad_phi(const XYZ &x) const {
-    double chi = norm(x);
-    double d = kind == 1 ? g : (kind == 2 ? g * chi : 0.0);
+    double d = base_dphi(norm(x));
     XYZ r;
     for (int k = 0; k < 3; ++k) r[k] = d * (x[k] / (norm(x) + 1e-50));
     return r;
@@ -1459,6 +1531,8 @@ const char *zfvm_oracle_last_error(void) { return g_oracle_err.c_str(); }
 //  [19] reconstruction (0 CWENO-AO, 1 WENO-AO)
 //  [20] step rejection drho_crit_rel [21] step rejection max exponent
 //  [22] heating rate              [23] heating r0   [24] heating r1
+//  [25] advected variables         [26..30] gravity parameters
+//  [31] gravity table length n     [32..] n radii, then n potentials
 int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, int64_t n_cells, const int64_t *vi,
                        const uint8_t *ghost, const int64_t *source, int qe, int qv, int qm,
                        const int8_t *n_stencils, const int8_t *k_high, const int8_t *n_l2g, const int32_t *l2g,
@@ -1513,6 +1587,14 @@ int zfvm_oracle_create(int n_dims, int64_t n_vertices, const double *vertices, i
     s.heat_r1 = scheme[24];
     s.na = (int)scheme[25];
     if (s.na < 0) throw Error{7, "negative number of advected variables"};
+    // [26..30] gravity parameters, [31] table length n, then n radii and n potentials
+    s.grav.set_params(scheme + 26);
+    if (s.grav.kind == 6) {
+      const int64_t nt = (int64_t)scheme[31];
+      if (nt < 2) throw Error{7, "tabulated gravity needs at least two radii"};
+      s.grav.tr.assign(scheme + 32, scheme + 32 + nt);
+      s.grav.tphi.assign(scheme + 32 + nt, scheme + 32 + 2 * nt);
+    }
     pr.rc.resize(n_cells);
     for (idx i = 0; i < n_cells; ++i) {
       CellRC &rc = pr.rc[i];
@@ -1820,6 +1902,31 @@ int zfvm_oracle_poly_eval(int n_dims, int n_coeffs, const double *coeffs, const 
   p.xc = XYZ{{x_center[0], x_center[1], x_center[2]}};
   p.len = length;
   *out = p.eval(XYZ{{x[0], x[1], x[2]}})[0];
+  return 0;
+}
+
+// The potential of a scheme vector (entries [13], [14], [26..]) and its
+// gradient at n points (n x 3): phi n, grad n x 3.
+int zfvm_oracle_gravity(const double *scheme, int64_t n, const double *x, double *phi, double *grad) {
+  Gravity grav;
+  grav.kind = (int)scheme[13];
+  grav.g = scheme[14];
+  grav.set_params(scheme + 26);
+  if (grav.kind == 6) {
+    const int64_t nt = (int64_t)scheme[31];
+    if (nt < 2) {
+      g_oracle_err = "tabulated gravity needs at least two radii";
+      return 1;
+    }
+    grav.tr.assign(scheme + 32, scheme + 32 + nt);
+    grav.tphi.assign(scheme + 32 + nt, scheme + 32 + 2 * nt);
+  }
+  for (int64_t k = 0; k < n; ++k) {
+    const XYZ xk{{x[3 * k], x[3 * k + 1], x[3 * k + 2]}};
+    phi[k] = grav.phi(xk);
+    const XYZ gk = grav.grad_phi(xk);
+    for (int d = 0; d < 3; ++d) grad[3 * k + d] = gk[d];
+  }
   return 0;
 }
 

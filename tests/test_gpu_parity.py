@@ -368,3 +368,49 @@ def test_zero_threshold_refreshes_every_reconstruction(zlib):
         s.advance(n_steps=5)
         out.append(s.get_state()[0])
     assert np.array_equal(out[0], out[1])
+
+
+def _gravities(z):
+    r = np.linspace(0.0, 1.5, 3001)
+    a = np.sqrt(2 * np.pi)
+    phi = -2.0 * np.sin(a * np.maximum(r, 1e-300)) / (a * np.maximum(r, 1e-300))
+    return {
+        "polytrope": dict(gravity=z.GRAVITY_POLYTROPE_RADIAL, gravity_params=[1.0, 1.0, 1.0]),
+        "jump": dict(gravity=z.GRAVITY_POLYTROPE_JUMP_RADIAL, gravity_params=[0.5, 1.0, 1.0, 2.0, 1.0]),
+        "point_mass": dict(gravity=z.GRAVITY_POINT_MASS_RADIAL, gravity_params=[1.0, 0.5, 1.0]),
+        # RadialGravity: the polytrope potential tabulated on 3001 radii
+        "table": dict(gravity=z.GRAVITY_RADIAL_TABLE, gravity_table=(r, phi)),
+    }
+
+
+@pytest.mark.parametrize("name", ["polytrope", "jump", "point_mass", "table"])
+def test_reference_gravity_potentials(zlib, olib, name):
+    """The reference's radial potentials (PolytropeGravityRadial,
+    PolytropeGravityWithJumpRadial, PointMassGravityRadial, RadialGravity) on
+    the well-balanced disk: right-hand side and steps against the oracle, and
+    the unperturbed isentropic polytrope of the potential at rest in both forms."""
+    from metrics import conserved_rel_errors
+    z = zlib
+    grav = _gravities(z)
+    raw, mesh, scheme, _ = polytrope_2d(n_rings=20)
+    scheme = z.Scheme(**{**scheme.__dict__, **grav[name], "gravity_strength": 0.0})
+    ic = {k: v for k, v in grav["polytrope" if name == "table" else name].items()}
+    u0 = mesh.initial_conditions("polytrope_in", gamma=2.0, K=1.0, rho_c=1.0, amplitude=1e-2, width=0.05,
+                                 x0=0.3, y0=0.0, **ic)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    o = _oracle(olib, raw, mesh, scheme)
+    t_gpu, t_ref = s.rate_of_change(), o.rate_of_change(u0)
+    assert np.abs(t_gpu - t_ref).max() <= 1e-11 * np.abs(t_ref).max()
+    s.advance(n_steps=5)
+    u_gpu, t1 = s.get_state()
+    u_ref, t_ref1, _ = o.run(u0, n_steps=5)
+    l1, linf = conserved_rel_errors(u_gpu, u_ref)
+    assert l1 < TOL_RUN and linf < TOL_RUN, (l1, linf)
+    assert abs(t1 - t_ref1) <= 1e-12 * t_ref1
+    if name != "table":  # the tabulated potential is not the one the data were built in
+        u_eq = mesh.initial_conditions("polytrope_in", gamma=2.0, K=1.0, rho_c=1.0, amplitude=0.0, **ic)
+        for prec in (z.FP64, z.MIXED):
+            se = z.Solver(mesh, z.Scheme(**{**scheme.__dict__, "precision": prec}))
+            se.set_state(u_eq)
+            assert np.abs(se.rate_of_change()).max() < 1e-10, (name, prec)

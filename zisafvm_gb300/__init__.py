@@ -32,6 +32,8 @@ MAX_STENCIL_SIZE = 24
 FLUX_HLLC, FLUX_RUSANOV = 0, 1
 EQ_NONE, EQ_ISENTROPIC = 0, 1
 GRAVITY_NONE, GRAVITY_CONSTANT_RADIAL, GRAVITY_HARMONIC_RADIAL = 0, 1, 2
+# PolytropeGravityRadial, PolytropeGravityWithJumpRadial, PointMassGravityRadial, RadialGravity
+GRAVITY_POLYTROPE_RADIAL, GRAVITY_POLYTROPE_JUMP_RADIAL, GRAVITY_POINT_MASS_RADIAL, GRAVITY_RADIAL_TABLE = 3, 4, 5, 6
 FLUX_BC_NONE, FLUX_BC_CONSTANT, FLUX_BC_ISENTROPIC = 0, 1, 2
 BC_NONE, BC_PERIODIC, BC_FROZEN = 0, 1, 2
 FP64, MIXED = 0, 1
@@ -83,7 +85,9 @@ class _SchemeDesc(C.Structure):
                 ("steps_per_recompute", C.c_int32), ("recompute_threshold", C.c_double),
                 ("reconstruction", C.c_int32), ("step_rejection_drho", C.c_double),
                 ("step_rejection_max_exponent", C.c_int32), ("heating_rate", C.c_double),
-                ("heating_r0", C.c_double), ("heating_r1", C.c_double), ("n_avars", C.c_int32)]
+                ("heating_r0", C.c_double), ("heating_r1", C.c_double), ("n_avars", C.c_int32),
+                ("gravity_params", C.c_double * 5), ("gravity_table_r", C.POINTER(C.c_double)),
+                ("gravity_table_phi", C.POINTER(C.c_double)), ("gravity_table_n", C.c_int64)]
 
 
 _LIB = None
@@ -326,7 +330,8 @@ class Mesh:
         return {"left": left, "right": right, "normals": normals, "areas": areas}
 
     def initial_conditions(self, kind: str, **p) -> np.ndarray:
-        """Cell averages (n_cells x 5) of 'vortex' or 'polytrope' initial data."""
+        """Cell averages (n_cells x 5) of 'vortex', 'polytrope' (phi = k r^2 / 2) or
+        'polytrope_in' (any analytic radial potential) initial data."""
         if kind == "vortex":
             params = [p.get("gamma", 1.4), p.get("beta", 5.0), p.get("x0", 0.5), p.get("y0", 0.5),
                       p.get("length", 0.1), p.get("rho_inf", 1.0), p.get("u_inf", 1.0), p.get("v_inf", 1.0),
@@ -336,6 +341,13 @@ class Mesh:
             params = [p.get("gamma", 2.0), p.get("K", 1.0), p.get("rho_c", 1.0), p.get("k_phi", 1.0),
                       p.get("amplitude", 1e-4), p.get("width", 0.05), p.get("x0", 0.3), p.get("y0", 0.0)]
             k = 1
+        elif kind == "polytrope_in":
+            # isentropic polytrope in a radial potential: gravity=GRAVITY_*, strength, params
+            gp = (list(p.get("gravity_params", [])) + [0.0] * 5)[:5]
+            params = [p.get("gamma", 2.0), p.get("K", 1.0), p.get("rho_c", 1.0), p.get("amplitude", 1e-4),
+                      p.get("width", 0.05), p.get("x0", 0.3), p.get("y0", 0.0), p["gravity"],
+                      p.get("gravity_strength", 0.0), *gp]
+            k = 2
         else:
             raise ValueError(kind)
         out = np.zeros((self.n_cells, 5))
@@ -370,6 +382,11 @@ class Scheme:
     heating_r0: float = 0.0
     heating_r1: float = 0.0
     n_avars: int = 0  # advected variables (mass-weighted tracers)
+    # parameters of the gravity kind: (rhoC, K, G) polytrope; (r_crit, rhoC,
+    # K_inner, K_outer, G) polytrope with a jump; (G, M, X) point mass
+    gravity_params: list = field(default_factory=lambda: [0.0] * 5)
+    # GRAVITY_RADIAL_TABLE: (radii, potentials), radii increasing
+    gravity_table: tuple | None = None
 
     def desc(self) -> _SchemeDesc:
         d = _SchemeDesc()
@@ -377,8 +394,20 @@ class Scheme:
             if f == "linear_weights":
                 for k, w in enumerate(self.linear_weights):
                     d.linear_weights[k] = w
+            elif f == "gravity_params":
+                for k, w in enumerate(self.gravity_params):
+                    d.gravity_params[k] = w
+            elif f in ("gravity_table_r", "gravity_table_phi", "gravity_table_n"):
+                continue
             else:
                 setattr(d, f, getattr(self, f))
+        if self.gravity_table is not None:
+            r = np.ascontiguousarray(self.gravity_table[0], dtype=np.float64)
+            phi = np.ascontiguousarray(self.gravity_table[1], dtype=np.float64)
+            if r.shape != phi.shape or r.ndim != 1:
+                raise ValueError("gravity_table: radii and potentials of the same length")
+            d._table = (r, phi)  # the arrays live as long as the descriptor
+            d.gravity_table_r, d.gravity_table_phi, d.gravity_table_n = _dp(r), _dp(phi), len(r)
         return d
 
     def oracle_vector(self) -> np.ndarray:
@@ -387,8 +416,15 @@ class Scheme:
                          self.rk_stages, self.cfl_number, self.equilibrium, self.gravity, self.gravity_strength,
                          self.flux_bc, self.boundary, self.steps_per_recompute, self.recompute_threshold,
                          self.reconstruction, self.step_rejection_drho, self.step_rejection_max_exponent,
-                         self.heating_rate, self.heating_r0, self.heating_r1, self.n_avars],
+                         self.heating_rate, self.heating_r0, self.heating_r1, self.n_avars,
+                         *(list(self.gravity_params) + [0.0] * 5)[:5], *self._table_vector()],
                         dtype=np.float64)
+
+    def _table_vector(self) -> list:
+        if self.gravity_table is None:
+            return [0.0]
+        r, phi = (np.asarray(a, dtype=np.float64) for a in self.gravity_table)
+        return [float(len(r)), *r.tolist(), *phi.tolist()]
 
 
 class Solver:

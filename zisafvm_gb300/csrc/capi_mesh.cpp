@@ -7,6 +7,7 @@
 #include <memory>
 #include <new>
 
+#include "gravity.hpp"
 #include "mesh_obj.hpp"
 
 namespace zfvm {
@@ -297,6 +298,23 @@ extern "C" int zfvm_mesh_get_faces(const zfvm_mesh *m, int64_t *left, int64_t *r
 extern "C" int zfvm_initial_conditions(const zfvm_mesh *m, int32_t kind, const double *p, double *cv) {
   if (!m || !p || !cv) return fail(ZFVM_EINVAL, "null argument");
   const auto &g = m->grid;
+  // kind 2: the potential of the polytrope
+  RadialPotential pot;
+  double h_top = 0.0;  // h_c + phi(0)
+  if (kind == 2) {
+    zfvm_scheme_desc sc{};
+    sc.gravity = (int32_t)p[7];
+    sc.gravity_strength = p[8];
+    for (int k = 0; k < 5; ++k) sc.gravity_params[k] = p[9 + k];
+    if (sc.gravity == ZFVM_GRAVITY_RADIAL_TABLE) return fail(ZFVM_EINVAL, "no polytrope initial data for a tabulated potential");
+    try {
+      pot = RadialPotential::from_scheme(sc);
+    } catch (const SetupError &e) {
+      return fail(ZFVM_EINVAL, e.what());
+    }
+    const double gamma = p[0], K = p[1], rho_c = p[2];
+    h_top = gamma / (gamma - 1.0) * K * std::pow(rho_c, gamma - 1.0) + pot.phi_r(0.0);
+  }
   const int nq = g.n_cell_qp;
   for (index_t i = 0; i < g.n_cells; ++i) {
     double acc[5] = {0, 0, 0, 0, 0};
@@ -330,6 +348,17 @@ extern "C" int zfvm_initial_conditions(const zfvm_mesh *m, int32_t kind, const d
         double r2 = x.x * x.x + x.y * x.y + x.z * x.z;
         double h_c = gamma / (gamma - 1.0) * K * std::pow(rho_c, gamma - 1.0);
         double h = h_c - 0.5 * kphi * r2;
+        double rho = std::pow((gamma - 1.0) / (gamma * K) * h, 1.0 / (gamma - 1.0));
+        double pr = K * std::pow(rho, gamma);
+        double d2 = ((x.x - x0) * (x.x - x0) + (x.y - y0) * (x.y - y0)) / (width * width);
+        pr *= 1.0 + A * std::exp(-d2);
+        u[0] = rho;
+        u[1] = u[2] = u[3] = 0.0;
+        u[4] = pr / (gamma - 1.0);
+      } else if (kind == 2) {
+        // isentropic polytrope in the potential: h + phi = h_c + phi(0)
+        double gamma = p[0], K = p[1], A = p[3], width = p[4], x0 = p[5], y0 = p[6];
+        double h = h_top - pot.phi(x);
         double rho = std::pow((gamma - 1.0) / (gamma * K) * h, 1.0 / (gamma - 1.0));
         double pr = K * std::pow(rho, gamma);
         double d2 = ((x.x - x0) * (x.x - x0) + (x.y - y0) * (x.y - y0)) / (width * width);

@@ -46,6 +46,7 @@ struct Request {
   int64_t id = 0;
   zfvm_mesh *mesh = nullptr;
   zfvm_scheme_desc scheme{};
+  std::vector<double> gravity_table;  // a tabulated potential, owned here (scheme points into it)
   std::vector<double> state;  // initial state; the final state once done
   double t0 = 0.0, t_end = 0.0;
   int64_t n_steps = 0;
@@ -392,6 +393,15 @@ extern "C" int zfvm_server_submit(zfvm_server *S, zfvm_mesh *mesh, const zfvm_sc
     auto r = std::make_unique<Request>();
     r->mesh = mesh;
     r->scheme = *scheme;
+    if (scheme->gravity == ZFVM_GRAVITY_RADIAL_TABLE && scheme->gravity_table_n > 0 && scheme->gravity_table_r &&
+        scheme->gravity_table_phi) {
+      // the solver is created later, on the set-up thread: keep the caller's table
+      const size_t n = (size_t)scheme->gravity_table_n;
+      r->gravity_table.assign(scheme->gravity_table_r, scheme->gravity_table_r + n);
+      r->gravity_table.insert(r->gravity_table.end(), scheme->gravity_table_phi, scheme->gravity_table_phi + n);
+      r->scheme.gravity_table_r = r->gravity_table.data();
+      r->scheme.gravity_table_phi = r->gravity_table.data() + n;
+    }
     r->n_cells = mesh->grid.n_cells;
     r->state.assign(cvars, cvars + (size_t)r->n_cells * 5);
     r->t0 = t0;

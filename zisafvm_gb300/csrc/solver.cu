@@ -362,6 +362,8 @@ int build_solver(zfvm_solver *s) {
   s->has_src = sc.gravity != ZFVM_GRAVITY_NONE;
   if (s->has_eq && !s->has_src) return fail(ZFVM_EINVAL, "isentropic well-balancing needs gravity");
   if (sc.heating_rate != 0.0 && !s->has_src) return fail(ZFVM_EINVAL, "heating needs a gravity source in this build");
+  if (sc.gravity < ZFVM_GRAVITY_NONE || sc.gravity > ZFVM_GRAVITY_RADIAL_TABLE)
+    return fail(ZFVM_EINVAL, "unknown gravity kind");
   if (sc.flux_bc == ZFVM_FLUX_BC_ISENTROPIC && !s->has_eq)
     return fail(ZFVM_EINVAL, "isentropic flux boundary needs isentropic well-balancing");
   Params &P = s->P;
@@ -496,20 +498,26 @@ int build_solver(zfvm_solver *s) {
       for (int k = 0; k < nd; ++k) h_frame[((size_t)a2 * nd + k) * lde + e] = fr[a2][k];
     h_farea[e] = g.face_area[e];
   }
-  // ---- gravity potential at quadrature points (phi = g r or k r^2 / 2 radially)
+  // ---- gravity potential and its gradient at the quadrature points
   const int nqc = s->nqc;
   std::vector<double> h_phi_cq, h_phi_m1, h_phi_var, h_gphi_cq, h_cqx, h_cqw, h_phi_fq;
+  try {
+    s->pot = RadialPotential::from_scheme(sc);
+  } catch (const SetupError &e) {
+    return fail(ZFVM_EINVAL, e.what());  // a configuration error, not a failed set-up
+  }
   if (s->has_src) {
-    auto phi = [&](const Vec3 &x) {
-      double r = norm(x);
-      return sc.gravity == ZFVM_GRAVITY_CONSTANT_RADIAL ? sc.gravity_strength * r : 0.5 * sc.gravity_strength * r * r;
-    };
-    auto gphi = [&](const Vec3 &x, int dir) {
-      // Gravity::dphi_dx = phi'(r) x_dir / (r + 1e-50)  (model/gravity_decl.hpp:24-36,85-88)
-      double r = norm(x);
-      double dphi = sc.gravity == ZFVM_GRAVITY_CONSTANT_RADIAL ? sc.gravity_strength : sc.gravity_strength * r;
-      return dphi * (x[dir] / (r + 1e-50));
-    };
+    const RadialPotential &pot = s->pot;
+    for (index_t i = 0; i < n; ++i)
+      for (int q = 0; q < nqc; ++q)
+        if (!pot.covers(norm(g.cell_qx[i * nqc + q])))
+          return fail(ZFVM_EINVAL, "the tabulated potential ends before the mesh does");
+    for (index_t e = 0; e < g.n_edges; ++e)
+      for (int q = 0; q < g.n_face_qp; ++q)
+        if (!pot.covers(norm(g.face_qx[e * g.n_face_qp + q])))
+          return fail(ZFVM_EINVAL, "the tabulated potential ends before the mesh does");
+    auto phi = [&](const Vec3 &x) { return pot.phi(x); };
+    auto gphi = [&](const Vec3 &x, int dir) { return pot.dphi_dx(x, dir); };
     h_phi_cq.assign((size_t)nqc * ld, 0.0);
     h_phi_m1.assign(ld, 0.0);
     h_phi_var.assign(ld, 0.0);
@@ -1245,9 +1253,7 @@ int eval_records(const zfvm_solver *s, int64_t n, const int64_t *cells, const do
       w[v] = acc;
     }
     if (at(PR::EQ + 3) != 0.0) {
-      const double r = std::sqrt(x[3 * k] * x[3 * k] + x[3 * k + 1] * x[3 * k + 1] + x[3 * k + 2] * x[3 * k + 2]);
-      const double phi = sc.gravity == ZFVM_GRAVITY_CONSTANT_RADIAL ? sc.gravity_strength * r
-                                                                    : 0.5 * sc.gravity_strength * r * r;
+      const double phi = s->pot.phi(Vec3{x[3 * k], x[3 * k + 1], x[3 * k + 2]});
       EqEval::Bound b{at(PR::EQ), at(PR::EQ + 1), at(PR::EQ + 2)};
       double rho, E;
       b.at(ev, phi, rho, E);

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "gravity.hpp"
 #include "mesh_obj.hpp"
 #include "solver_kernels.cuh"
 
@@ -73,6 +74,7 @@ struct zfvm_solver {
   cudaStream_t stream = nullptr;
   cudaEvent_t ev_in = nullptr;    // recorded after a host upload
   cudaEvent_t ev_sync = nullptr;  // recorded by a batch before it uses the solver
+  zfvm::RadialPotential pot;  // the gravity potential (its table copied from the scheme)
   zfvm::dev::Params P{};
   zfvm::dev::DevData D{};
   // device buffers
