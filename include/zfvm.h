@@ -275,6 +275,34 @@ int zfvm_rate_of_change(zfvm_solver *s, double *tendency);
  *    current fails with ZFVM_EINVAL instead of handing over that device's array. */
 int zfvm_rate_of_change_noalloc(zfvm_solver *s, double *tendency);
 
+/* ---- fluxes and boundary conditions outside the solver's loop ----------------
+ * For callers that keep the reference's own loops (FluxLoop with a numerical
+ * flux template argument, RungeKutta with a BoundaryCondition object) around
+ * the GPU arithmetic.  Each call is one launch over n entries of host arrays,
+ * with device scratch allocated for the call: batch many face points per call. */
+
+/* HLLCBatten::flux (flux/hllc.hpp:142-176), or the Rusanov flux, of n pairs of
+ * face states in the face frame (rows of 5: rho, normal momentum, tangential
+ * momenta, E; ideal gas with gamma).  flux_out: n x 5.  speeds (may be null):
+ * n x 3, (s_L, s_star, s_R) of the HLLC fan, (-s_max, 0, s_max) for Rusanov. */
+int zfvm_numerical_flux(int32_t flux, double gamma, int64_t n, const double *uL, const double *uR,
+                        double *flux_out, double *speeds);
+
+/* HLLCBatten::tracer_flux (flux/hllc.hpp:178-197), or the Rusanov flux, of an
+ * advected variable mq for n face points, with the speeds zfvm_numerical_flux
+ * returned for the same states.  flux_out: n. */
+int zfvm_tracer_flux(int32_t flux, int64_t n, const double *uL, const double *uR, const double *mqL,
+                     const double *mqR, const double *speeds, double *flux_out);
+
+/* BoundaryCondition::apply (boundary/boundary_condition.hpp:12-21) with the
+ * solver's ghost cells on a host state (n_cells x 5, and n_cells x n_avars
+ * when the scheme has advected variables), in place: a frozen ghost cell takes
+ * its row of frozen_cvars / frozen_avars (FrozenBC::apply,
+ * boundary/frozen_boundary_condition.cpp:39-55; null keeps the row), a periodic
+ * image its source cell's row; interior rows are unchanged. */
+int zfvm_apply_boundary(zfvm_solver *s, const double *frozen_cvars, const double *frozen_avars, double *cvars,
+                        double *avars);
+
 /* EulerGlobalReconstruction::compute (reconstruction/global_reconstruction_impl.hpp:100-163):
  * reconstruct the current state in every interior and first-layer ghost cell;
  * the limited polynomials stay with the solver until the next call. */

@@ -8,6 +8,9 @@
 //   GpuLocalCFL             : zisa::CFLCondition      (model/cfl_condition.hpp:12-18)
 //   GpuGlobalReconstruction : zisa::GlobalReconstruction<euler_var_t>
 //                             (reconstruction/global_reconstruction_decl.hpp:20-32)
+//   GpuBoundaryCondition    : zisa::BoundaryCondition (boundary/boundary_condition.hpp:12-21)
+//   GpuHLLCBatten, GpuRusanov: HLLCBatten's static numerical-flux interface
+//                             (flux/hllc.hpp:142-202), a FluxLoop template argument
 // Outside it (ZFVM_STANDALONE) they implement the same member signatures on a
 // minimal AllVariables stand-in so the boundary compiles and tests on its own.
 //
@@ -22,11 +25,13 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "zfvm.h"
 
 #if __has_include(<zisa/ode/rate_of_change.hpp>) && !defined(ZFVM_STANDALONE)
+#include <zisa/boundary/boundary_condition.hpp>
 #include <zisa/model/all_variables.hpp>
 #include <zisa/model/cfl_condition.hpp>
 #include <zisa/ode/rate_of_change.hpp>
@@ -56,6 +61,7 @@ inline double *avars_data(AllVariables &u) { return u.avars.raw(); }
 inline const double *avars_data(const AllVariables &u) { return u.avars.raw(); }
 inline int64_t n_cells_of(const AllVariables &u) { return int64_t(u.cvars.shape(0)); }
 inline int32_t n_avars_of(const AllVariables &u) { return int32_t(u.avars.shape(1)); }
+using BoundaryConditionBase = zisa::BoundaryCondition;
 using VisualizationBase = zisa::Visualization;
 using DataSourceBase = zisa::DataSource;
 using SimulationClock = zisa::SimulationClock;
@@ -129,6 +135,17 @@ struct CFLConditionBase {
   virtual ~CFLConditionBase() = default;
   virtual double operator()(const AllVariables &all_variables) = 0;
 };
+struct BoundaryConditionBase {
+  virtual ~BoundaryConditionBase() = default;
+  virtual void apply(AllVariables &u, double t) = 0;
+  virtual std::string str() const = 0;
+};
+// IdealGasEOS and Euler as the numerical flux receives them (only gamma is read).
+struct IdealGasEOS {
+  double gamma_ = 1.4, specific_gas_constant_ = 1.0;
+  double gamma() const { return gamma_; }
+};
+struct Euler {};
 using XYZ = std::array<double, 3>;
 using euler_var_t = std::array<double, 5>;  // rho, m1, m2, m3, E
 struct CellsView {
@@ -278,6 +295,64 @@ class GpuGlobalReconstruction : public GlobalReconstructionBase {
   std::shared_ptr<DeviceSolver> s_;
   std::vector<int64_t> l2g_;
   std::vector<int64_t> n_l2g_;
+};
+
+// A numerical flux with HLLCBatten's static interface (flux/hllc.hpp:142-202),
+// evaluated by the same device code as the solver's face kernel: the flux of
+// two face states (normal momentum first) with the wave speeds of the fan, and
+// the flux of an advected variable for those speeds.  One call is one launch;
+// flux_batch evaluates many face points in one.
+template <int32_t FLUX>
+struct GpuNumericalFlux {
+  using speeds_t = std::tuple<double, double, double>;
+
+  template <class EulerT, class EOS>
+  static std::tuple<euler_var_t, speeds_t> flux(const EulerT &, const EOS &eosL, const euler_var_t &uL,
+                                                const EOS &eosR, const euler_var_t &uR) {
+    if (eosL.gamma() != eosR.gamma()) throw std::runtime_error("zfvm: the flux needs one ideal gas on both sides");
+    double a[5], b[5], f[5], sp[3];
+    for (int k = 0; k < 5; ++k) a[k] = uL[k], b[k] = uR[k];
+    check(zfvm_numerical_flux(FLUX, eosL.gamma(), 1, a, b, f, sp));
+    return {to_cvars(f), speeds_t{sp[0], sp[1], sp[2]}};
+  }
+  static double tracer_flux(const euler_var_t &uL, const euler_var_t &uR, double mqL, double mqR,
+                            const speeds_t &speeds) {
+    double a[5], b[5], f;
+    for (int k = 0; k < 5; ++k) a[k] = uL[k], b[k] = uR[k];
+    const double sp[3] = {std::get<0>(speeds), std::get<1>(speeds), std::get<2>(speeds)};
+    check(zfvm_tracer_flux(FLUX, 1, a, b, &mqL, &mqR, sp, &f));
+    return f;
+  }
+  // n face points (rows of 5) in one launch; speeds n x 3 (may be null)
+  static void flux_batch(double gamma, int64_t n, const double *uL, const double *uR, double *f, double *speeds) {
+    check(zfvm_numerical_flux(FLUX, gamma, n, uL, uR, f, speeds));
+  }
+  static std::string str() {
+    return FLUX == ZFVM_FLUX_HLLC ? "HLLC with Batten wavespeeds on the GPU (`GpuHLLCBatten`)"
+                                  : "Rusanov on the GPU (`GpuRusanov`)";
+  }
+};
+using GpuHLLCBatten = GpuNumericalFlux<ZFVM_FLUX_HLLC>;
+using GpuRusanov = GpuNumericalFlux<ZFVM_FLUX_RUSANOV>;
+
+// The solver's ghost-cell boundary condition as a BoundaryCondition object for
+// the reference's RungeKutta: frozen ghost cells are reset to the rows of the
+// state given at construction (FrozenBC, boundary/frozen_boundary_condition.cpp:11-55),
+// periodic images take their source cells' rows.
+class GpuBoundaryCondition : public BoundaryConditionBase {
+ public:
+  GpuBoundaryCondition(std::shared_ptr<DeviceSolver> s, const AllVariables &frozen)
+      : s_(std::move(s)), frozen_(frozen) {}
+  void apply(AllVariables &u, double /* t */) override {
+    const bool q = s_->n_avars() > 0;
+    check(zfvm_apply_boundary(s_->get(), cvars_data(frozen_), q ? avars_data(frozen_) : nullptr, cvars_data(u),
+                              q ? avars_data(u) : nullptr));
+  }
+  std::string str() const override { return "GB300 ghost-cell boundary conditions (`GpuBoundaryCondition`)"; }
+
+ private:
+  std::shared_ptr<DeviceSolver> s_;
+  AllVariables frozen_;
 };
 
 // DumpSnapshot (io/dump_snapshot_impl.hpp:21-38) writing .npz snapshot files

@@ -1,7 +1,8 @@
 // Drives the solver through the C++ adaptors of include/zfvm_zisa.hpp, the way
 // a ZisaFVM time loop would: LocalCFL, RateOfChange, RungeKutta::compute_step
-// and GlobalReconstruction, then DumpSnapshot / LoadSnapshot.  Prints the
-// results for tests/test_adaptors.py.
+// and GlobalReconstruction, then DumpSnapshot / LoadSnapshot, the numerical
+// flux interface and the BoundaryCondition object.  Prints the results for
+// tests/test_adaptors.py.
 #define ZFVM_STANDALONE 1
 #include <cstdio>
 #include <cstdlib>
@@ -124,6 +125,27 @@ int main(int argc, char **argv) {
   load(back, clock2);
   std::printf("snapshot %d %.17g %lld\n", int(back.cvars == u1->cvars && back.avars == u1->avars), clock2.current_time(),
               (long long)clock2.current_step());
+
+  // the numerical flux as a FluxLoop template argument would call it
+  const zfvm::euler_var_t fl = {1.0, 0.3, -0.2, 0.1, 2.5}, fr = {0.8, 0.1, 0.05, -0.1, 1.9};
+  const zfvm::IdealGasEOS eos{1.4, 1.0};
+  const auto [nf, speeds] = zfvm::GpuHLLCBatten::flux(zfvm::Euler{}, eos, fl, eos, fr);
+  std::printf("hllc");
+  for (int k = 0; k < 5; ++k) std::printf(" %.17g", nf[k]);
+  std::printf(" %.17g %.17g %.17g\n", std::get<0>(speeds), std::get<1>(speeds), std::get<2>(speeds));
+  std::printf("tracer %.17g\n", zfvm::GpuHLLCBatten::tracer_flux(fl, fr, 0.4, 0.6, speeds));
+  const auto [rf, rs] = zfvm::GpuRusanov::flux(zfvm::Euler{}, eos, fl, eos, fr);
+  std::printf("rusanov");
+  for (int k = 0; k < 5; ++k) std::printf(" %.17g", rf[k]);
+  std::printf(" %.17g\n", std::get<2>(rs));
+
+  // the boundary condition object the reference's RungeKutta applies after
+  // every stage; this mesh has no ghost cells, so the state is unchanged
+  zfvm::GpuBoundaryCondition bc(ds, *u0);
+  zfvm::AllVariables w = *u1;
+  bc.apply(w, dt);
+  std::printf("bc %d\n", int(w.cvars == u1->cvars && w.avars == u1->avars));
+
   ds.reset();
   zfvm_mesh_destroy(mesh);
   return 0;

@@ -1,7 +1,7 @@
 """The C++ drop-in adaptors (include/zfvm_zisa.hpp: GpuLocalCFL, GpuRateOfChange,
-GpuRungeKutta, GpuGlobalReconstruction, NpzDumpSnapshot, NpzLoadSnapshot)
-compile against the C ABI, and on a GPU give the same numbers as the
-library's other bindings."""
+GpuRungeKutta, GpuGlobalReconstruction, GpuBoundaryCondition, GpuHLLCBatten,
+GpuRusanov, NpzDumpSnapshot, NpzLoadSnapshot) compile against the C ABI, and
+on a GPU give the same numbers as the library's other bindings and the oracle."""
 import subprocess
 from pathlib import Path
 
@@ -66,3 +66,14 @@ def test_adaptors_match_python_binding(tmp_path, zlib):
     assert np.allclose([float(a) for a in out["recon"]], ux, rtol=1e-15, atol=0)
     st = mesh.stencils()
     assert out["cell"][1] == "stencil" and int(out["cell"][2]) == int(st["n_l2g"][cell])
+    # HLLCBatten's static interface and the Rusanov flux against the oracle's
+    from oracle import pyoracle
+    fl, fr = [1.0, 0.3, -0.2, 0.1, 2.5], [0.8, 0.1, 0.05, -0.1, 1.9]
+    hllc = np.array([float(a) for a in out["hllc"]])
+    assert np.allclose(hllc[:5], pyoracle.flux(0, 1.4, fl, fr), rtol=1e-14, atol=1e-15)
+    f, sp = z.numerical_flux(z.FLUX_HLLC, 1.4, fl, fr)
+    assert np.array_equal(hllc[:5], f[0]) and np.array_equal(hllc[5:], sp[0])
+    assert float(out["tracer"][0]) == pytest.approx(pyoracle.tracer_flux(0, 1.4, fl, fr, 0.4, 0.6), rel=1e-14)
+    rus = np.array([float(a) for a in out["rusanov"]])
+    assert np.allclose(rus[:5], pyoracle.flux(1, 1.4, fl, fr), rtol=1e-14, atol=1e-15)
+    assert out["bc"][0] == "1"

@@ -164,6 +164,9 @@ def load_library() -> C.CDLL:
         "zfvm_snapshot_read": [C.c_char_p, i64, dp, i32, dp, dp, C.POINTER(i64)],
         "zfvm_solver_write_snapshot": [vp, C.c_char_p, i64],
         "zfvm_solver_read_snapshot": [vp, C.c_char_p, C.POINTER(i64)],
+        "zfvm_numerical_flux": [i32, C.c_double, i64, dp, dp, dp, dp],
+        "zfvm_tracer_flux": [i32, i64, dp, dp, dp, dp, dp, dp],
+        "zfvm_apply_boundary": [vp, dp, dp, dp, dp],
     }
     for name, args in sig.items():
         fn = getattr(lib, name)
@@ -187,6 +190,30 @@ def _dp(a: np.ndarray):
 
 def _i64p(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def numerical_flux(kind: int, gamma: float, uL, uR):
+    """HLLCBatten::flux (or Rusanov) of face states on the GPU: rows of
+    (rho, normal momentum, tangential momenta, E) -> (fluxes n x 5, speeds n x 3)."""
+    a = np.ascontiguousarray(np.atleast_2d(uL), dtype=np.float64)
+    b = np.ascontiguousarray(np.atleast_2d(uR), dtype=np.float64)
+    if a.shape != b.shape or a.shape[1] != 5:
+        raise ValueError("uL, uR: n x 5 face states")
+    f, sp = np.zeros_like(a), np.zeros((a.shape[0], 3))
+    _check(load_library().zfvm_numerical_flux(kind, gamma, a.shape[0], _dp(a), _dp(b), _dp(f), _dp(sp)))
+    return f, sp
+
+
+def tracer_flux(kind: int, uL, uR, mqL, mqR, speeds):
+    """HLLCBatten::tracer_flux (or Rusanov) on the GPU for n face points."""
+    a = np.ascontiguousarray(np.atleast_2d(uL), dtype=np.float64)
+    b = np.ascontiguousarray(np.atleast_2d(uR), dtype=np.float64)
+    qa = np.ascontiguousarray(np.atleast_1d(mqL), dtype=np.float64)
+    qb = np.ascontiguousarray(np.atleast_1d(mqR), dtype=np.float64)
+    sp = np.ascontiguousarray(np.atleast_2d(speeds), dtype=np.float64)
+    f = np.zeros(a.shape[0])
+    _check(load_library().zfvm_tracer_flux(kind, a.shape[0], _dp(a), _dp(b), _dp(qa), _dp(qb), _dp(sp), _dp(f)))
+    return f
 
 
 @dataclass
@@ -498,6 +525,20 @@ class Solver:
         n = C.c_int64()
         _check(load_library().zfvm_solver_read_snapshot(self._h, os.fsencode(path), C.byref(n)))
         return n.value
+
+    def apply_boundary(self, cvars: np.ndarray, frozen: np.ndarray | None = None, avars=None,
+                       frozen_avars=None):
+        """BoundaryCondition::apply with this solver's ghost cells on host
+        states: frozen ghosts from `frozen` (unchanged without), periodic
+        images from their sources.  Returns new arrays."""
+        u = np.array(cvars, dtype=np.float64, order="C", copy=True)
+        fz = None if frozen is None else np.ascontiguousarray(frozen, dtype=np.float64)
+        q = None if avars is None else np.array(avars, dtype=np.float64, order="C", copy=True)
+        fq = None if frozen_avars is None else np.ascontiguousarray(frozen_avars, dtype=np.float64)
+        _check(load_library().zfvm_apply_boundary(self._h, None if fz is None else _dp(fz),
+                                                  None if fq is None else _dp(fq), _dp(u),
+                                                  None if q is None else _dp(q)))
+        return u if q is None else (u, q)
 
     def rate_of_change(self) -> np.ndarray:
         a = np.zeros((self.mesh.n_cells, 5))

@@ -28,7 +28,7 @@ NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "--compress-mode=size", "-
              "--expt-relaxed-constexpr"]
 
 HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp", "snapshot.cpp"]
-CUDA_SOURCES = ["solver.cu", "batch.cu", "server.cu", "noalloc.cu"]
+CUDA_SOURCES = ["solver.cu", "batch.cu", "server.cu", "noalloc.cu", "flux_api.cu"]
 # inst_shape.cu compiled once per stencil shape x precision x (single solver,
 # batch): (object name, -D flags)
 SHAPES = {"s2o3": "S2o3", "s2o2": "S2o2", "s3o3": "S3o3", "s3o2": "S3o2"}
