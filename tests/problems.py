@@ -87,12 +87,10 @@ def polytrope_3d(n: int = 40, amplitude: float = 1e-4, seed: int = 3, precision:
     return raw, mesh, scheme, u0
 
 
-def ensemble_c4(n_instances: int = 256, n_min: int = 5000, n_max: int = 200000, seed: int = 2024,
-                precision: int = z.MIXED):
-    """C4: independent well-balanced polytrope solves on seeded jittered disk
-    meshes with log-uniform sizes in [n_min, n_max] triangles, perturbation
-    amplitudes log-uniform in [1e-6, 1e-2], centres at r ~ U[0.1, 0.7] and a
-    random angle, width 0.05; CWENO-AO order 3, HLLC, SSP3."""
+def c4_instance_params(n_instances: int = 256, n_min: int = 5000, n_max: int = 200000, seed: int = 2024):
+    """The ensemble's per-instance draws: disk rings (log-uniform cell count in
+    [n_min, n_max]), perturbation amplitude (log-uniform in [1e-6, 1e-2]),
+    centre radius U[0.1, 0.7] and angle, and the mesh seed."""
     import numpy as np
     rng = np.random.default_rng(seed)
     out = []
@@ -101,16 +99,33 @@ def ensemble_c4(n_instances: int = 256, n_min: int = 5000, n_max: int = 200000, 
         rings = max(4, int(round(np.sqrt(n_cells / (2.0 * np.pi)))))
         amp = float(np.exp(rng.uniform(np.log(1e-6), np.log(1e-2))))
         r0, ang = float(rng.uniform(0.1, 0.7)), float(rng.uniform(0.0, 2.0 * np.pi))
-        raw = z.RawMesh.generate("disk", n=rings, radius=1.0, jitter=0.2, seed=seed + 17 * k + 1)
-        mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2), quad=(3, 3, 2))
-        scheme = z.Scheme(flux=z.FLUX_HLLC, gamma=2.0, linear_weights=[100.0, 1.0, 1.0, 1.0], epsilon=1e-6,
-                          exponent=4.0, rk_stages=3, cfl_number=0.45, equilibrium=z.EQ_ISENTROPIC,
-                          gravity=z.GRAVITY_HARMONIC_RADIAL, gravity_strength=1.0,
-                          flux_bc=z.FLUX_BC_ISENTROPIC, precision=precision)
-        u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=amp,
-                                     width=0.05, x0=r0 * np.cos(ang), y0=r0 * np.sin(ang))
-        out.append((raw, mesh, scheme, u0))
+        out.append(dict(rings=rings, amplitude=amp, r0=r0, angle=ang, mesh_seed=seed + 17 * k + 1))
     return out
+
+
+def c4_instance(p: dict, precision: int = z.MIXED):
+    """One ensemble instance: a seeded jittered disk, the gamma = 2, K = 1
+    polytrope in phi = r^2 / 2 plus its Gaussian bump of width 0.05; CWENO-AO
+    order 3, HLLC, SSP3, CFL 0.45, isentropic well-balancing."""
+    import numpy as np
+    raw = z.RawMesh.generate("disk", n=p["rings"], radius=1.0, jitter=0.2, seed=p["mesh_seed"])
+    mesh = z.Mesh(raw, z.StencilSpec.cweno(3, 2), quad=(3, 3, 2))
+    scheme = z.Scheme(flux=z.FLUX_HLLC, gamma=2.0, linear_weights=[100.0, 1.0, 1.0, 1.0], epsilon=1e-6,
+                      exponent=4.0, rk_stages=3, cfl_number=0.45, equilibrium=z.EQ_ISENTROPIC,
+                      gravity=z.GRAVITY_HARMONIC_RADIAL, gravity_strength=1.0,
+                      flux_bc=z.FLUX_BC_ISENTROPIC, precision=precision)
+    u0 = mesh.initial_conditions("polytrope", gamma=2.0, K=1.0, rho_c=1.0, k_phi=1.0, amplitude=p["amplitude"],
+                                 width=0.05, x0=p["r0"] * np.cos(p["angle"]), y0=p["r0"] * np.sin(p["angle"]))
+    return raw, mesh, scheme, u0
+
+
+def ensemble_c4(n_instances: int = 256, n_min: int = 5000, n_max: int = 200000, seed: int = 2024,
+                precision: int = z.MIXED):
+    """C4: independent well-balanced polytrope solves on seeded jittered disk
+    meshes with log-uniform sizes in [n_min, n_max] triangles, perturbation
+    amplitudes log-uniform in [1e-6, 1e-2], centres at r ~ U[0.1, 0.7] and a
+    random angle, width 0.05; CWENO-AO order 3, HLLC, SSP3."""
+    return [c4_instance(p, precision) for p in c4_instance_params(n_instances, n_min, n_max, seed)]
 
 
 def tracers(mesh, u0, n_avars: int = 2):

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 
 TOL_RUN = 1e-12
 # ten times the deviation error measured on GB300
-DEV_TOL_C2 = 4e-10
+DEV_TOL_C2 = 5e-10  # measured 3.6e-11 - 4.8e-11 (the oracle against itself: the same order)
 
 
 def _run_pair(z, olib, raw, mesh, scheme, u0, n_steps):
@@ -57,6 +57,11 @@ def test_c3_full_50_steps(zlib, olib, order):
     raw, mesh, scheme, u0 = vortex_tube_3d(n=70, order=order)
     assert mesh.n_cells == 2058000
     u_gpu, u_ref = _run_pair(z, olib, raw, mesh, scheme, u0, 50)
-    l1, linf = rel_errors(u_gpu, u_ref, cols=(0, 1, 2, 3, 4))
+    l1, linf = conserved_rel_errors(u_gpu, u_ref)
+    print(f"C3 order {order} 50 steps: conserved rel L1 {l1:.3e} Linf {linf:.3e}")
+    assert l1 < TOL_RUN and linf < TOL_RUN
+    # per variable, but for the third momentum: the tube's flow is planar and
+    # its z-momentum stays at round-off size
+    l1, linf = rel_errors(u_gpu, u_ref, cols=(0, 1, 2, 4))
     print(f"C3 order {order} 50 steps: per-variable rel L1 {l1:.3e} Linf {linf:.3e}")
     assert l1 < TOL_RUN and linf < TOL_RUN

@@ -5,9 +5,10 @@ Bars: FP64 tendencies within 1e-13 of each variable's largest tendency, FP64
 runs within 1e-12 relative L1 and Linf per variable (the conserved-variable
 bars).  On the well-balanced polytrope near rest the contact speed s* that
 upwinds the tracers is a small difference of O(1) terms and the tendency a
-small divergence, so its bars are the ones the conserved variables use there
-(test_gpu_parity.py::test_polytrope_*): 1e-9 of the largest tendency, and of
-the largest change over the run.  The mixed form's tracers within 1e-6 relative L1 of the FP64 oracle
+small divergence, so its tendency and change over the run are bounded against
+their own size at ten times the errors measured on GB300 (tendency 1.4e-12,
+change 6.4e-13), as the conserved variables are there
+(test_gpu_parity.py::test_polytrope_*).  The mixed form's tracers within 1e-6 relative L1 of the FP64 oracle
 (the mixed form's bar), since their wave speeds come from the mixed form's
 face states.  Tracers are passive: the conserved variables must not change
 when tracers are added (bit for bit in FP64).
@@ -26,7 +27,8 @@ pytestmark = pytest.mark.gpu
 TOL_RHS = 1e-13
 TOL_RUN = 1e-12
 TOL_MIXED = 1e-6
-TOL_WB = 1e-9
+TOL_WB = 1.4e-11      # tendency; measured 1.4e-12
+TOL_WB_RUN = 6.4e-12  # change over the run; measured 6.4e-13
 NA = 2
 WB_CASES = ("polytrope", "frozen")
 
@@ -107,7 +109,7 @@ def test_tracer_steps(zlib, olib, case):
             d, dref = (a - a0)[inner], (ref - a0)[inner]
             err = np.abs(d - dref).max() / np.abs(dref).max()
             print(f"tracer run {case}: change error {err:.2e}")
-            assert err < TOL_WB, err
+            assert err < TOL_WB_RUN, err
         return
     cols = (0, 1, 2, 4) if raw.n_dims == 2 else (0, 1, 2, 3, 4)
     l1, linf = rel_errors(u_gpu, u_ref, inner, cols)
@@ -174,7 +176,9 @@ def test_tracers_with_step_rejection(zlib, olib):
     _, q_ref, t_ref, n_ref = _oracle(olib, raw, mesh, scheme).run(u0, n_steps=12, avars=q0)
     assert n_ref == 12 and abs(t_gpu - t_ref) <= 1e-12 * t_ref
     d_gpu, d_ref = q_gpu - q0, q_ref - q0
-    assert np.abs(d_gpu - d_ref).max() <= 1e-9 * np.abs(d_ref).max()
+    err = np.abs(d_gpu - d_ref).max() / np.abs(d_ref).max()
+    print(f"tracers with step rejection: change error {err:.2e}")
+    assert err <= TOL_WB_RUN
 
 
 def test_tracer_snapshot_restart(zlib, tmp_path):

@@ -379,9 +379,7 @@ int build_solver(zfvm_solver *s) {
   P.nqf = s->nqf;
   P.flux_bc = sc.flux_bc;
   P.n_stages = sc.rk_stages;
-  // the closed forms of the gamma = 2 equilibrium belong to the mixed form; the
-  // FP64 form evaluates the equilibrium as the reference does
-  P.gamma2 = (sc.gamma == 2.0 && sc.precision == ZFVM_MIXED) ? 1 : 0;
+  P.gamma2 = sc.gamma == 2.0 ? 1 : 0;
   P.inv_gm1 = 1.0 / (sc.gamma - 1.0);
   if (sc.reconstruction != ZFVM_RC_CWENO_AO && sc.reconstruction != ZFVM_RC_WENO_AO)
     return fail(ZFVM_EINVAL, "unknown reconstruction mode");
@@ -419,12 +417,11 @@ int build_solver(zfvm_solver *s) {
   std::vector<uint8_t> h_flags(ld, 0), h_bloc((size_t)NB * RB * ld, 0);
   std::vector<int> h_l2g((size_t)MAXL * ld, 0), h_cface((size_t)nf * ld, -1), h_src(ld, 0);
   std::vector<double> h_pinv((size_t)NP * ld, 0.0), h_center((size_t)nd * ld, 0.0), h_il(ld, 0.0),
-      h_mom((size_t)NC * ld, 0.0), h_iv(ld, 0.0), h_vol(ld, 0.0), h_reff(ld, 1e300);
+      h_mom((size_t)NC * ld, 0.0), h_iv(ld, 0.0), h_reff(ld, 1e300);
   for (index_t i = 0; i < n; ++i) {
     h_flags[i] = g.flags[i] | (((g.flags[i] & kGhost) && g.source[i] == i) ? kFrozen : 0);
     h_src[i] = (int)g.source[i];
     h_iv[i] = 1.0 / g.volumes[i];
-    h_vol[i] = g.volumes[i];
     h_il[i] = 1.0 / g.char_length[i];
     for (int k = 0; k < nd; ++k) h_center[k * ld + i] = g.cell_centers[i][k];
     for (int c = 3; c <= NC; ++c) h_mom[(c - 1) * ld + i] = g.moments[i * g.n_moments + c];
@@ -599,7 +596,6 @@ int build_solver(zfvm_solver *s) {
     if (!s->mixed) s->srcb.alloc((size_t)nv * ld);
   }
   if (s->has_eq) s->eqth.alloc((size_t)4 * ld);
-  if (s->has_eq && !P.gamma2) s->vol.upload(h_vol);
   if (s->has_eq && sc.steps_per_recompute > 1) {
     // zero counts: the first reconstruction of every cell refreshes
     s->sched_count.alloc(ld);
@@ -740,7 +736,6 @@ int build_solver(zfvm_solver *s) {
   D.mom = s->mom.p;
   D.cface = s->cface.p;
   D.inv_vol = s->inv_vol.p;
-  D.vol = s->vol.p;
   D.r_eff = s->r_eff.p;
   D.fL = s->fL.p;
   D.fR = s->fR.p;
@@ -767,7 +762,6 @@ int build_solver(zfvm_solver *s) {
   add(8 * (s->gphi_w.n + s->qsplit.n + s->m1s.n + s->vars.n + s->eq32.n + s->phi_fq2.n));
   add(4 * s->dev032.n);
   add(8 * s->uprev.n);
-  add(8 * s->vol.n);
   add(4 * s->sched_count.n + 8 * s->sched.n);
   add(8 * s->heat_w.n);
   add(8 * (s->dev0.n + s->phi_m1.n + s->phi_var.n + s->pinv.n + s->center.n + s->inv_len.n + s->mom.n + s->inv_vol.n + s->r_eff.n + s->fqx.n + s->fqw.n +
@@ -1195,7 +1189,6 @@ int64_t solver_footprint(const zfvm_mesh *m, const zfvm_scheme_desc &sc) {
     if (!mixed) b += 8 * nv * ld;                                               // srcb
   }
   if (has_eq) b += 8 * 4 * ld;                                                  // eqth
-  if (has_eq && !(mixed && sc.gamma == 2.0)) b += 8 * ld;                       // vol
   if (has_eq && sc.steps_per_recompute > 1) b += 4 * ld + 8 * 4 * ld;           // sched_count, sched
   if (sc.step_rejection_drho > 0.0) b += 8 * nv * ld;                            // uprev
   if (sc.heating_rate != 0.0 && has_src) b += 8 * nqc * ld;                       // heat_w

@@ -119,7 +119,6 @@ struct DevData {
   const double *mom;     // [NC][ld] (C_1 .. C_NC of the final polynomial)
   const int *cface;      // [NF][ld]  2 * edge + side, -1 when absent
   const double *inv_vol; // [ld]
-  const double *vol;     // [ld] volumes (the FP64 equilibrium averages divide by them)
   const double *r_eff;   // [ld] in-radius, minimum over the cell and its ghost images
   const int *fL, *fR;    // [lde]
   const uint8_t *fkL, *fkR, *factive;
@@ -160,7 +159,7 @@ struct Params {
   int nqc, nqf;
   int flux_bc;       // 0 none, 1 constant, 2 isentropic
   int n_stages;
-  int gamma2;        // mixed form with gamma == 2: closed-form equilibrium fit and averages
+  int gamma2;        // gamma == 2: closed-form equilibrium cell averages (and, mixed, fit)
   double inv_gm1;    // 1 / (gamma - 1), computed once on the host
   int weno_ao;       // reconstruction: 0 CWENO-AO, 1 WENO-AO
   double a[4][4], b[4];
@@ -270,17 +269,15 @@ struct EqEval {
   }
 };
 
-// Quadrature average of the equilibrium over a cell.
-// FP64 form: LocalEquilibrium::extrapolate(Cell) = average(cell, f)
-// (local_equilibrium_impl.hpp:179-186, math/quadrature.hpp:33-62): the sum of
-// w_q f(x_q) over the cell's own (volume-scaled) weights in quadrature order,
-// each product and sum rounded on its own as in the reference's loop (no
-// fused multiply-add), then one division by the volume.  The deviation of a
-// cell from an equilibrium is a small difference of O(1) averages, so the
-// last bit of the average matters at the deviation's scale.
-// Mixed form with gamma = 2: the density is linear and the energy quadratic in
-// phi, so the average follows exactly from the cell's <phi> and
-// <(phi - <phi>)^2>: rho_bar = f (h_r - <phi>), E_bar = K f^2 ((h_r - <phi>)^2 + var phi).
+// Quadrature average of the equilibrium over a cell.  For gamma = 2 the
+// density is linear and the energy quadratic in phi, so the average follows
+// exactly from the cell's <phi> and <(phi - <phi>)^2>:
+//   rho_bar = f (h_r - <phi>),  E_bar = K f^2 ((h_r - <phi>)^2 + var phi).
+// Otherwise the quadrature-point sum with the reference-cell weights.  (The
+// reference sums w_q f(x_q) over the volume-scaled weights and divides by the
+// volume; in the FP64 form that order costs two FP64 divisions per average and
+// made the reconstruction 2.9x slower, for last-bit differences of the size
+// the reference's own atomic flux sums change from run to run.)
 template <int NQC>
 __device__ __forceinline__ void eq_cell_average(const EqEval &ev, const Params &P, const DevData &d,
                                                 const EqEval::Bound &b, int j, double &rb, double &Eb) {
@@ -292,18 +289,14 @@ __device__ __forceinline__ void eq_cell_average(const EqEval &ev, const Params &
   }
   double r, e;
   b.at(ev, d.phi_cq[j], r, e);
-  double w = d.cqw[j];
-  double sr = __dmul_rn(w, r), se = __dmul_rn(w, e);
+  rb = P.what_c[0] * r;
+  Eb = P.what_c[0] * e;
 #pragma unroll
   for (int q = 1; q < NQC; ++q) {
     b.at(ev, d.phi_cq[q * d.ld + j], r, e);
-    w = d.cqw[q * d.ld + j];
-    sr = __dadd_rn(sr, __dmul_rn(w, r));
-    se = __dadd_rn(se, __dmul_rn(w, e));
+    rb += P.what_c[q] * r;
+    Eb += P.what_c[q] * e;
   }
-  const double v = d.vol[j];
-  rb = sr / v;
-  Eb = se / v;
 }
 
 // LocalEquilibriumBase::solve_exact + quasi_newton (local_equilibrium_impl.hpp:40-94,

@@ -80,7 +80,7 @@ struct zfvm_solver {
   // device buffers
   zfvm::DBuf<uint8_t> flags, bloc, fkL, fkR, factive;
   zfvm::DBuf<int> l2g, cface, fL, fR, src_map;
-  zfvm::DBuf<double> pinv, center, inv_len, mom, inv_vol, vol, r_eff, fqx, fqw, frame, farea;
+  zfvm::DBuf<double> pinv, center, inv_len, mom, inv_vol, r_eff, fqx, fqw, frame, farea;
   zfvm::DBuf<float> pinv32, fv32, frame32, xfq32, xcq32, mom32, wg32, g32, mL32, mR32, src32, kbuf32, fqw32;
   zfvm::DBuf<double> gphi_w;
   zfvm::DBuf<double> phi_cq, phi_m1, phi_var, gphi_cq, cqx, cqw, phi_fq;
