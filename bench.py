@@ -1,28 +1,39 @@
 """Benchmark: cell-stage updates/s of the rate-of-change + SSP-RK step loop.
 
-Default workload (C2): the well-balanced 2D polytrope (gamma = 2, K = 1,
-phi = r^2 / 2 on the unit disk, ~200k jittered Delaunay triangles, CWENO-AO
-order 3, HLLC, SSP3, CFL 0.45, perturbation 1e-4), seeded synthetic data.  One
-"step" is one SSP3 time step over the whole mesh: 3 cell-stage updates per cell.
+One cell-stage update is one cell through one RK stage (reconstruction, its
+share of the face fluxes, the source and the stage combination); SSP3 makes
+three per cell per step.
+
+Default workload (C4, the metric's mixed-batched form): 256 independent
+well-balanced polytrope solves (gamma = 2, K = 1, phi = r^2 / 2 on seeded
+jittered disks of 5k-200k triangles, perturbation amplitudes 1e-6-1e-2,
+CWENO-AO order 3, HLLC, SSP3, CFL 0.45), mixed FP32/FP64, batched into one
+persistent launch per phase per RK stage with autotuned launch shapes, next to
+the plain FP64 form run one solve at a time on the same instances.  The same
+JSON line carries the other workloads as sub-blocks, measured the same way:
+  c2   the well-balanced polytrope disk of 199,076 cells, mixed and FP64, its
+       run to t = 0.5 and its well-balanced residual
+  c3   the 2,058,000-tetrahedron vortex tube, order 3, mixed and FP64
+  c5   the serving loop: Poisson arrivals of 2D / 3D solves, p50 / p99
+       latency and throughput, mixed and FP64
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                  [--workload c2|c1|c3|c3o2|c4|...] [--precision mixed|fp64]
+                  [--workload c4|c2|c1|c3|c3o2|c5|...] [--precision mixed|fp64]
+                  [--no-blocks] [--profile]
 
-value    whole-job cell-stage updates/s of the --precision form (default: the
-         mixed FP32/FP64 form), state resident in HBM, CUDA events on the
-         solver stream around K graph-replayed steps (max over ranks).  With
-         the mixed form the plain FP64 form is timed the same way on the same
-         mesh ("fp64"), and the mixed form's error against it and its
-         well-balanced residual are reported.
-c4       256 solves of uneven size batched into one persistent launch per
-         phase per RK stage (autotuned grids), against the FP64 form run one
-         solve at a time on the same instances.
+value    whole-job cell-stage updates/s of the headline workload, state
+         resident in HBM, CUDA events around K graph-replayed steps (max over
+         ranks); inputs larger than L2.
 e2e      the same metric through the public API with host buffers: every step
-         copies the state from pinned host memory to the device, advances one
-         CFL step and reads the new state back.
-roofline dominant kernel (the reconstruction kernel): algorithmic bytes per
-         launch / its event-timed launch duration, against the measured HBM
-         copy bandwidth; the FP64 pipe bounds these kernels first.
+         copies the states from pinned host memory to the device, advances one
+         CFL step and reads the new states back.
+roofline the dominant kernel (the reconstruction): algorithmic bytes per launch
+         / its event-timed launch duration, against the measured HBM copy
+         bandwidth; the FP64 form also against its FP64 pipe.
+reference (--impl reference) the reference's CPU path (its FP64 restatement,
+         the oracle; the reference itself cannot be built) on a sample of the
+         same instances, all host cores, from meshes and stencils that build()
+         wrote, so the process loads no part of the GPU library.
 Multi-GPU: replicas only -- every rank solves its own copy (no data exchange).
 """
 from __future__ import annotations
@@ -42,24 +53,36 @@ for p in (ROOT, ROOT / "tests"):
     if str(p) not in sys.path:
         sys.path.insert(0, str(p))
 
-FP64_PEAK_TFLOPS = 1.254  # FMA-chain probe on this machine's GB300 (2 flop / DFMA)
+METRIC = "cell-stage updates/s, FP64 vs mixed-batched at ≤1e-6 L1 error; p50/p99 latency"
+UNIT = "cell-stage updates/s"
+# meshes, stencils and initial states of the reference arm's samples, written
+# by build() (write_reference_inputs) and read by --impl reference
+REF_INPUTS = ROOT / "oracle" / "_build" / "reference_inputs"
+C4_SEED = 2024
+# C4 instances the CPU arms time: the ensemble's size quantiles 5, 25, 50, 75 and 95 %
+C4_SAMPLE_QUANTILES = (0.05, 0.25, 0.5, 0.75, 0.95)
+# FP64 pipe of GB300: 2 DFMA thread-instructions per cycle per SM (ncu's
+# sm__sass_thread_inst_executed_op_dfma_pred_on.avg.peak_sustained), 2 flop each
+DFMA_PER_CLK_PER_SM = 2.0
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=160)
-    ap.add_argument("--warmup", type=int, default=16)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2",
-                    choices=["c2", "c1", "c3", "c3o2", "c4", "c5", "c2-small", "c1-small", "c3-small", "c4-small",
+    ap.add_argument("--workload", default="c4",
+                    choices=["c4", "c2", "c1", "c3", "c3o2", "c5", "c2-small", "c1-small", "c3-small", "c4-small",
                              "c5-small"])
     ap.add_argument("--load", type=float, default=0.7, help="c5: offered load as a fraction of throughput")
     ap.add_argument("--budget-gb", type=float, default=24.0, help="c5: device memory budget of the server")
     ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"],
-                    help="form whose throughput is `value`; with mixed the FP64 form is timed beside it")
+                    help="single-mesh workloads: the form whose throughput is `value` (mixed times FP64 beside it)")
+    ap.add_argument("--no-blocks", action="store_true", help="c4: skip the c2 / c3 / c5 sub-blocks")
     ap.add_argument("--profile", action="store_true",
                     help="timed loop only (no CPU baseline, no e2e loop): the command profiled with ncu")
+    ap.add_argument("--write-reference-inputs", action="store_true", help=argparse.SUPPRESS)
     return ap.parse_args()
 
 
@@ -70,39 +93,61 @@ def dist_env():
     return rank, world, local
 
 
+# ------------------------------------------------------------------ configs
+def c4_config(world: int, n_inst: int = 256) -> dict:
+    """The C4 workload as both arms name it."""
+    return {"workload": f"C4 batched ensemble of {n_inst} well-balanced polytrope disks", "instances": n_inst,
+            "cells_per_instance": "log-uniform 5k-200k", "amplitudes": "log-uniform 1e-6-1e-2", "seed": C4_SEED,
+            "precision": "mixed (FP64 beside it)", "batched": True,
+            "scheme": "CWENO-AO o3, HLLC, SSP3, CFL 0.45, isentropic well-balancing",
+            "parallelism": f"replicas x{world}", "l2": "inputs larger than L2"}
+
+
+SINGLE_DESC = {
+    "c2": {"workload": "C2 well-balanced polytrope disk", "cells": 199076, "gamma": 2.0,
+           "scheme": "CWENO-AO o3, HLLC, SSP3, CFL 0.45, isentropic well-balancing"},
+    "c2-small": {"workload": "C2 well-balanced polytrope disk (small)"},
+    "c1": {"workload": "C1 periodic isentropic vortex", "cells": 51200,
+           "scheme": "CWENO-AO o3, Rusanov, SSP3, CFL 0.45"},
+    "c1-small": {"workload": "C1 periodic isentropic vortex (small)"},
+    "c3": {"workload": "C3 tetrahedral vortex tube", "cells": 2058000, "scheme": "CWENO-AO o3, HLLC, SSP3, CFL 0.3"},
+    "c3o2": {"workload": "C3 tetrahedral vortex tube, order 2", "cells": 2058000,
+             "scheme": "CWENO-AO o2, HLLC, SSP3, CFL 0.3"},
+    "c3-small": {"workload": "C3 tetrahedral vortex tube (small)"},
+}
+
+
+def single_config(name: str, precision: str, world: int) -> dict:
+    return {**SINGLE_DESC[name], "precision": precision, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 for c2 / c3 (state, operators and face data > 129 MB)"}
+
+
 def workload(name: str, precision: str):
     import zisafvm_gb300 as z
     from problems import polytrope_2d, vortex_2d, vortex_tube_3d
     prec = z.MIXED if precision == "mixed" else z.FP64
     if name == "c2":
         raw, mesh, scheme, u0 = polytrope_2d(n_rings=178, amplitude=1e-4)
-        desc = {"workload": "C2 well-balanced polytrope disk", "cells": mesh.n_cells, "gamma": 2.0,
-                "scheme": "CWENO-AO o3, HLLC, SSP3, CFL 0.45, isentropic well-balancing"}
     elif name == "c2-small":
         raw, mesh, scheme, u0 = polytrope_2d(n_rings=60, amplitude=1e-4)
-        desc = {"workload": "C2 well-balanced polytrope disk (small)", "cells": mesh.n_cells}
     elif name == "c1":
         raw, mesh, scheme, u0 = vortex_2d(n=160, halo=3)
-        desc = {"workload": "C1 periodic isentropic vortex", "cells": mesh.info["n_interior_cells"],
-                "scheme": "CWENO-AO o3, Rusanov, SSP3, CFL 0.45"}
     elif name == "c1-small":
         raw, mesh, scheme, u0 = vortex_2d(n=48, halo=3)
-        desc = {"workload": "C1 periodic isentropic vortex (small)", "cells": mesh.info["n_interior_cells"]}
     elif name == "c3o2":
         raw, mesh, scheme, u0 = vortex_tube_3d(n=70, order=2)
-        desc = {"workload": "C3 tetrahedral vortex tube, order 2", "cells": mesh.n_cells,
-                "scheme": "CWENO-AO o2, HLLC, SSP3, CFL 0.3"}
     elif name == "c3-small":
         raw, mesh, scheme, u0 = vortex_tube_3d(n=24, order=3)
-        desc = {"workload": "C3 tetrahedral vortex tube (small)", "cells": mesh.n_cells}
     else:
         raw, mesh, scheme, u0 = vortex_tube_3d(n=70, order=3)
-        desc = {"workload": "C3 tetrahedral vortex tube", "cells": mesh.n_cells,
-                "scheme": "CWENO-AO o3, HLLC, SSP3, CFL 0.3"}
     scheme.precision = prec
-    return raw, mesh, scheme, u0, desc
+    cells = mesh.info["n_interior_cells"] if name.startswith("c1") else mesh.n_cells
+    if "cells" in SINGLE_DESC[name]:
+        assert cells == SINGLE_DESC[name]["cells"], (name, cells)
+    return raw, mesh, scheme, u0, cells
 
 
+# ------------------------------------------------------------- rooflines
 def algorithmic_bytes_per_cell_stage(mesh, scheme, mixed: bool = False) -> int:
     """Compulsory unique HBM traffic of one cell through one stage of the
     reconstruction kernel, from the array sizes the kernel reads and writes.
@@ -153,6 +198,67 @@ def algorithmic_bytes_per_cell_stage(mesh, scheme, mixed: bool = False) -> int:
     return int(b)
 
 
+def _profile_value(key: str, kernel: str, workload_name: str, precision: str):
+    """A per-launch figure (DRAM bytes, FP64 flops) of `kernel` from the
+    committed ncu summaries (profiles/traffic.txt)."""
+    f = ROOT / "profiles" / "traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        kv = dict(x.split("=", 1) for x in line.split() if "=" in x)
+        if kv.get("kernel") == kernel and kv.get("workload") == workload_name and kv.get("precision") == precision \
+                and key in kv:
+            return float(kv[key])
+    return None
+
+
+def measured_peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return {"hbm_gbs": float(d.get("hbm_gbs", 6800.0)), "sm_max_mhz": float(d.get("sm_max_mhz", 2070.0)),
+                "kind": "measured"}
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "kind": "fallback"}
+
+
+def sm_count() -> int:
+    try:
+        import torch
+        return int(torch.cuda.get_device_properties(0).multi_processor_count)
+    except Exception:
+        return 152
+
+
+def fp64_peak_tflops() -> float:
+    """FP64 pipe peak: DFMA issue rate x 2 flop x SMs x maximum SM clock."""
+    return DFMA_PER_CLK_PER_SM * 2.0 * sm_count() * measured_peaks()["sm_max_mhz"] * 1e6 / 1e12
+
+
+def roofline_block(mesh, scheme, kt: dict, mixed: bool, workload_name: str, n_cells_launch: int,
+                   kernel: str = "k_reconstruct"):
+    """HBM roofline of the reconstruction kernel (the dominant launch): the
+    algorithmic bytes of one launch over its event-timed duration.  The FP64
+    form adds its FP64-pipe roofline: FP64 flops per launch (counted by ncu,
+    per cell) over the same duration against the FP64 pipe's peak."""
+    b_cell = algorithmic_bytes_per_cell_stage(mesh, scheme, mixed)
+    bytes_launch = b_cell * n_cells_launch
+    achieved = bytes_launch / (kt["reconstruct"] * 1e-3) / 1e9
+    peaks = measured_peaks()
+    prec = "mixed" if mixed else "fp64"
+    traffic = _profile_value("bytes_per_launch", kernel, workload_name, prec)
+    out = {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+           "frac": achieved / peaks["hbm_gbs"], "peak_kind": peaks["kind"], "bytes_per_cell_stage": b_cell,
+           "bytes_per_launch": bytes_launch, "traffic": traffic, "kernel_ms": kt}
+    flops_cell = _profile_value("fp64_flops_per_cell", kernel, workload_name, prec)
+    if flops_cell is not None:
+        tf = flops_cell * n_cells_launch / (kt["reconstruct"] * 1e-3) / 1e12
+        peak = fp64_peak_tflops()
+        out["fp64_pipe"] = {"achieved": tf, "peak": peak, "unit": "TFLOP/s", "frac": tf / peak,
+                            "flops_per_cell_stage": flops_cell,
+                            "peak_from": "2 DFMA/clk/SM x 2 flop x SMs x max SM clock"}
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -195,112 +301,145 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def profiles_traffic(kernel: str, workload_name: str, precision: str):
-    """DRAM traffic per launch of `kernel` from the committed ncu summary."""
-    f = ROOT / "profiles" / "traffic.txt"
-    if not f.exists():
-        return None
-    for line in f.read_text().splitlines():
-        kv = dict(x.split("=", 1) for x in line.split() if "=" in x)
-        if kv.get("kernel") == kernel and kv.get("workload") == workload_name and kv.get("precision") == precision:
-            return float(kv["bytes_per_launch"])
-    return None
-
-
-def measured_peaks():
-    f = ROOT / "MEASURED_PEAKS.json"
-    if f.exists():
-        d = json.loads(f.read_text())
-        return float(d.get("hbm_gbs", 6800.0)), "measured"
-    return 6800.0, "fallback"
-
-
-def cpu_baseline(raw, mesh, scheme, u0, desc, budget_s=20.0):
-    """The oracle (C++ restatement of the reference's OpenMP path) on a bounded
-    sample: whole RK steps of the full workload on all host cores."""
+# -------------------------------------------------- CPU arms (the oracle)
+def _oracle_step_rate(problems, threads: int, budget_s: float, min_steps: int = 1):
+    """Cell-stage updates/s of the oracle's SSP3 steps over `problems`
+    ((raw, stencils, vector, quad, u0, cells) each), one step of every
+    problem per round, rounds until the budget is spent."""
     from oracle import pyoracle
-    threads = os.cpu_count() or 1
-    o = pyoracle.Oracle(raw, mesh.stencils(), scheme.oracle_vector(), quad=mesh.quad, threads=threads)
-    dt = o.cfl_dt(u0)
+    orcs = []
+    for raw, st, vec, quad, u0, cells in problems:
+        o = pyoracle.Oracle(raw, st, vec, quad=quad, threads=threads)
+        orcs.append([o, u0, o.cfl_dt(u0), cells])
+    for rec in orcs:  # warm-up round
+        rec[1] = rec[0].step(rec[1], rec[2])
     t0 = time.perf_counter()
-    u = o.step(u0, dt)
-    one = time.perf_counter() - t0
-    n = max(1, min(20, int(budget_s / max(one, 1e-3))))
-    t0 = time.perf_counter()
-    for _ in range(n):
-        u = o.step(u, dt)
+    rounds = 0
+    while rounds < min_steps or time.perf_counter() - t0 < budget_s:
+        for rec in orcs:
+            rec[1] = rec[0].step(rec[1], rec[2])
+        rounds += 1
     el = time.perf_counter() - t0
-    cells = desc["cells"]
-    return {"value": cells * scheme.rk_stages * n / el, "unit": "cell-stage updates/s", "cores": threads,
-            "kind": "port", "sample": f"{n} SSP3 steps of the full {desc['workload']} mesh ({cells} cells) "
-                                      f"with the oracle's OpenMP loops on {threads} threads"}
+    cells = sum(rec[3] for rec in orcs)
+    return cells * 3 * rounds / el, rounds, cells
 
 
-def reference_sample(workload_name: str):
-    """A bounded sample of the workload for the CPU arm: the same scheme on a
-    smaller mesh of the same family."""
-    from problems import polytrope_2d, vortex_2d, vortex_tube_3d
-    if workload_name.startswith("c1"):
-        raw, mesh, scheme, u0 = vortex_2d(n=48, halo=3)
-        return raw, mesh, scheme, u0, mesh.info["n_interior_cells"], "C1 periodic isentropic vortex"
-    if workload_name.startswith("c3"):
-        raw, mesh, scheme, u0 = vortex_tube_3d(n=12, order=2 if workload_name == "c3o2" else 3)
-        return raw, mesh, scheme, u0, mesh.n_cells, "C3 tetrahedral vortex tube"
-    raw, mesh, scheme, u0 = polytrope_2d(n_rings=60, amplitude=1e-4)
-    name = {"c4": "C4 polytrope ensemble", "c5": "C5 serving request (polytrope disk)"}.get(
-        workload_name[:2], "C2 well-balanced polytrope disk")
-    return raw, mesh, scheme, u0, mesh.n_cells, name
+def cpu_baseline(problems, label: str, budget_s: float = 12.0, budget_1t_s: float = 6.0) -> dict:
+    """The oracle (the FP64 restatement of the reference's OpenMP path) on a
+    bounded sample of the workload: every host core, and one thread on the
+    sample's smallest problem (when one step of it takes seconds, not minutes)."""
+    threads = os.cpu_count() or 1
+    rate, rounds, cells = _oracle_step_rate(problems, threads, budget_s)
+    out = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"{rounds} SSP3 steps of {label} ({cells} cells) with the oracle's OpenMP loops on "
+                     f"{threads} threads"}
+    smallest = min(problems, key=lambda pr: pr[5])
+    if smallest[5] <= 300000:
+        rate1, rounds1, cells1 = _oracle_step_rate([smallest], 1, budget_1t_s)
+        out["one_thread"] = {"value": rate1, "unit": UNIT, "cores": 1,
+                             "sample": f"{rounds1} SSP3 steps of {cells1} cells on one thread"}
+    return out
+
+
+def _problem_of(raw, mesh, scheme, u0, cells):
+    return (raw, mesh.stencils(), scheme.oracle_vector(), mesh.quad, u0, cells)
+
+
+def c4_sample_indices(params) -> list:
+    order = sorted(range(len(params)), key=lambda k: params[k]["rings"])
+    return sorted({order[min(len(order) - 1, int(q * len(order)))] for q in C4_SAMPLE_QUANTILES})
+
+
+def write_reference_inputs(out_dir: Path = REF_INPUTS) -> list:
+    """Meshes, stencils, scheme vectors and initial states of the CPU arm's
+    samples (C4 size quantiles; the C2 disk), written by the product's set-up
+    so the reference arm reads them without loading the GPU library."""
+    import numpy as np
+    from problems import c4_instance, c4_instance_params, polytrope_2d
+    out_dir.mkdir(parents=True, exist_ok=True)
+    written = []
+
+    def save(name, raw, mesh, scheme, u0, cells):
+        st = mesh.stencils()
+        width = max(1, int(st["n_l2g"].max()))
+        np.savez_compressed(out_dir / f"{name}.npz", n_dims=raw.n_dims, vertices=raw.vertices,
+                            vertex_indices=raw.vertex_indices,
+                            ghost=raw.ghost if raw.ghost is not None else np.zeros(0, np.uint8),
+                            source=raw.source if raw.source is not None else np.zeros(0, np.int64),
+                            **{f"st_{k}": (v[:, :width] if k == "l2g" else v) for k, v in st.items()},
+                            vector=scheme.oracle_vector(), quad=np.array(mesh.quad), u0=u0, cells=cells)
+        written.append(out_dir / f"{name}.npz")
+
+    params = c4_instance_params(256, seed=C4_SEED)
+    for k in c4_sample_indices(params):
+        raw, mesh, scheme, u0 = c4_instance(params[k])
+        save(f"c4_{k:03d}", raw, mesh, scheme, u0, mesh.n_cells)
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=178, amplitude=1e-4)
+    save("c2", raw, mesh, scheme, u0, mesh.n_cells)
+    return written
+
+
+def read_reference_inputs(prefix: str, in_dir: Path = REF_INPUTS) -> list:
+    import types
+
+    import numpy as np
+    out = []
+    for f in sorted(in_dir.glob(f"{prefix}*.npz")):
+        d = np.load(f)
+        raw = types.SimpleNamespace(n_dims=int(d["n_dims"]), vertices=d["vertices"], vertex_indices=d["vertex_indices"],
+                                    ghost=d["ghost"] if d["ghost"].size else None,
+                                    source=d["source"] if d["source"].size else None)
+        st = {k[3:]: d[k] for k in d.files if k.startswith("st_")}
+        out.append((raw, st, d["vector"], tuple(int(x) for x in d["quad"]), d["u0"], int(d["cells"])))
+    return out
 
 
 def run_reference(args, rank, world):
-    """The reference's CPU implementation of the path (its oracle restatement;
-    the reference cannot be built here) timed on the host cores."""
+    """The reference's CPU implementation of the path (its FP64 restatement,
+    the oracle; the reference cannot be built here) on every host core, on a
+    bounded sample of the workload: each step is one SSP3 step of every
+    sample problem.  The meshes and stencils come from build()'s files, so
+    this process loads the oracle only."""
     if rank != 0:
         return
+    name = "c4" if args.workload.startswith("c4") else ("c2" if args.workload.startswith("c2") else None)
+    problems = read_reference_inputs("c4_" if name == "c4" else "c2") if name else []
+    if not problems:
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"no reference inputs for {args.workload} under {REF_INPUTS.relative_to(ROOT)} "
+                          "(build() writes the c4 and c2 samples)"}), flush=True)
+        return
     from oracle import pyoracle
-    raw, mesh, scheme, u0, cells, wl = reference_sample(args.workload)
     threads = os.cpu_count() or 1
-    o = pyoracle.Oracle(raw, mesh.stencils(), scheme.oracle_vector(), quad=mesh.quad, threads=threads)
-    dt = o.cfl_dt(u0)
-    u = u0
+    orcs = []
+    for raw, st, vec, quad, u0, cells in problems:
+        o = pyoracle.Oracle(raw, st, vec, quad=quad, threads=threads)
+        orcs.append([o, u0, o.cfl_dt(u0), cells])
     for _ in range(args.warmup):
-        u = o.step(u, dt)
+        for rec in orcs:
+            rec[1] = rec[0].step(rec[1], rec[2])
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        u = o.step(u, dt)
+        for rec in orcs:
+            rec[1] = rec[0].step(rec[1], rec[2])
     el = time.perf_counter() - t0
+    cells = sum(rec[3] for rec in orcs)
     value = cells * 3 * args.steps / el
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": wl, "cells_per_step_sample": cells, "precision": "fp64"},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"each step: one SSP3 step of a {cells}-cell mesh of the same workload "
-                                       f"family, oracle OpenMP loops on {threads} threads"},
+    config = c4_config(world) if name == "c4" else single_config("c2", "mixed", world)
+    sample = (f"each step: one SSP3 step of each of {len(orcs)} instances ({cells} cells; the ensemble's size "
+              f"quantiles {', '.join(str(q) for q in C4_SAMPLE_QUANTILES)}), oracle OpenMP loops on {threads} threads"
+              if name == "c4" else f"each step: one SSP3 step of the {cells}-cell disk, oracle OpenMP loops on "
+                                   f"{threads} threads")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded meshes and data)",
+            "impl": "reference", "config": config,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-METRIC = "cell-stage updates/s, FP64 vs mixed-batched at \u22641e-6 L1 error; p50/p99 latency"
-UNIT = "cell-stage updates/s"
-
-
-def roofline_block(mesh, scheme, kt: dict, mixed: bool, workload_name: str, n_cells_launch: int,
-                   kernel: str = "k_reconstruct"):
-    """HBM roofline of the reconstruction kernel (the dominant launch): the
-    algorithmic bytes of one launch over its event-timed duration."""
-    b_cell = algorithmic_bytes_per_cell_stage(mesh, scheme, mixed)
-    bytes_launch = b_cell * n_cells_launch
-    achieved = bytes_launch / (kt["reconstruct"] * 1e-3) / 1e9
-    hbm, peak_kind = measured_peaks()
-    traffic = profiles_traffic(kernel, workload_name, "mixed" if mixed else "fp64")
-    return {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "peak_kind": peak_kind, "bytes_per_cell_stage": b_cell,
-            "bytes_per_launch": bytes_launch, "traffic": traffic, "kernel_ms": kt,
-            "fp64_pipe_note": "the FP64 pipe (1.25 TFLOP/s measured) bounds these kernels before HBM does"}
-
-
+# ------------------------------------------------------------- GPU arm
 def pinned(shape):
     import numpy as np
     try:
@@ -346,92 +485,86 @@ def sum_over_ranks(pg, x: float) -> float:
     return float(t.item())
 
 
-def run_single_mesh(args, rank, world, local, pg):
+def single_mesh(name, precision, steps, warmup, rank, world, local, pg, profile=False, cpu=True,
+                extras=True) -> dict:
+    """One mesh: the `precision` form timed over `steps` graph-replayed steps
+    (value), its kernels, rooflines and e2e loop; with the mixed form the FP64
+    form beside it, the error between them, the well-balanced residual and (C2)
+    the run to t = 0.5."""
     import dataclasses
 
-    import numpy as np
     import zisafvm_gb300 as z
-    raw, mesh, scheme, u0, desc = workload(args.workload, args.precision)
-    mixed = args.precision == "mixed"
+    raw, mesh, scheme, u0, cells = workload(name, precision)
+    mixed = precision == "mixed"
     solver = z.Solver(mesh, scheme)
     solver.set_state(u0)
-    cells = desc["cells"]
     stages = scheme.rk_stages
-
-    # warm-up, then K graph-replayed steps timed with CUDA events
-    if args.warmup:
-        solver.advance_timed(args.warmup)
+    if warmup:
+        solver.advance_timed(warmup)
     if pg:
         pg.barrier()
     with ClockSampler(local) as clk:
-        ms = solver.advance_timed(args.steps)
+        ms = solver.advance_timed(steps)
     ms = max_over_ranks(pg, ms)
-    value = world * cells * stages * args.steps / (ms * 1e-3)
-
-    if args.profile:
-        if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms / args.steps,
-                              "config": desc, "profile_run": True}), flush=True)
-        return
-
-    kt = solver.kernel_times(min(args.steps, 32))
-    roof = roofline_block(mesh, scheme, kt, mixed, args.workload, mesh.n_cells)
-    e2e_steps = max(4, min(args.steps, 64))
+    value = world * cells * stages * steps / (ms * 1e-3)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": warmup,
+           "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32+f64" if mixed else "f64", "data": "synthetic (seeded mesh and initial data)",
+           "config": single_config(name, precision, world)}
+    if profile:
+        out["profile_run"] = True
+        return out
+    kt = solver.kernel_times(min(steps, 32))
+    out["roofline"] = roofline_block(mesh, scheme, kt, mixed, name, mesh.n_cells)
+    e2e_steps = max(4, min(steps, 64))
     e2e_s = max_over_ranks(pg, e2e_single(solver, mesh, u0, e2e_steps, pg))
-    e2e_value = world * cells * stages * e2e_steps / e2e_s
     io_bytes = mesh.n_cells * 5 * 8
-
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64",
-        "data": "synthetic (seeded mesh and initial data)",
-        "config": {**desc, "precision": args.precision, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 for c2/c3 (state, operators and face data > 129 MB)"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-                "path": "Solver.step_host (zfvm_step_host: upload, one CFL step, download) with pinned host buffers"},
-        "roofline": roof,
-        "gpu_launches": solver.launches_per_step() * args.steps,
-        "clocks": clk.summary(),
-    }
+    out["e2e"] = {"value": world * cells * stages * e2e_steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": io_bytes,
+                  "d2h_bytes_per_step": io_bytes,
+                  "path": "Solver.step_host (zfvm_step_host: upload, one CFL step, download) with pinned host buffers"}
+    out["gpu_launches"] = solver.launches_per_step() * steps
+    out["clocks"] = clk.summary()
+    solver.close()
     if mixed:
         # the plain FP64 form on the same mesh and data, timed the same way
-        s64 = z.Solver(mesh, dataclasses.replace(scheme, precision=z.FP64))
+        sch64 = dataclasses.replace(scheme, precision=z.FP64)
+        s64 = z.Solver(mesh, sch64)
         s64.set_state(u0)
-        if args.warmup:
-            s64.advance_timed(args.warmup)
-        ms64 = max_over_ranks(pg, s64.advance_timed(args.steps))
-        v64 = world * cells * stages * args.steps / (ms64 * 1e-3)
-        kt64 = s64.kernel_times(min(args.steps, 32))
-        line["fp64"] = {"value": v64, "ms_per_step": ms64 / args.steps,
-                        "roofline": roofline_block(mesh, dataclasses.replace(scheme, precision=z.FP64), kt64,
-                                                   False, args.workload, mesh.n_cells)}
-        line["mixed_over_fp64"] = value / v64
-        # error of the mixed form against the FP64 form after the same steps
-        from metrics import perturbation_rel_l1, state_rel_l1
-        s64.set_state(u0)
-        s32 = z.Solver(mesh, scheme)
-        s32.set_state(u0)
-        n_cmp = min(args.steps, 100)
-        s64.advance(n_steps=n_cmp)
-        s32.advance(n_steps=n_cmp)
-        u64, _ = s64.get_state()
-        u32, _ = s32.get_state()
-        mask = raw.ghost == 0 if raw.ghost is not None else None
-        line["error_vs_fp64"] = {"steps": n_cmp, "state_rel_l1": state_rel_l1(u32, u64, mask),
-                                 "perturbation_rel_l1": perturbation_rel_l1(u32, u64, u0, mask)}
-        if scheme.equilibrium:
-            line["well_balanced"] = well_balanced_residual(z, mesh, scheme, n_cmp)
-        if args.workload == "c2":
-            line["run_to_t_end"] = run_to_t_end(z, mesh, scheme, u0, 0.5)
-    if rank == 0:
+        if warmup:
+            s64.advance_timed(warmup)
+        ms64 = max_over_ranks(pg, s64.advance_timed(steps))
+        kt64 = s64.kernel_times(min(steps, 32))
+        out["fp64"] = {"value": world * cells * stages * steps / (ms64 * 1e-3), "ms_per_step": ms64 / steps,
+                       "roofline": roofline_block(mesh, sch64, kt64, False, name, mesh.n_cells)}
+        out["mixed_over_fp64"] = value / out["fp64"]["value"]
+        if extras:
+            # error of the mixed form against the FP64 form after the same steps
+            from metrics import perturbation_rel_l1, state_rel_l1
+            s64.set_state(u0)
+            s32 = z.Solver(mesh, scheme)
+            s32.set_state(u0)
+            n_cmp = min(max(steps, 20), 100)
+            s64.advance(n_steps=n_cmp)
+            s32.advance(n_steps=n_cmp)
+            u64, _ = s64.get_state()
+            u32, _ = s32.get_state()
+            s32.close()
+            mask = raw.ghost == 0 if raw.ghost is not None else None
+            out["error_vs_fp64"] = {"steps": n_cmp, "state_rel_l1": state_rel_l1(u32, u64, mask),
+                                    "perturbation_rel_l1": perturbation_rel_l1(u32, u64, u0, mask)}
+            if scheme.equilibrium:
+                out["well_balanced"] = well_balanced_residual(z, mesh, scheme, n_cmp)
+            if name == "c2":
+                out["run_to_t_end"] = run_to_t_end(z, mesh, scheme, u0, 0.5)
+        s64.close()
+    if cpu and rank == 0:
         try:
-            line["cpu_baseline"] = cpu_baseline(raw, mesh, scheme, u0, desc)
+            out["cpu_baseline"] = cpu_baseline([_problem_of(raw, mesh, scheme, u0, cells)],
+                                               f"the full {SINGLE_DESC[name]['workload']} mesh", budget_s=8.0,
+                                               budget_1t_s=4.0)
         except Exception as exc:  # the baseline must not hide the GPU number
-            line["cpu_baseline"] = {"error": str(exc)}
-        print(json.dumps(line), flush=True)
-    if pg:
-        pg.barrier()
+            out["cpu_baseline"] = {"error": str(exc)}
+    return out
 
 
 def run_to_t_end(z, mesh, scheme, u0, t_end: float) -> dict:
@@ -442,15 +575,15 @@ def run_to_t_end(z, mesh, scheme, u0, t_end: float) -> dict:
     from metrics import perturbation_rel_l1, state_rel_l1
     out = {"t_end": t_end}
     states = {}
-    for name, prec in (("mixed", z.MIXED), ("fp64", z.FP64)):
+    for label, prec in (("mixed", z.MIXED), ("fp64", z.FP64)):
         s = z.Solver(mesh, dataclasses.replace(scheme, precision=prec))
         s.set_state(u0)
         t0 = time.perf_counter()
         t, n = s.advance(t_end=t_end)
         wall = time.perf_counter() - t0
-        states[name], _ = s.get_state()
-        out[name] = {"t": t, "steps": n, "wall_s": wall,
-                     "cell_stage_updates_per_s": mesh.n_cells * scheme.rk_stages * n / wall}
+        states[label], _ = s.get_state()
+        out[label] = {"t": t, "steps": n, "wall_s": wall,
+                      "cell_stage_updates_per_s": mesh.n_cells * scheme.rk_stages * n / wall}
         s.close()
     out["error_vs_fp64"] = {"state_rel_l1": state_rel_l1(states["mixed"], states["fp64"]),
                             "perturbation_rel_l1": perturbation_rel_l1(states["mixed"], states["fp64"], u0)}
@@ -467,25 +600,28 @@ def well_balanced_residual(z, mesh, scheme, steps: int) -> dict:
     res = float(np.abs(s_eq.rate_of_change()).max())
     s_eq.advance(n_steps=steps)
     u_end, _ = s_eq.get_state()
+    s_eq.close()
     cols = [0, 4]  # rho and E (the momenta of the equilibrium are zero)
     drift = float((np.abs(u_end - u_eq)[:, cols].max(axis=0) / np.abs(u_eq)[:, cols].max(axis=0)).max())
     return {"max_abs_dudt": res, "rel_drift": drift, "steps": steps}
 
 
-def run_ensemble(args, rank, world, local, pg):
+def run_ensemble(args, rank, world, local, pg) -> dict:
     """C4: 256 independent well-balanced polytrope solves of uneven size in one
-    batch (mixed form, one persistent launch per phase per RK stage, grids
-    picked by the autotuner), against the plain FP64 form run one solve at a
-    time on the same instances."""
+    batch (mixed form, one persistent launch per phase per RK stage, launch
+    shapes picked by the autotuner), against the plain FP64 form run one solve
+    at a time on the same instances."""
     import dataclasses
 
     import numpy as np
     import zisafvm_gb300 as z
     from metrics import perturbation_rel_l1, state_rel_l1
-    from problems import ensemble_c4
-    n_inst = 256 if args.workload == "c4" else 16
+    from problems import c4_instance, c4_instance_params
+    small = args.workload == "c4-small"
+    n_inst = 16 if small else 256
     t_setup = time.perf_counter()
-    inst = ensemble_c4(n_inst, n_max=200000 if args.workload == "c4" else 40000, seed=2024 + 7919 * rank)
+    params = c4_instance_params(n_inst, n_max=40000 if small else 200000, seed=C4_SEED + 7919 * rank)
+    inst = [c4_instance(p) for p in params]
     t_setup = time.perf_counter() - t_setup
     total_cells = sum(m.n_cells for _, m, _, _ in inst)
     stages = 3
@@ -507,13 +643,17 @@ def run_ensemble(args, rank, world, local, pg):
         ms = batch.advance_timed(args.steps)
     ms = max_over_ranks(pg, ms)
     value = world * total_cells * stages * args.steps / (ms * 1e-3)
+    config = c4_config(world, n_inst)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded meshes and data)", "config": config}
     if args.profile:
-        if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms / args.steps,
-                              "config": {"workload": "C4", "instances": n_inst}, "profile_run": True}), flush=True)
-        return
+        line["profile_run"] = True
+        return line
+    sizes = sorted(m.n_cells for _, m, _, _ in inst)
     kt = batch.kernel_times(min(args.steps, 16))
     roof = roofline_block(inst[0][1], inst[0][2], kt, True, args.workload, total_cells, kernel="km_reconstruct")
+    tuned = batch.tuned_shapes() if hasattr(batch, "tuned_shapes") else None
 
     # end to end: every step uploads all states from pinned host memory, advances
     # the batch one step and reads every state back
@@ -531,11 +671,12 @@ def run_ensemble(args, rank, world, local, pg):
         for h, s in zip(hosts, solvers):
             s.get_state(out=h)
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
-    e2e_value = world * total_cells * stages * e2e_steps / e2e_s
     io_bytes = total_cells * 5 * 8
     launches = 1 + stages * 3   # clock + three persistent kernels per stage, one group
     batch.close()
-    del solvers
+    for s in solvers:
+        s.close()
+    del solvers, hosts
 
     # plain FP64 form, one solve at a time, same steps per instance
     k64 = max(3, min(args.steps, 24))
@@ -550,62 +691,55 @@ def run_ensemble(args, rank, world, local, pg):
     v64 = world * total_cells * stages * k64 / (ms64 * 1e-3)
 
     # accuracy of the mixed batched form against FP64 on a sample of instances
-    errs = []
-    sample = [inst[j] for j in np.linspace(0, n_inst - 1, 6).astype(int)]
+    # (among them the ends of the amplitude range)
+    amps = np.array([p["amplitude"] for p in params])
+    pick = sorted({int(j) for j in np.linspace(0, n_inst - 1, 6).astype(int)} | {int(amps.argmin()), int(amps.argmax())})
     n_cmp = 50
-    b2 = z.Batch(len(sample))
+    b2 = z.Batch(len(pick))
     pairs = []
-    for raw, mesh, scheme, u0 in sample:
+    for j in pick:
+        raw, mesh, scheme, u0 = inst[j]
         s32 = z.Solver(mesh, scheme)
         s32.set_state(u0)
         b2.add(s32, n_steps=n_cmp)
         s64 = z.Solver(mesh, dataclasses.replace(scheme, precision=z.FP64))
         s64.set_state(u0)
         s64.advance(n_steps=n_cmp)
-        pairs.append((s32, s64, raw, u0))
+        pairs.append((s32, s64, u0, params[j]["amplitude"]))
     while b2.advance(8):
         pass
-    for s32, s64, raw, u0 in pairs:
+    errs = []
+    for s32, s64, u0, amp in pairs:
         u32, _ = s32.get_state()
         u64, _ = s64.get_state()
-        errs.append((state_rel_l1(u32, u64, None), perturbation_rel_l1(u32, u64, u0, None)))
+        errs.append((state_rel_l1(u32, u64, None), perturbation_rel_l1(u32, u64, u0, None), amp))
+        s64.close()
     b2.close()
-    wb = well_balanced_residual(z, sample[0][1], sample[0][2], n_cmp)
+    wb = well_balanced_residual(z, inst[0][1], inst[0][2], n_cmp)
 
-    sizes = sorted(m.n_cells for _, m, _, _ in inst)
-    line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded meshes and data)",
-        "config": {"workload": f"C4 batched ensemble of {n_inst} well-balanced polytrope disks",
-                   "instances": n_inst, "cells": total_cells, "cells_min": sizes[0], "cells_median": sizes[len(sizes) // 2],
-                   "cells_max": sizes[-1], "precision": "mixed", "batched": True,
-                   "scheme": "CWENO-AO o3, HLLC, SSP3, CFL 0.45, isentropic well-balancing",
-                   "parallelism": f"replicas x{world}", "l2": "inputs larger than L2",
-                   "setup_s": t_setup, "autotune_s": t_tune},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
+    line.update({
+        "cells_total": total_cells, "cells_min": sizes[0], "cells_median": sizes[len(sizes) // 2],
+        "cells_max": sizes[-1], "setup_s": t_setup, "autotune_s": t_tune, "launch_shapes": tuned,
+        "e2e": {"value": world * total_cells * stages * e2e_steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
                 "path": "set_state of every slot / Batch.advance(1) / get_state of every slot, pinned buffers"},
-        "roofline": roof,
-        "gpu_launches": launches * args.steps,
-        "clocks": clk.summary(),
+        "roofline": roof, "gpu_launches": launches * args.steps, "clocks": clk.summary(),
         "fp64": {"value": v64, "ms_per_step": ms64 / k64, "form": "plain FP64, one solve at a time",
                  "steps_per_instance": k64},
         "mixed_batched_over_fp64": value / v64,
-        "error_vs_fp64": {"instances": len(sample), "steps": n_cmp,
+        "error_vs_fp64": {"instances": len(errs), "steps": n_cmp,
                           "state_rel_l1_max": max(e[0] for e in errs),
-                          "perturbation_rel_l1_max": max(e[1] for e in errs)},
+                          "perturbation_rel_l1_max": max(e[1] for e in errs),
+                          "perturbation_rel_l1_at_amplitude": {f"{e[2]:.2e}": e[1] for e in errs}},
         "well_balanced": wb,
-    }
+    })
     if rank == 0:
-        raw, mesh, scheme, u0 = inst[len(inst) // 2]
         try:
-            line["cpu_baseline"] = cpu_baseline(raw, mesh, scheme, u0,
-                                                {"cells": mesh.n_cells, "workload": "C4 ensemble instance"})
+            sample = [_problem_of(*inst[k], inst[k][1].n_cells) for k in c4_sample_indices(params)]
+            line["cpu_baseline"] = cpu_baseline(sample, f"{len(sample)} ensemble instances (size quantiles)")
         except Exception as exc:
             line["cpu_baseline"] = {"error": str(exc)}
-        print(json.dumps(line), flush=True)
-    if pg:
-        pg.barrier()
+    return line
 
 
 def serving_requests(n_req: int, seed: int, small: bool):
@@ -622,6 +756,7 @@ def serving_requests(n_req: int, seed: int, small: bool):
     from problems import polytrope_2d, polytrope_3d, vortex_2d
     rng = np.random.default_rng(seed)
     lo2, hi2, lo3, hi3 = (2000, 60000, 20000, 120000) if small else (2000, 500000, 50000, 2000000)
+
     def logu(lo, hi):
         return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
     pool = {"disk": [], "square": [], "cube": []}
@@ -687,13 +822,12 @@ def percentile(xs, q):
     return float(np.percentile(np.asarray(xs), q)) if xs else None
 
 
-def run_serving(args, rank, world, local, pg):
+def run_serving(args, rank, world, local, pg, small: bool) -> dict:
     """C5: Poisson arrivals of uneven 2D / 3D solves, admitted by device
     footprint and batched continuously; mixed form (value) next to the plain
     FP64 form serving the same stream."""
     import numpy as np
     import zisafvm_gb300 as z
-    small = args.workload == "c5-small"
     n_req = 12 if small else 32
     t0 = time.perf_counter()
     pool, reqs = serving_requests(n_req, seed=77 + 7919 * rank, small=small)
@@ -728,9 +862,8 @@ def run_serving(args, rank, world, local, pg):
     errs = [state_rel_l1(a[0], b[0], None) for a, b in zip(res, res64)]
     err_by_kind = {k: max([e for e, r in zip(errs, reqs) if r["kind"] == k], default=None)
                    for k in ("disk", "square", "cube")}
-    # e2e here is the serving path itself: host states in, host states out
     io_in = sum(r["mesh"].n_cells * 5 * 8 for r in reqs)
-    line = {
+    return {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": None, "warmup": 0,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64", "data": "synthetic (seeded meshes, data and arrivals)",
@@ -752,16 +885,24 @@ def run_serving(args, rank, world, local, pg):
         "error_vs_fp64": {"state_rel_l1_max": max(errs) if errs else None, "by_kind": err_by_kind},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": io_in, "d2h_bytes_per_step": io_in,
                 "path": "Server.submit / wait with host states (bytes per stream, not per step)"},
-        "roofline": None,
-        "gpu_launches": None,
         "clocks": clk.summary(),
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+
+
+BLOCK_DROP = ("metric", "unit", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "data")
+
+
+def _block(d: dict) -> dict:
+    """A workload's result as a sub-block of the headline line."""
+    return {k: v for k, v in d.items() if k not in BLOCK_DROP}
 
 
 def main():
     args = parse()
+    if args.write_reference_inputs:
+        for f in write_reference_inputs():
+            print(f.relative_to(ROOT))
+        return
     rank, world, local = dist_env()
     if world > 1:
         # replicas only: one GPU per process, no collective on the data path
@@ -774,11 +915,27 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
     elif args.workload.startswith("c4"):
-        run_ensemble(args, rank, world, local, pg)
+        line = run_ensemble(args, rank, world, local, pg)
+        # the other workloads as sub-blocks (one GPU: the scaling runs keep the headline only)
+        if not args.profile and not args.no_blocks and world == 1 and args.workload == "c4":
+            blocks = {}
+            for name in ("c2", "c3"):
+                blocks[name] = _block(single_mesh(name, "mixed", args.steps, args.warmup, rank, world, local, pg,
+                                                  cpu=False))
+            blocks["c5"] = _block(run_serving(args, rank, world, local, pg, small=False))
+            line.update(blocks)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
     elif args.workload.startswith("c5"):
-        run_serving(args, rank, world, local, pg)
+        line = run_serving(args, rank, world, local, pg, small=args.workload == "c5-small")
+        line["roofline"], line["gpu_launches"] = None, None
+        if rank == 0:
+            print(json.dumps(line), flush=True)
     else:
-        run_single_mesh(args, rank, world, local, pg)
+        line = single_mesh(args.workload, args.precision, args.steps, args.warmup, rank, world, local, pg,
+                           profile=args.profile)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
     if pg:
         pg.barrier()
 
