@@ -44,15 +44,19 @@ def test_max_and_sum_over_two_ranks():
 def test_reference_arm_under_torchrun_prints_one_line(zlib, olib):
     """`bench.py --impl reference` launched with two ranks: rank 0 alone times
     the CPU implementation and prints; rank 1 exits 0 without work."""
+    import bench
+    if not bench.read_reference_inputs("c2"):
+        bench.write_reference_inputs()  # build() writes them; a fresh checkout may not have run it
     port = _free_port()
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--workload", "c1-small"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--workload", "c2"]
     env = {**os.environ, "OMP_NUM_THREADS": "2"}
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [json.loads(x) for x in r.stdout.splitlines() if x.startswith("{")]
     assert len(lines) == 1
     line = lines[0]
+    assert "unavailable" not in line, line
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
