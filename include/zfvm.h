@@ -368,6 +368,14 @@ int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_running);
 int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *ms);
 /* Pick the persistent grid sizes of each group's kernels by timing candidates. */
 int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *best_ms);
+
+/* The launch shape of each of the batch's kernel groups (solvers of one stencil
+ * shape, form, flux and equilibrium): 6 entries per group -- shape id, threads
+ * per block (= cells or faces per tile), grids of the reconstruction, face and
+ * update kernels (0: one block per tile), 1 when the autotuner chose them.
+ * *n_groups is the number of groups; at most max_groups are written.  No
+ * counterpart in the reference (it runs one solve per process). */
+int zfvm_batch_launch_shapes(const zfvm_batch *b, int32_t max_groups, int32_t *shapes, int32_t *n_groups);
 /* Average per-launch device time (ms) of the three batched stage kernels
  * {reconstruct, face flux, update} over `n_steps` steps (events, no graph). */
 int zfvm_batch_kernel_times(zfvm_batch *b, int32_t n_steps, float *ms);

@@ -67,13 +67,17 @@ def test_batch_t_end(zlib):
 
 
 def test_batch_autotune_keeps_results(zlib):
-    """The persistent grid size the autotuner picks does not change results."""
+    """The launch shape the autotuner picks (cells or faces per tile = threads
+    per block, 64 / 128 / 256, and the persistent grid) does not change results."""
     raw, mesh, scheme, u0 = polytrope_2d(n_rings=14, amplitude=1e-3, precision=z.MIXED)
     s_tuned = z.Solver(mesh, scheme)
     s_tuned.set_state(u0)
     tuner = z.Batch(2)
     slot = tuner.add(s_tuned, n_steps=1000)
+    assert tuner.tuned_shapes() == []  # no group before the first advance
     tuner.autotune(2)
+    shapes = tuner.tuned_shapes()
+    assert len(shapes) == 1 and shapes[0]["tuned"] and shapes[0]["block"] in (64, 128, 256), shapes
     tuner.remove(slot)
     u1, t1 = s_tuned.get_state()
     s_plain = z.Solver(mesh, scheme)
@@ -184,3 +188,20 @@ def test_step_host_matches_separate_calls(zlib):
     out = u0.copy()
     u_b, t_b, n_b = b.step_host(out, n_steps=1, fixed_dt=1e-3, out=out)  # in place
     assert n_b == 1 and abs(t_b - 1e-3) < 1e-18 and np.array_equal(u_b, u_a)
+
+
+def test_batch_advance_takes_exactly_the_steps_asked(zlib):
+    """Batch.advance(n) replays n steps even when n is not a multiple of the
+    captured step chunk (whole chunks, then a graph of the rest)."""
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=10, amplitude=1e-3, precision=z.MIXED)
+    s = z.Solver(mesh, scheme)
+    s.set_state(u0)
+    b = z.Batch(1)
+    slot = b.add(s, n_steps=1 << 40)
+    total = 0
+    for n in (12, 5, 8, 3):
+        b.advance(n)
+        total += n
+        assert b.status(slot)["steps"] == total
+    b.advance_timed(13)
+    assert b.status(slot)["steps"] == total + 13

@@ -70,5 +70,5 @@ def test_apply_boundary_frozen_cells(zlib):
     assert np.array_equal(out[ghost], u0[ghost]) and np.array_equal(out[~ghost], u[~ghost])
     assert np.array_equal(qout[ghost], q0[ghost]) and np.array_equal(qout[~ghost], q[~ghost])
     # without frozen rows the ghost rows are kept
-    kept = s.apply_boundary(u)
-    assert np.array_equal(kept, u)
+    kept, qkept = s.apply_boundary(u, avars=q)
+    assert np.array_equal(kept, u) and np.array_equal(qkept, q)

@@ -357,27 +357,41 @@ def test_equilibrium_refresh_schedule(zlib, olib, spr, threshold):
     reconstructions, or sooner when the scaled (rho, E_int) of the cell move
     recompute_threshold away from the equilibrium's own cell average.  Every
     reconstruction counts (right-hand sides and RK stages alike), on the GPU
-    as in the oracle."""
+    as in the oracle.  A stale equilibrium changes a well-balanced
+    reconstruction only a little, so the disk carries a large perturbation
+    (amplitude 0.3), where the schedule moves the result by 1e-7 - 1e-6 of its
+    change: the GPU must follow the oracle to a thousandth of that."""
     z = zlib
-    raw, mesh, scheme, u0 = polytrope_2d(n_rings=20, amplitude=1e-2)
-    scheme.steps_per_recompute, scheme.recompute_threshold = spr, threshold
-    s = z.Solver(mesh, scheme)
-    s.set_state(u0)
-    o = _oracle(olib, raw, mesh, scheme)
-    t_gpu, t_ref = s.rate_of_change(), o.rate_of_change(u0)
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=0.3)
+
+    def run(spr_, thr_, oracle=False):
+        sc = z.Scheme(**{**scheme.__dict__, "steps_per_recompute": spr_, "recompute_threshold": thr_})
+        if oracle:
+            o = _oracle(olib, raw, mesh, sc)
+            t = o.rate_of_change(u0)
+            return t, o.run(u0, n_steps=8)[0]
+        s = z.Solver(mesh, sc)
+        s.set_state(u0)
+        t = s.rate_of_change()
+        s.advance(n_steps=8)
+        u, _ = s.get_state()
+        s.close()
+        return t, u
+
+    t_gpu, u_gpu = run(spr, threshold)
+    t_ref, u_ref = run(spr, threshold, oracle=True)
     assert np.abs(t_gpu - t_ref).max() <= RHS_WB * np.abs(t_ref).max()
-    s.advance(n_steps=6)
-    u_gpu, t1 = s.get_state()
-    u_ref, t_ref1, _ = o.run(u0, n_steps=6)
     _assert_state(u_gpu, u_ref)
-    assert abs(t1 - t_ref1) <= 1e-12 * t_ref1
-    # the schedule changes the result: a refresh at every reconstruction differs
-    every = z.Solver(mesh, z.Scheme(**{**scheme.__dict__, "steps_per_recompute": 1}))
-    every.set_state(u0)
-    every.rate_of_change()
-    every.advance(n_steps=6)
-    u_every, _ = every.get_state()
-    assert np.abs(u_every - u_gpu).max() > 1e-3 * np.abs(u_ref - u0).max()
+    err = deviation_rel_max(u_gpu, u_ref, u0)
+    # the schedule acts: against a refresh at every reconstruction and, with a
+    # threshold, against never refreshing after the first
+    effect = deviation_rel_max(run(1, 0.0)[1], u_ref, u0)
+    print(f"schedule {spr}/{threshold:g}: GPU vs oracle {err:.2e}, schedule effect {effect:.2e}")
+    assert err <= 1e-3 * effect
+    if threshold < 1.0:
+        never = deviation_rel_max(run(1000000, 1e30)[1], u_ref, u0)
+        print(f"  against never refreshing: {never:.2e}")
+        assert err <= 1e-3 * never
 
 
 def test_zero_threshold_refreshes_every_reconstruction(zlib):

@@ -143,6 +143,7 @@ def load_library() -> C.CDLL:
         "zfvm_batch_advance_timed": [vp, i32, C.POINTER(C.c_float)],
         "zfvm_batch_autotune": [vp, i32, C.POINTER(C.c_float)],
         "zfvm_batch_kernel_times": [vp, i32, C.POINTER(C.c_float)],
+        "zfvm_batch_launch_shapes": [vp, i32, C.POINTER(i32), C.POINTER(i32)],
         "zfvm_batch_slot_status": [vp, i32, dp, C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)],
         "zfvm_batch_slots": [vp, C.POINTER(i32)],
         "zfvm_solver_footprint": [vp, vp, C.POINTER(i64)],
@@ -643,6 +644,16 @@ class Batch:
         ms = (C.c_float * 3)()
         _check(load_library().zfvm_batch_kernel_times(self._h, n_steps, ms))
         return {"reconstruct": ms[0], "face_flux": ms[1], "update": ms[2]}
+
+    def tuned_shapes(self) -> list:
+        """Launch shape of each kernel group: stencil shape id, threads per block
+        (= tile size), grids of the three kernels (0: one block per tile), tuned."""
+        buf = (C.c_int32 * (6 * 16))()
+        n = C.c_int32()
+        _check(load_library().zfvm_batch_launch_shapes(self._h, 16, buf, C.byref(n)))
+        return [{"shape": buf[6 * k], "block": buf[6 * k + 1], "grid_recon": buf[6 * k + 2],
+                 "grid_face": buf[6 * k + 3], "grid_update": buf[6 * k + 4], "tuned": bool(buf[6 * k + 5])}
+                for k in range(min(n.value, 16))]
 
     def status(self, slot: int) -> dict:
         t, st, done, status = C.c_double(), C.c_int64(), C.c_int32(), C.c_int32()

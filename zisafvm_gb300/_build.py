@@ -30,12 +30,12 @@ NVCCFLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "--compress-mode=size", "-
 HOST_SOURCES = ["grid.cpp", "stencil.cpp", "mesh.cpp", "capi_mesh.cpp", "snapshot.cpp"]
 CUDA_SOURCES = ["solver.cu", "batch.cu", "server.cu", "noalloc.cu", "flux_api.cu"]
 # inst_shape.cu compiled once per stencil shape x precision x (single solver,
-# batch): (object name, -D flags)
+# batch of 64, 128 or 256 threads per block): (object name, -D flags)
 SHAPES = {"s2o3": "S2o3", "s2o2": "S2o2", "s3o3": "S3o3", "s3o2": "S3o2"}
 SHAPE_UNITS = [
-    (f"inst_{name}_{'mix' if mixed else 'f64'}{'_batch' if batch else ''}",
+    (f"inst_{name}_{'mix' if mixed else 'f64'}{f'_batch{batch}' if batch else ''}",
      [f"-DZFVM_SHAPE_NAME={name}", f"-DZFVM_SHAPE={cls}", f"-DZFVM_MIXED={mixed}", f"-DZFVM_BATCH={batch}"])
-    for name, cls in SHAPES.items() for mixed in (0, 1) for batch in (0, 1)
+    for name, cls in SHAPES.items() for mixed in (0, 1) for batch in (0, 64, 128, 256)
 ]
 
 
@@ -79,7 +79,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     workers = max(1, min(len(jobs), os.cpu_count() or 4))
     if jobs:
         # the slowest units first, so they do not start last
-        jobs.sort(key=lambda cmd: 0 if "-DZFVM_SHAPE_NAME=s3o2" in cmd or "-DZFVM_SHAPE_NAME=s3o3" in cmd else 1)
+        jobs.sort(key=lambda cmd: (0 if "-DZFVM_BATCH=0" in cmd else 1,
+                                   0 if "-DZFVM_SHAPE_NAME=s3o2" in cmd or "-DZFVM_SHAPE_NAME=s3o3" in cmd else 1))
         with ThreadPoolExecutor(max_workers=workers) as ex:
             for cmd, _ in zip(jobs, ex.map(_run, jobs)):
                 if verbose:

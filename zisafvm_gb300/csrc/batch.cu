@@ -2,9 +2,9 @@
 //
 // Solvers are added to slots; slots of one kernel configuration form a group.
 // Every RK stage launches one persistent reconstruction, one face and one
-// update kernel per group; each walks the group's tile list (128 cells or
-// faces per tile, one instance per tile), so meshes of any size share the
-// launches.  Each slot keeps its own device clock: its own CFL time step, step
+// update kernel per group; each walks the group's tile list (64, 128 or 256
+// cells or faces per tile as the autotuner picked, one instance per tile), so
+// meshes of any size share the launches.  Each slot keeps its own device clock: its own CFL time step, step
 // count and end time; a slot that is done stops doing work.  The step loop is
 // captured in a CUDA graph and replayed; adding or removing a slot only
 // rebuilds the small device tables and re-captures the graph.
@@ -50,7 +50,8 @@ struct Group {
   DBuf<BatchInst> inst;
   DBuf<Tile> cell_tiles, face_tiles;
   int n_ct = 0, n_ft = 0;
-  int grid[3] = {0, 0, 0};
+  int block = 128;          // threads per block = cells or faces per tile
+  int grid[3] = {0, 0, 0};  // persistent grid of the three kernels (0: one block per tile)
   bool tuned = false;
 };
 
@@ -65,8 +66,10 @@ struct zfvm_batch {
   DBuf<double> cfls;
   DBuf<int> running;
   int n_clock = 0;
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
+  // captured step loops: `graph` replays graph_steps steps, `graph_tail` the
+  // remainder of a step count that is not a multiple of it
+  cudaGraphExec_t graph = nullptr, graph_tail = nullptr;
+  int graph_steps = 0, graph_tail_steps = 0;
   bool dirty = true;
   int sms = 0;
 };
@@ -80,6 +83,7 @@ void launch_group_stage(zfvm_batch *b, Group &g, int stage, cudaEvent_t *ev = nu
   c.src = g.key.src;
   c.mixed = g.key.mixed;
   c.flux = g.key.flux;
+  c.block = g.block;
   c.grid_recon = g.grid[0];
   c.grid_face = g.grid[1];
   c.grid_update = g.grid[2];
@@ -112,6 +116,13 @@ void enqueue_batch_step(zfvm_batch *b) {
   }
 }
 
+void drop_graphs(zfvm_batch *b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->graph_tail) cudaGraphExecDestroy(b->graph_tail);
+  b->graph = b->graph_tail = nullptr;
+  b->graph_steps = b->graph_tail_steps = 0;
+}
+
 // Rebuild the device tables of every group from the current slots.
 void rebuild(zfvm_batch *b) {
   for (auto &kv : b->groups) kv.second->slots.clear();
@@ -142,8 +153,8 @@ void rebuild(zfvm_batch *b) {
       I.P = s->P;
       for (int st = 0; st < 3; ++st) I.a[st] = stage_args(s, std::min(st, s->P.n_stages - 1), nullptr);
       inst.push_back(I);
-      for (int c = 0; c < s->n_cells; c += 128) ct.push_back(Tile{(int)j, c});
-      for (int e = 0; e < s->n_edges; e += 128) ft.push_back(Tile{(int)j, e});
+      for (int c = 0; c < s->n_cells; c += g.block) ct.push_back(Tile{(int)j, c});
+      for (int e = 0; e < s->n_edges; e += g.block) ft.push_back(Tile{(int)j, e});
     }
     g.inst.upload(inst);
     g.cell_tiles.upload(ct);
@@ -154,27 +165,42 @@ void rebuild(zfvm_batch *b) {
   b->clock_ptrs.upload(clocks);
   b->cfls.upload(cfls);
   b->n_clock = (int)clocks.size();
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  drop_graphs(b);
   b->dirty = false;
 }
 
-void ensure_graph(zfvm_batch *b, int steps) {
-  if (b->dirty) rebuild(b);
-  if (b->graph && b->graph_steps == steps) return;
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+void capture_steps(zfvm_batch *b, int steps, cudaGraphExec_t *out) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < steps; ++k) enqueue_batch_step(b);
   CK(cudaStreamEndCapture(b->stream, &g));
-  CK(cudaGraphInstantiate(&b->graph, g, 0));
+  CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);
-  b->graph_steps = steps;
+}
+
+// The graphs that replay exactly n_steps steps: n_steps / chunk replays of a
+// `chunk`-step graph (chunk = min(n_steps, chunk_max)) and one graph of the rest.
+int prepare_graphs(zfvm_batch *b, int n_steps, int chunk_max) {
+  if (b->dirty) rebuild(b);
+  const int chunk = std::min(n_steps, chunk_max), tail = n_steps % chunk;
+  if (!b->graph || b->graph_steps != chunk) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    capture_steps(b, chunk, &b->graph);
+    b->graph_steps = chunk;
+  }
+  if (tail && (!b->graph_tail || b->graph_tail_steps != tail)) {
+    if (b->graph_tail) cudaGraphExecDestroy(b->graph_tail);
+    b->graph_tail = nullptr;
+    capture_steps(b, tail, &b->graph_tail);
+    b->graph_tail_steps = tail;
+  }
+  return chunk;
+}
+
+void launch_graphs(zfvm_batch *b, int n_steps, int chunk) {
+  for (int k = 0; k + chunk <= n_steps; k += chunk) CK(cudaGraphLaunch(b->graph, b->stream));
+  if (n_steps % chunk) CK(cudaGraphLaunch(b->graph_tail, b->stream));
 }
 
 // Work a caller queued on a slot's own stream (the layout and CFL kernels of
@@ -230,7 +256,7 @@ extern "C" int zfvm_batch_create(int32_t max_slots, zfvm_batch **out) {
 
 extern "C" int zfvm_batch_destroy(zfvm_batch *b) {
   if (!b) return ZFVM_OK;
-  if (b->graph) cudaGraphExecDestroy(b->graph);
+  drop_graphs(b);
   if (b->stream) {
     cudaStreamSynchronize(b->stream);
     cudaStreamDestroy(b->stream);
@@ -277,14 +303,9 @@ extern "C" int zfvm_batch_remove(zfvm_batch *b, int32_t slot) {
 extern "C" int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_running) {
   if (!b || max_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
   BATCH_GUARD_BEGIN
-  const int chunk = std::min(max_steps, 8);
-  ensure_graph(b, chunk);
+  const int chunk = prepare_graphs(b, max_steps, 8);
   wait_for_slots(b);
-  int done_steps = 0;
-  while (done_steps < max_steps) {
-    CK(cudaGraphLaunch(b->graph, b->stream));
-    done_steps += chunk;
-  }
+  launch_graphs(b, max_steps, chunk);
   int r = running_count(b);
   if (n_running) *n_running = r;
   return ZFVM_OK;
@@ -294,15 +315,14 @@ extern "C" int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_r
 extern "C" int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *ms) {
   if (!b || !ms || n_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
   BATCH_GUARD_BEGIN
-  const int chunk = std::min(n_steps, 8);
-  ensure_graph(b, chunk);
+  const int chunk = prepare_graphs(b, n_steps, 8);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   wait_for_slots(b);
   CK(cudaStreamSynchronize(b->stream));
   CK(cudaEventRecord(e0, b->stream));
-  for (int k = 0; k < n_steps; k += chunk) CK(cudaGraphLaunch(b->graph, b->stream));
+  launch_graphs(b, n_steps, chunk);
   CK(cudaEventRecord(e1, b->stream));
   CK(cudaEventSynchronize(e1));
   CK(cudaEventElapsedTime(ms, e0, e1));
@@ -312,9 +332,11 @@ extern "C" int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *m
   BATCH_GUARD_END
 }
 
-// Autotuner: time the persistent grid size of each group's kernels
-// (multiples of the SM count up to the occupancy limit, or one block per tile)
-// over `trial_steps` steps and keep the fastest.  The slots' states advance.
+// Autotuner: for each group, every tile size / block size (64, 128, 256 cells
+// or faces per tile and threads per block) with every grid (one block per
+// tile, or a persistent grid of 1x or 2x the occupancy limit times the SM
+// count), timed over `trial_steps` steps; the fastest is kept.  The slots'
+// states advance.
 extern "C" int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *best_ms) {
   if (!b || trial_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
   BATCH_GUARD_BEGIN
@@ -324,45 +346,66 @@ extern "C" int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *be
   for (auto &kv : b->groups) {
     Group &g = *kv.second;
     if (g.n_ct == 0) continue;
-    BatchCfg c{};
-    c.mixed = g.key.mixed;
-    int occ[3] = {1, 1, 1};
-    switch (g.key.shape) {
-      case 0: batch_occupancy_s2o3(c, occ); break;
-      case 1: batch_occupancy_s2o2(c, occ); break;
-      case 2: batch_occupancy_s3o3(c, occ); break;
-      case 3: batch_occupancy_s3o2(c, occ); break;
-    }
-    std::vector<std::array<int, 3>> cands;
-    cands.push_back({0, 0, 0});  // one block per tile
-    for (int m : {1, 2})
-      cands.push_back({std::max(1, occ[0] * m) * b->sms, std::max(1, occ[1] * m) * b->sms,
-                       std::max(1, occ[2] * m) * b->sms});
     float best = 1e30f;
-    std::array<int, 3> pick = cands[0];
-    for (auto &cand : cands) {
-      for (int j = 0; j < 3; ++j) g.grid[j] = cand[j];
-      if (b->graph) {
-        cudaGraphExecDestroy(b->graph);
-        b->graph = nullptr;
+    int best_block = g.block;
+    std::array<int, 3> pick{0, 0, 0};
+    for (int block : {64, 128, 256}) {
+      g.block = block;
+      rebuild(b);  // the group's tile lists for this tile size
+      BatchCfg c{};
+      c.mixed = g.key.mixed;
+      c.block = block;
+      int occ[3] = {1, 1, 1};
+      switch (g.key.shape) {
+        case 0: batch_occupancy_s2o3(c, occ); break;
+        case 1: batch_occupancy_s2o2(c, occ); break;
+        case 2: batch_occupancy_s3o3(c, occ); break;
+        case 3: batch_occupancy_s3o2(c, occ); break;
       }
-      float ms = 0;
-      int32_t n = trial_steps;
-      int st = zfvm_batch_advance_timed(b, n, &ms);
-      if (st) return st;
-      if (ms < best) best = ms, pick = cand;
+      std::vector<std::array<int, 3>> cands;
+      cands.push_back({0, 0, 0});  // one block per tile
+      for (int m : {1, 2})
+        cands.push_back({std::max(1, occ[0] * m) * b->sms, std::max(1, occ[1] * m) * b->sms,
+                         std::max(1, occ[2] * m) * b->sms});
+      for (auto &cand : cands) {
+        for (int j = 0; j < 3; ++j) g.grid[j] = cand[j];
+        drop_graphs(b);
+        float ms = 0;
+        int st = zfvm_batch_advance_timed(b, trial_steps, &ms);
+        if (st) return st;
+        if (ms < best) best = ms, best_block = block, pick = cand;
+      }
     }
+    g.block = best_block;
     for (int j = 0; j < 3; ++j) g.grid[j] = pick[j];
     g.tuned = true;
+    rebuild(b);
     overall += best;
   }
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  drop_graphs(b);
   if (best_ms) *best_ms = overall;
   return ZFVM_OK;
   BATCH_GUARD_END
+}
+
+// The launch shape of every group: shape id, threads per block (= tile size),
+// the grids of the reconstruction, face and update kernels (0: one block per
+// tile), and whether the autotuner chose them.
+extern "C" int zfvm_batch_launch_shapes(const zfvm_batch *b, int32_t max_groups, int32_t *shapes,
+                                        int32_t *n_groups) {
+  if (!b || !n_groups || (max_groups > 0 && !shapes)) return fail(ZFVM_EINVAL, "null argument");
+  int k = 0;
+  for (const auto &kv : b->groups) {
+    const Group &g = *kv.second;
+    if (g.slots.empty()) continue;
+    if (k < max_groups) {
+      int32_t *o = shapes + 6 * k;
+      o[0] = g.key.shape, o[1] = g.block, o[2] = g.grid[0], o[3] = g.grid[1], o[4] = g.grid[2], o[5] = g.tuned;
+    }
+    ++k;
+  }
+  *n_groups = k;
+  return ZFVM_OK;
 }
 
 // Average device time (ms) of one launch of each of the three stage kernels
@@ -373,10 +416,7 @@ extern "C" int zfvm_batch_kernel_times(zfvm_batch *b, int32_t n_steps, float *ms
   BATCH_GUARD_BEGIN
   if (b->dirty) rebuild(b);
   wait_for_slots(b);
-  if (b->graph) {
-    cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-  }
+  drop_graphs(b);
   cudaEvent_t ev[4];
   for (auto &e : ev) CK(cudaEventCreate(&e));
   double acc[3] = {0.0, 0.0, 0.0};

@@ -783,19 +783,29 @@ void reset_clock_for_run(zfvm_solver *s, int64_t n_steps, double t_end, double f
 
 namespace {
 
-void build_graph(zfvm_solver *s, int steps) {
-  if (s->graph && s->graph_steps == steps) return;
-  if (s->graph) {
-    cudaGraphExecDestroy(s->graph);
-    s->graph = nullptr;
-  }
+void capture_steps(zfvm_solver *s, int steps, cudaGraphExec_t *out) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < steps; ++k) enqueue_step(s);
   CK(cudaStreamEndCapture(s->stream, &g));
-  CK(cudaGraphInstantiate(&s->graph, g, 0));
+  CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);
+}
+
+void build_graph(zfvm_solver *s, int steps) {
+  if (s->graph && s->graph_steps == steps) return;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  capture_steps(s, steps, &s->graph);
   s->graph_steps = steps;
+}
+
+void build_tail_graph(zfvm_solver *s, int steps) {
+  if (s->graph_tail && s->graph_tail_steps == steps) return;
+  if (s->graph_tail) cudaGraphExecDestroy(s->graph_tail);
+  s->graph_tail = nullptr;
+  capture_steps(s, steps, &s->graph_tail);
+  s->graph_tail_steps = steps;
 }
 
 }  // namespace
@@ -1081,18 +1091,17 @@ extern "C" int zfvm_advance_timed(zfvm_solver *s, int64_t n_steps, float *ms) {
   if (!s || !ms || n_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
   SOLVER_GUARD_BEGIN
   reset_clock_for_run(s, n_steps, 0.0, 0.0);
-  const int chunk = (int)std::min<int64_t>(n_steps, 16);
+  // exactly n_steps steps: whole 16-step graphs and one graph of the rest
+  const int chunk = (int)std::min<int64_t>(n_steps, 16), tail = (int)(n_steps % chunk);
   build_graph(s, chunk);
+  if (tail) build_tail_graph(s, tail);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   CK(cudaStreamSynchronize(s->stream));
   CK(cudaEventRecord(e0, s->stream));
-  int64_t launched = 0;
-  while (launched < n_steps) {
-    CK(cudaGraphLaunch(s->graph, s->stream));
-    launched += chunk;
-  }
+  for (int64_t k = 0; k + chunk <= n_steps; k += chunk) CK(cudaGraphLaunch(s->graph, s->stream));
+  if (tail) CK(cudaGraphLaunch(s->graph_tail, s->stream));
   CK(cudaEventRecord(e1, s->stream));
   CK(cudaEventSynchronize(e1));
   CK(cudaEventElapsedTime(ms, e0, e1));

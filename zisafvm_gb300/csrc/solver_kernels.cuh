@@ -1642,9 +1642,16 @@ struct Tile {
   int slot, begin;
 };
 
-template <class S, int EQ, int SRC, bool MIXED>
-__global__ void __launch_bounds__(128) km_reconstruct(const BatchInst *__restrict__ inst,
-                                                      const Tile *__restrict__ tiles, int n_tiles, int stage) {
+// The batched kernels run blocks of BS threads over tiles of BS cells or
+// faces (BS = 64, 128 or 256, picked per group by the autotuner).  The mixed
+// reconstruction keeps the single-solver kernel's register budget per thread:
+// its per-shape bound of blocks per SM scaled to the block size.
+template <class S, int EQ, int BS>
+constexpr int kBatchReconBlocks = (kMixedReconBlocks<S, EQ> * 128 + BS - 1) / BS;
+
+template <class S, int EQ, int SRC, bool MIXED, int BS>
+__global__ void __launch_bounds__(BS) km_reconstruct(const BatchInst *__restrict__ inst,
+                                                     const Tile *__restrict__ tiles, int n_tiles, int stage) {
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const Tile tl = tiles[t];
     const BatchInst &I = inst[tl.slot];
@@ -1652,10 +1659,9 @@ __global__ void __launch_bounds__(128) km_reconstruct(const BatchInst *__restric
   }
 }
 
-template <class S, int EQ, int SRC, bool MIXED>
-__global__ void __launch_bounds__(128, kMixedReconBlocks<S, EQ>) km_reconstruct_mixed(const BatchInst *__restrict__ inst,
-                                                                                  const Tile *__restrict__ tiles,
-                                                                                  int n_tiles, int stage) {
+template <class S, int EQ, int SRC, bool MIXED, int BS>
+__global__ void __launch_bounds__(BS, (kBatchReconBlocks<S, EQ, BS>)) km_reconstruct_mixed(
+    const BatchInst *__restrict__ inst, const Tile *__restrict__ tiles, int n_tiles, int stage) {
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const Tile tl = tiles[t];
     const BatchInst &I = inst[tl.slot];
@@ -1663,17 +1669,17 @@ __global__ void __launch_bounds__(128, kMixedReconBlocks<S, EQ>) km_reconstruct_
   }
 }
 
-template <class S, int EQ, int SRC, bool MIXED>
+template <class S, int EQ, int SRC, bool MIXED, int BS>
 constexpr auto batch_recon_kernel() {
   if constexpr (MIXED)
-    return &km_reconstruct_mixed<S, EQ, SRC, MIXED>;
+    return &km_reconstruct_mixed<S, EQ, SRC, MIXED, BS>;
   else
-    return &km_reconstruct<S, EQ, SRC, MIXED>;
+    return &km_reconstruct<S, EQ, SRC, MIXED, BS>;
 }
 
-template <class S, int FLUX, int EQ, bool MIXED>
-__global__ void __launch_bounds__(128) km_face_flux(const BatchInst *__restrict__ inst,
-                                                    const Tile *__restrict__ tiles, int n_tiles, int stage) {
+template <class S, int FLUX, int EQ, bool MIXED, int BS>
+__global__ void __launch_bounds__(BS) km_face_flux(const BatchInst *__restrict__ inst,
+                                                   const Tile *__restrict__ tiles, int n_tiles, int stage) {
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const Tile tl = tiles[t];
     const BatchInst &I = inst[tl.slot];
@@ -1681,9 +1687,9 @@ __global__ void __launch_bounds__(128) km_face_flux(const BatchInst *__restrict_
   }
 }
 
-template <class S, bool MIXED>
-__global__ void __launch_bounds__(128) km_update(const BatchInst *__restrict__ inst, const Tile *__restrict__ tiles,
-                                                 int n_tiles, int stage) {
+template <class S, bool MIXED, int BS>
+__global__ void __launch_bounds__(BS) km_update(const BatchInst *__restrict__ inst, const Tile *__restrict__ tiles,
+                                                int n_tiles, int stage) {
   for (int t = blockIdx.x; t < n_tiles; t += gridDim.x) {
     const Tile tl = tiles[t];
     const BatchInst &I = inst[tl.slot];
@@ -1697,53 +1703,58 @@ __global__ void __launch_bounds__(128) km_update(const BatchInst *__restrict__ i
 struct BatchCfg {
   bool eq, src, mixed;
   int flux;
-  int grid_recon, grid_face, grid_update;  // persistent grid sizes (autotuned)
+  int block = 128;                         // threads per block = cells or faces per tile
+  int grid_recon, grid_face, grid_update;  // persistent grid sizes (autotuned; 0: one block per tile)
   cudaStream_t stream;
   cudaEvent_t *ev = nullptr;  // optional: 4 events recorded around the three stage kernels
 };
 
-template <class S, bool MIXED>
+template <class S, bool MIXED, int BS>
 void launch_batch_stage_p(const BatchInst *inst, const Tile *cell_tiles, int n_ct, const Tile *face_tiles, int n_ft,
                           int stage, const BatchCfg &c) {
   const int gr = c.grid_recon > 0 ? c.grid_recon : n_ct, gf = c.grid_face > 0 ? c.grid_face : n_ft,
             gu = c.grid_update > 0 ? c.grid_update : n_ct;
   if (c.ev) cudaEventRecord(c.ev[0], c.stream);
   if (c.eq && c.src)
-    batch_recon_kernel<S, 1, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 1, MIXED, BS>()<<<gr, BS, recon_smem_bytes<S, 1, MIXED>(BS), c.stream>>>(inst, cell_tiles,
+                                                                                                     n_ct, stage);
   else if (c.eq)
-    batch_recon_kernel<S, 1, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, 1, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 1, 0, MIXED, BS>()<<<gr, BS, recon_smem_bytes<S, 1, MIXED>(BS), c.stream>>>(inst, cell_tiles,
+                                                                                                     n_ct, stage);
   else if (c.src)
-    batch_recon_kernel<S, 0, 1, MIXED>()<<<gr, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 1, MIXED, BS>()<<<gr, BS, recon_smem_bytes<S, 0, MIXED>(BS), c.stream>>>(inst, cell_tiles,
+                                                                                                     n_ct, stage);
   else
-    batch_recon_kernel<S, 0, 0, MIXED>()<<<gr, 128, recon_smem_bytes<S, 0, MIXED>(128), c.stream>>>(inst, cell_tiles, n_ct, stage);
+    batch_recon_kernel<S, 0, 0, MIXED, BS>()<<<gr, BS, recon_smem_bytes<S, 0, MIXED>(BS), c.stream>>>(inst, cell_tiles,
+                                                                                                     n_ct, stage);
   if (c.ev) cudaEventRecord(c.ev[1], c.stream);
   if (c.flux == 0) {
     if (c.eq)
-      km_face_flux<S, 0, 1, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+      km_face_flux<S, 0, 1, MIXED, BS><<<gf, BS, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
     else
-      km_face_flux<S, 0, 0, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+      km_face_flux<S, 0, 0, MIXED, BS><<<gf, BS, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
   } else {
     if (c.eq)
-      km_face_flux<S, 1, 1, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+      km_face_flux<S, 1, 1, MIXED, BS><<<gf, BS, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
     else
-      km_face_flux<S, 1, 0, MIXED><<<gf, 128, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
+      km_face_flux<S, 1, 0, MIXED, BS><<<gf, BS, 0, c.stream>>>(inst, face_tiles, n_ft, stage);
   }
   if (c.ev) cudaEventRecord(c.ev[2], c.stream);
-  km_update<S, MIXED><<<gu, 128, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
+  km_update<S, MIXED, BS><<<gu, BS, 0, c.stream>>>(inst, cell_tiles, n_ct, stage);
   if (c.ev) cudaEventRecord(c.ev[3], c.stream);
 }
 
 // Occupancy-limited block counts of the three batch kernels (for the autotuner).
-template <class S, bool MIXED>
+template <class S, bool MIXED, int BS>
 void batch_occupancy_p(int *blocks_per_sm) {
   auto occ = [](const void *k, size_t smem = 0) {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, 128, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, BS, smem);
     return b;
   };
-  blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, MIXED>(), recon_smem_bytes<S, 1, MIXED>(128));
-  blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, MIXED>);
-  blocks_per_sm[2] = occ((const void *)km_update<S, MIXED>);
+  blocks_per_sm[0] = occ((const void *)batch_recon_kernel<S, 1, 1, MIXED, BS>(), recon_smem_bytes<S, 1, MIXED>(BS));
+  blocks_per_sm[1] = occ((const void *)km_face_flux<S, 0, 1, MIXED, BS>);
+  blocks_per_sm[2] = occ((const void *)km_update<S, MIXED, BS>);
 }
 
 // ------------------------------------------------------------ launching
@@ -1831,14 +1842,35 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
 // Instantiation: inst_shape.cu is compiled once per (shape, precision, single
 // solver or batch) so the sixteen kernel sets build in parallel; the shape-level
 // entry points below pick the precision at run time.
+#define ZFVM_DECLARE_SHAPE_BATCH_BS(name, sfx, bs)                                                         \
+  void launch_batch_stage_##name##_##sfx##_b##bs(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, \
+                                                 int n_ft, int stage, const BatchCfg &c);                         \
+  void batch_occupancy_##name##_##sfx##_b##bs(int *blocks_per_sm);
 #define ZFVM_DECLARE_SHAPE_PREC(name, sfx)                                                                \
   void launch_stage_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c);  \
   void launch_export_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, const LaunchCfg &c); \
   void launch_tracer_##name##_##sfx(const DevData &D, const Params &P, StageArgs &a, TracerArgs &ta,      \
                                     const LaunchCfg &c);                                                  \
-  void launch_batch_stage_##name##_##sfx(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, \
-                                         int n_ft, int stage, const BatchCfg &c);                         \
-  void batch_occupancy_##name##_##sfx(int *blocks_per_sm);
+  ZFVM_DECLARE_SHAPE_BATCH_BS(name, sfx, 64)                                                              \
+  ZFVM_DECLARE_SHAPE_BATCH_BS(name, sfx, 128)                                                             \
+  ZFVM_DECLARE_SHAPE_BATCH_BS(name, sfx, 256)                                                             \
+  inline void launch_batch_stage_##name##_##sfx(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft, \
+                                                int n_ft, int stage, const BatchCfg &c) {                 \
+    if (c.block == 64)                                                                                    \
+      launch_batch_stage_##name##_##sfx##_b64(inst, ct, n_ct, ft, n_ft, stage, c);                        \
+    else if (c.block == 256)                                                                              \
+      launch_batch_stage_##name##_##sfx##_b256(inst, ct, n_ct, ft, n_ft, stage, c);                       \
+    else                                                                                                  \
+      launch_batch_stage_##name##_##sfx##_b128(inst, ct, n_ct, ft, n_ft, stage, c);                       \
+  }                                                                                                       \
+  inline void batch_occupancy_##name##_##sfx(int block, int *blocks_per_sm) {                             \
+    if (block == 64)                                                                                      \
+      batch_occupancy_##name##_##sfx##_b64(blocks_per_sm);                                                \
+    else if (block == 256)                                                                                \
+      batch_occupancy_##name##_##sfx##_b256(blocks_per_sm);                                               \
+    else                                                                                                  \
+      batch_occupancy_##name##_##sfx##_b128(blocks_per_sm);                                               \
+  }
 #define ZFVM_DECLARE_SHAPE(name)                                                                          \
   ZFVM_DECLARE_SHAPE_PREC(name, f64)                                                                      \
   ZFVM_DECLARE_SHAPE_PREC(name, mix)                                                                      \
@@ -1859,7 +1891,8 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
             : launch_batch_stage_##name##_f64(inst, ct, n_ct, ft, n_ft, stage, c);                        \
   }                                                                                                       \
   inline void batch_occupancy_##name(const BatchCfg &c, int *blocks_per_sm) {                             \
-    c.mixed ? batch_occupancy_##name##_mix(blocks_per_sm) : batch_occupancy_##name##_f64(blocks_per_sm);  \
+    c.mixed ? batch_occupancy_##name##_mix(c.block, blocks_per_sm)                                        \
+            : batch_occupancy_##name##_f64(c.block, blocks_per_sm);                                       \
   }
 // the single-solver kernels of one shape and precision (the FP64 unit also
 // holds the shape's CFL pass)
@@ -1878,13 +1911,13 @@ void launch_cfl_t(const DevData &D, const Params &P, const double *u, const Laun
   void launch_cfl_##name(const DevData &D, const Params &P, const double *u, const LaunchCfg &c) {          \
     launch_cfl_t<S>(D, P, u, c);                                                                           \
   }
-// the batched (persistent, multi-instance) kernels of one shape and precision
-#define ZFVM_DEFINE_SHAPE_BATCH(name, S, MIXED, sfx)                                                       \
-  void launch_batch_stage_##name##_##sfx(const BatchInst *inst, const Tile *ct, int n_ct, const Tile *ft,  \
-                                         int n_ft, int stage, const BatchCfg &c) {                         \
-    launch_batch_stage_p<S, MIXED>(inst, ct, n_ct, ft, n_ft, stage, c);                                    \
+// the batched (persistent, multi-instance) kernels of one shape, precision and block size
+#define ZFVM_DEFINE_SHAPE_BATCH(name, S, MIXED, sfx, bs)                                                   \
+  void launch_batch_stage_##name##_##sfx##_b##bs(const BatchInst *inst, const Tile *ct, int n_ct,          \
+                                                 const Tile *ft, int n_ft, int stage, const BatchCfg &c) { \
+    launch_batch_stage_p<S, MIXED, bs>(inst, ct, n_ct, ft, n_ft, stage, c);                                \
   }                                                                                                        \
-  void batch_occupancy_##name##_##sfx(int *blocks_per_sm) { batch_occupancy_p<S, MIXED>(blocks_per_sm); }
+  void batch_occupancy_##name##_##sfx##_b##bs(int *blocks_per_sm) { batch_occupancy_p<S, MIXED, bs>(blocks_per_sm); }
 
 ZFVM_DECLARE_SHAPE(s2o3)
 ZFVM_DECLARE_SHAPE(s2o2)

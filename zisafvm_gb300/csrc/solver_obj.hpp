@@ -101,8 +101,10 @@ struct zfvm_solver {
   std::vector<double> poly_host;
   zfvm::DBuf<zfvm::dev::Clock> clock;
   bool has_src = false, has_eq = false, mixed = false;
-  cudaGraphExec_t graph = nullptr;
-  int graph_steps = 0;
+  // captured step loops: `graph` replays graph_steps steps, `graph_tail` the
+  // remainder of a timed step count that is not a multiple of it
+  cudaGraphExec_t graph = nullptr, graph_tail = nullptr;
+  int graph_steps = 0, graph_tail_steps = 0;
   int64_t device_bytes = 0;
   zfvm_solver() = default;
   zfvm_solver(const zfvm_solver &) = delete;
@@ -111,6 +113,7 @@ struct zfvm_solver {
   // ends before the buffers (members, freed after this body) go away.
   ~zfvm_solver() {
     if (graph) cudaGraphExecDestroy(graph);
+    if (graph_tail) cudaGraphExecDestroy(graph_tail);
     if (stream) {
       cudaStreamSynchronize(stream);
       cudaStreamDestroy(stream);
