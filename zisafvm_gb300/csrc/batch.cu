@@ -172,7 +172,15 @@ void rebuild(zfvm_batch *b) {
 void capture_steps(zfvm_batch *b, int steps, cudaGraphExec_t *out) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < steps; ++k) enqueue_batch_step(b);
+  try {
+    for (int k = 0; k < steps; ++k) enqueue_batch_step(b);
+  } catch (...) {
+    // end the capture, so the thread and the stream are usable again
+    cudaGraph_t broken = nullptr;
+    cudaStreamEndCapture(b->stream, &broken);
+    if (broken) cudaGraphDestroy(broken);
+    throw;
+  }
   CK(cudaStreamEndCapture(b->stream, &g));
   CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);

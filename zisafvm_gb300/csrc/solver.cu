@@ -786,7 +786,15 @@ namespace {
 void capture_steps(zfvm_solver *s, int steps, cudaGraphExec_t *out) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-  for (int k = 0; k < steps; ++k) enqueue_step(s);
+  try {
+    for (int k = 0; k < steps; ++k) enqueue_step(s);
+  } catch (...) {
+    // end the capture, so the thread and the stream are usable again
+    cudaGraph_t broken = nullptr;
+    cudaStreamEndCapture(s->stream, &broken);
+    if (broken) cudaGraphDestroy(broken);
+    throw;
+  }
   CK(cudaStreamEndCapture(s->stream, &g));
   CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);
