@@ -382,6 +382,35 @@ struct PolyRecord {
                        EQ = MOM + S::NC, VALID = EQ + 4, SIZE = VALID + 1;
 };
 
+// ------------------------------------------------------------- load paths
+// A kernel's per-cell operands that only the thread of that cell reads (its
+// stencil operator, its quadrature offsets, its slots of the index tables) are
+// read once and bypass L1 (ld.global.nc.L1::no_allocate): the L1 that the
+// shared-memory carve-out leaves then holds the stencil gathers, which
+// neighbouring threads reuse.  Gathered operands that no thread of the running
+// kernel writes take the read-only path (ld.global.nc).  Both leave the L2
+// policy alone: between the stages of a run the operators stay L2-resident
+// when they fit.
+__device__ __forceinline__ float ld_once(const float *p) {
+  float v;
+  asm("ld.global.nc.L1::no_allocate.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ double ld_once(const double *p) {
+  double v;
+  asm("ld.global.nc.L1::no_allocate.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ int ld_once(const int *p) {
+  int v;
+  asm("ld.global.nc.L1::no_allocate.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+template <class T>
+__device__ __forceinline__ T ld_gather(const T *p) {
+  return __ldg(p);
+}
+
 // ------------------------------------------------- FP32 pair ("double-float")
 // Unevaluated sums hi + lo of two FP32 numbers, with the error-free
 // transformations of Knuth (two-sum, TAOCP vol. 2, 4.2.2) and Dekker (two-product,
@@ -478,7 +507,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   const double gamma = P.gamma;
   EqEval ev{gamma, gamma - 1.0, P.inv_gm1};
 
-  const int j0 = d.l2g[i];
+  const int j0 = ld_once(&d.l2g[i]);
   double u0[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) u0[v] = q[v * ld + j0];
@@ -637,10 +666,10 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   DF own_q[NV], own_m1{0.f, 0.f}, own_var{0.f, 0.f}, df_f{0.f, 0.f}, df_kf2{0.f, 0.f}, df_2t{0.f, 0.f};
   if (MIXED && (!EQ || diff_form)) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) own_q[v] = df_of(a.qs[v * ld + j0]);
+    for (int v = 0; v < NV; ++v) own_q[v] = df_of(ld_gather(&a.qs[v * ld + j0]));
     if (diff_form) {
-      own_m1 = df_of(d.m1s[j0]);
-      own_var = df_of(d.vars[j0]);
+      own_m1 = df_of(ld_gather(&d.m1s[j0]));
+      own_var = df_of(ld_gather(&d.vars[j0]));
       df_f = f_split;
       df_kf2 = df_split(eqb.K * (eqb.f * eqb.f));
       df_2t = df_split(2.0 * (eqb.hr - d.phi_m1[j0]));
@@ -650,7 +679,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     if (MIXED && !EQ) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        const float2 x = a.qs[v * ld + j];
+        const float2 x = ld_gather(&a.qs[v * ld + j]);
         dq[v] = R(__fadd_rn(__fsub_rn(x.x, own_q[v].hi), __fsub_rn(x.y, own_q[v].lo)));
       }
     } else if (MIXED && diff_form) {
@@ -659,18 +688,18 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       // dm = <phi>_0 - <phi>_j
       // <phi> may differ by more than a factor of two near the centre of the
       // potential: full two-sum there
-      const DF dm = df_sub(own_m1, df_of(d.m1s[j]));
+      const DF dm = df_sub(own_m1, df_of(ld_gather(&d.m1s[j])));
 #pragma unroll
       for (int v = 1; v < NV - 1; ++v) {
-        const float2 x = a.qs[v * ld + j];
+        const float2 x = ld_gather(&a.qs[v * ld + j]);
         dq[v] = R(__fadd_rn(__fsub_rn(x.x, own_q[v].hi), __fsub_rn(x.y, own_q[v].lo)));
       }
-      dq[0] = R(df_round(df_sub_close(df_sub_close(df_of(a.qs[j]), own_q[0]), df_mul(df_f, dm))));
+      dq[0] = R(df_round(df_sub_close(df_sub_close(df_of(ld_gather(&a.qs[j])), own_q[0]), df_mul(df_f, dm))));
       // 2 (h_r - <phi>_0) + dm with |dm| << |2 (h_r - <phi>_0)|
       const float sh = __fadd_rn(df_2t.hi, dm.hi);
       const DF sum{sh, __fadd_rn(__fsub_rn(dm.hi, __fsub_rn(sh, df_2t.hi)), __fadd_rn(df_2t.lo, dm.lo))};
-      const DF t = df_add(df_mul(dm, sum), df_sub_close(df_of(d.vars[j]), own_var));
-      const DF dE = df_sub_close(df_sub_close(df_of(a.qs[(NV - 1) * ld + j]), own_q[NV - 1]), df_mul(df_kf2, t));
+      const DF t = df_add(df_mul(dm, sum), df_sub_close(df_of(ld_gather(&d.vars[j])), own_var));
+      const DF dE = df_sub_close(df_sub_close(df_of(ld_gather(&a.qs[(NV - 1) * ld + j])), own_q[NV - 1]), df_mul(df_kf2, t));
       dq[NV - 1] = R(df_round(dE));
     } else {
       double dq64[NV];
@@ -703,7 +732,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     // all stencil indices first, as independent loads, parked in the first
     // slot of their own row until the row is computed
 #pragma unroll
-    for (int l = 1; l < S::MAXL; ++l) rows_smem[((l - 1) * NV) * bd + tid] = __int_as_float(d.l2g[l * ld + i]);
+    for (int l = 1; l < S::MAXL; ++l) rows_smem[((l - 1) * NV) * bd + tid] = __int_as_float(ld_once(&d.l2g[l * ld + i]));
 #pragma unroll 2
     for (int l = 1; l < S::MAXL; ++l) {
       const int j = __float_as_int(rows_smem[((l - 1) * NV) * bd + tid]);
@@ -721,7 +750,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     for (int r = 0; r < S::R0; ++r) {
 #pragma unroll
       for (int c = 0; c < S::C0; ++c) {
-        const R pc = R(d.pinv32[(c * S::R0 + r) * ld + i]);
+        const R pc = R(ld_once(&d.pinv32[(c * S::R0 + r) * ld + i]));
 #pragma unroll
         for (int v = 0; v < NV; ++v) b0[c][v] += pc * rows_smem[(r * NV + v) * bd + tid];
       }
@@ -736,7 +765,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
         for (int v = 0; v < NV; ++v) dq[v] = l > 0 ? rows_smem[((l - 1) * NV + v) * bd + tid] : R(0);
 #pragma unroll
         for (int c = 0; c < S::CB; ++c) {
-          const R pc = R(d.pinv32[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i]);
+          const R pc = R(ld_once(&d.pinv32[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i]));
 #pragma unroll
           for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
         }
@@ -747,7 +776,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     // cost a block per SM, which costs more than the wait)
     int jc[S::R0], jb[S::NB * S::RB];
 #pragma unroll
-    for (int r = 0; r < S::R0; ++r) jc[r] = d.l2g[(r + 1) * ld + i];
+    for (int r = 0; r < S::R0; ++r) jc[r] = ld_once(&d.l2g[(r + 1) * ld + i]);
 #pragma unroll
     for (int kr = 0; kr < S::NB * S::RB; ++kr) jb[kr] = d.l2g[d.bloc[kr * ld + i] * ld + i];
 #pragma unroll 2
@@ -756,7 +785,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       row_diff(jc[r], dq);
 #pragma unroll
       for (int c = 0; c < S::C0; ++c) {
-        const R pc = R(d.pinv32[(c * S::R0 + r) * ld + i]);
+        const R pc = R(ld_once(&d.pinv32[(c * S::R0 + r) * ld + i]));
 #pragma unroll
         for (int v = 0; v < NV; ++v) b0[c][v] += pc * dq[v];
       }
@@ -769,7 +798,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
         row_diff(jb[k * S::RB + r], dq);
 #pragma unroll
         for (int c = 0; c < S::CB; ++c) {
-          const R pc = R(d.pinv32[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i]);
+          const R pc = R(ld_once(&d.pinv32[(S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i]));
 #pragma unroll
           for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
         }
@@ -779,10 +808,10 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
 #pragma unroll 2
     for (int r = 0; r < S::R0; ++r) {
       R dq[NV];
-      row_diff(d.l2g[(r + 1) * ld + i], dq);
+      row_diff(ld_once(&d.l2g[(r + 1) * ld + i]), dq);
 #pragma unroll
       for (int c = 0; c < S::C0; ++c) {
-        const R pc = MIXED ? R(d.pinv32[(c * S::R0 + r) * ld + i]) : R(d.pinv[(c * S::R0 + r) * ld + i]);
+        const R pc = MIXED ? R(ld_once(&d.pinv32[(c * S::R0 + r) * ld + i])) : R(ld_once(&d.pinv[(c * S::R0 + r) * ld + i]));
 #pragma unroll
         for (int v = 0; v < NV; ++v) b0[c][v] += pc * dq[v];
       }
@@ -793,11 +822,11 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       for (int r = 0; r < S::RB; ++r) {
         const int l = d.bloc[(k * S::RB + r) * ld + i];
         R dq[NV];
-        row_diff(d.l2g[l * ld + i], dq);
+        row_diff(ld_once(&d.l2g[l * ld + i]), dq);
 #pragma unroll
         for (int c = 0; c < S::CB; ++c) {
           const int pi = (S::R0 * S::C0 + (k * S::CB + c) * S::RB + r) * ld + i;
-          const R pc = MIXED ? R(d.pinv32[pi]) : R(d.pinv[pi]);
+          const R pc = MIXED ? R(ld_once(&d.pinv32[pi])) : R(ld_once(&d.pinv[pi]));
 #pragma unroll
           for (int v = 0; v < NV; ++v) bb[k][c][v] += pc * dq[v];
         }
@@ -870,7 +899,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     il = d.inv_len[i];
   }
 #pragma unroll
-  for (int c = 0; c < NC; ++c) C[c] = MIXED ? R(d.mom32[c * ld + i]) : R(d.mom[c * ld + i]);
+  for (int c = 0; c < NC; ++c) C[c] = MIXED ? R(ld_once(&d.mom32[c * ld + i])) : R(d.mom[c * ld + i]);
   if constexpr (EXPORT) {
     using PR = PolyRecord<S>;
     double *o = a.poly_out;
@@ -927,7 +956,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       if (MIXED) {
         R X[ND];
 #pragma unroll
-        for (int k = 0; k < ND; ++k) X[k] = R(d.xfq32[((f * S::NQF + qq) * ND + k) * ld + i]);
+        for (int k = 0; k < ND; ++k) X[k] = R(ld_once(&d.xfq32[((f * S::NQF + qq) * ND + k) * ld + i]));
         poly_X(X, pv);
       } else {
         double x[ND];
@@ -976,8 +1005,8 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
       R X[ND], wg[ND], pv[NV];
 #pragma unroll
       for (int k = 0; k < ND; ++k) {
-        X[k] = R(d.xcq32[(qq * ND + k) * ld + i]);
-        wg[k] = R(d.wg32[(qq * ND + k) * ld + i]);
+        X[k] = R(ld_once(&d.xcq32[(qq * ND + k) * ld + i]));
+        wg[k] = R(ld_once(&d.wg32[(qq * ND + k) * ld + i]));
         G[k] += wg[k];
       }
       poly_X(X, pv);
