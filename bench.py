@@ -626,11 +626,11 @@ def run_ensemble(args, rank, world, local, pg) -> dict:
     total_cells = sum(m.n_cells for _, m, _, _ in inst)
     stages = 3
     batch = z.Batch(n_inst)
-    solvers = []
+    solvers, slots = [], []
     for raw, mesh, scheme, u0 in inst:
         s = z.Solver(mesh, scheme)
         s.set_state(u0)
-        batch.add(s, n_steps=1 << 40)
+        slots.append(batch.add(s, n_steps=1 << 40))
         solvers.append(s)
     t_tune = time.perf_counter()
     batch.autotune(trial_steps=4)
@@ -656,20 +656,17 @@ def run_ensemble(args, rank, world, local, pg) -> dict:
     tuned = batch.tuned_shapes() if hasattr(batch, "tuned_shapes") else None
 
     # end to end: every step uploads all states from pinned host memory, advances
-    # the batch one step and reads every state back
-    hosts = [pinned((m.n_cells, 5)) for _, m, _, _ in inst]
-    for h, s in zip(hosts, solvers):
-        s.get_state(out=h)
+    # the batch one step and reads every state back (Batch.step_host: one host
+    # round trip for the whole batch)
+    hosts = {slot: pinned((m.n_cells, 5)) for slot, (_, m, _, _) in zip(slots, inst)}
+    for slot, s in zip(slots, solvers):
+        s.get_state(out=hosts[slot])
     e2e_steps = max(3, min(args.steps, 16))
     if pg:
         pg.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        for h, s in zip(hosts, solvers):
-            s.set_state(h)
-        batch.advance(1)
-        for h, s in zip(hosts, solvers):
-            s.get_state(out=h)
+        batch.step_host(hosts, hosts, 1)
     e2e_s = max_over_ranks(pg, time.perf_counter() - t0)
     io_bytes = total_cells * 5 * 8
     launches = 1 + stages * 3   # clock + three persistent kernels per stage, one group
@@ -722,7 +719,8 @@ def run_ensemble(args, rank, world, local, pg) -> dict:
         "cells_max": sizes[-1], "setup_s": t_setup, "autotune_s": t_tune, "launch_shapes": tuned,
         "e2e": {"value": world * total_cells * stages * e2e_steps / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes,
-                "path": "set_state of every slot / Batch.advance(1) / get_state of every slot, pinned buffers"},
+                "path": "Batch.step_host: every slot's state in from pinned host memory, one batched step, "
+                        "every state out, one host synchronisation"},
         "roofline": roof, "gpu_launches": launches * args.steps, "clocks": clk.summary(),
         "fp64": {"value": v64, "ms_per_step": ms64 / k64, "form": "plain FP64, one solve at a time",
                  "steps_per_instance": k64},

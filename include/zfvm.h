@@ -365,6 +365,18 @@ int zfvm_batch_add(zfvm_batch *b, zfvm_solver *s, int64_t n_steps, double t_end,
 int zfvm_batch_remove(zfvm_batch *b, int32_t slot);
 /* Replay up to max_steps batched steps; returns the number of slots still running. */
 int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_running);
+/* The batch form of zfvm_step_host, with one host synchronisation for the
+ * whole batch: each slot k with states_in[k] non-null takes that state
+ * (n_cells x 5 AoS doubles) at the time its clock holds, the batch advances up
+ * to max_steps steps (zfvm_batch_advance), and each slot k with states_out[k]
+ * non-null is read back into it (states_out[k] may be states_in[k]).  Both
+ * arrays are indexed by slot, max_slots long, and may be null.  Every slot's
+ * open step is closed before the new states land (a rejected one put back), as
+ * zfvm_batch_remove does; advected variables keep their device values.  Host
+ * buffers in page-locked memory let the copies run asynchronously.  No
+ * counterpart in the reference. */
+int zfvm_batch_step_host(zfvm_batch *b, const double *const *states_in, double *const *states_out,
+                         int32_t max_steps, int32_t *n_running);
 int zfvm_batch_advance_timed(zfvm_batch *b, int32_t n_steps, float *ms);
 /* Pick the persistent grid sizes of each group's kernels by timing candidates. */
 int zfvm_batch_autotune(zfvm_batch *b, int32_t trial_steps, float *best_ms);

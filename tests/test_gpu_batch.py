@@ -205,3 +205,47 @@ def test_batch_advance_takes_exactly_the_steps_asked(zlib):
         assert b.status(slot)["steps"] == total
     b.advance_timed(13)
     assert b.status(slot)["steps"] == total + 13
+
+
+@pytest.mark.parametrize("precision", [z.FP64, z.MIXED])
+def test_batch_step_host_matches_device_resident_steps(zlib, precision):
+    """Batch.step_host (every slot's state in, one batched step, every state
+    out, one host synchronisation) steps what a batch that keeps its states on
+    the device steps: the states pass through the host in FP64, the FP32 pairs
+    and the next step's CFL minimum are formed from them as the update forms
+    them, so the states agree bit for bit, and the clocks count the same time
+    and steps."""
+    probs = [polytrope_2d(n_rings=r, amplitude=a, seed=r, precision=precision) for r, a in ((14, 1e-2), (22, 1e-4))]
+    raw, mesh, scheme, u0 = vortex_2d(n=16, halo=3)
+    scheme.precision = precision
+    probs.append((raw, mesh, scheme, u0))
+
+    def make():
+        b = z.Batch(4)
+        solvers, slots = [], []
+        for raw, mesh, scheme, u0 in probs:
+            s = z.Solver(mesh, scheme)
+            s.set_state(u0)
+            solvers.append(s)
+            slots.append(b.add(s, n_steps=1000))
+        return b, solvers, slots
+
+    b1, s1, k1 = make()
+    b1.advance(5)
+    b2, s2, k2 = make()
+    hosts = {k: u0.copy() for k, (_, _, _, u0) in zip(k2, probs)}
+    for _ in range(5):
+        assert b2.step_host(hosts, hosts, 1) == len(probs)
+    for j in range(len(probs)):
+        st1, st2 = b1.status(k1[j]), b2.status(k2[j])
+        assert st1["steps"] == st2["steps"] == 5 and st1["t"] == st2["t"]
+        u1, _ = s1[j].get_state()
+        assert np.array_equal(hosts[k2[j]], u1), np.abs(hosts[k2[j]] - u1).max()
+    # reading back only, and taking a state in without reading it back
+    out = {k2[0]: np.zeros_like(hosts[k2[0]])}
+    b2.step_host(None, out, 1)
+    b1.advance(1)
+    assert np.array_equal(out[k2[0]], s1[0].get_state()[0])
+    b2.step_host({k2[1]: hosts[k2[1]]}, None, 1)
+    with pytest.raises(z.ZfvmError):
+        b2.step_host({k2[0]: np.zeros((3, 5))}, None, 1)

@@ -140,6 +140,7 @@ def load_library() -> C.CDLL:
         "zfvm_batch_add": [vp, vp, i64, C.c_double, C.POINTER(i32)],
         "zfvm_batch_remove": [vp, i32],
         "zfvm_batch_advance": [vp, i32, C.POINTER(i32)],
+        "zfvm_batch_step_host": [vp, pp, pp, i32, C.POINTER(i32)],
         "zfvm_batch_advance_timed": [vp, i32, C.POINTER(C.c_float)],
         "zfvm_batch_autotune": [vp, i32, C.POINTER(C.c_float)],
         "zfvm_batch_kernel_times": [vp, i32, C.POINTER(C.c_float)],
@@ -606,6 +607,7 @@ class Batch:
         _check(load_library().zfvm_batch_create(max_slots, C.byref(h)))
         self._h = h
         self._members = {}
+        self._max_slots = max_slots
 
     def close(self):
         if getattr(self, "_h", None) is not None and _LIB is not None:
@@ -634,6 +636,31 @@ class Batch:
         ms = C.c_float()
         _check(load_library().zfvm_batch_advance_timed(self._h, n_steps, C.byref(ms)))
         return float(ms.value)
+
+    def step_host(self, states_in: dict | None, states_out: dict | None, max_steps: int = 1) -> int:
+        """One host round trip for the whole batch (zfvm_batch_step_host): the
+        slots in `states_in` ({slot: n_cells x 5 float64 array}) take those
+        states, the batch advances up to max_steps steps, and the slots in
+        `states_out` are read back into their arrays (which may be the input
+        arrays; page-locked arrays make the copies asynchronous).  Returns the
+        number of slots still running."""
+        def table(states, writable):
+            if states is None:
+                return None
+            arr = (C.c_void_p * self._max_slots)()
+            for slot, a in states.items():
+                if slot not in self._members:
+                    raise ZfvmError(1, f"slot {slot} holds no solver")
+                want = (self._members[slot].mesh.n_cells, 5)
+                if a.dtype != np.float64 or not a.flags.c_contiguous or a.shape != want or (
+                        writable and not a.flags.writeable):
+                    raise ZfvmError(1, f"slot {slot}: need a C-contiguous float64 array of shape {want}")
+                arr[slot] = a.ctypes.data
+            return arr
+        tin, tout = table(states_in, False), table(states_out, True)
+        n = C.c_int32()
+        _check(load_library().zfvm_batch_step_host(self._h, tin, tout, max_steps, C.byref(n)))
+        return n.value
 
     def autotune(self, trial_steps: int = 4) -> float:
         ms = C.c_float()

@@ -31,6 +31,84 @@ __global__ void k_clock_multi(Clock *const *clocks, const double *cfl, int n, in
   if (k < n) clock_step(clocks[k], cfl[k], mode);
 }
 
+// Host states of a batch round trip (zfvm_batch_step_host): per group
+// instance, the staging rows and the buffers the layout kernels fill.
+struct SlotIO {
+  double *aos;       // n_cells x 5 rows (the solver's staging buffer)
+  float2 *pairs;     // mixed form: FP32 pairs of the step and the stage state, else null
+  const int *src;    // periodic source of every cell (ghost rows report their source)
+  int slot, nv;
+};
+
+// Close every slot's open step (clock_step mode 1) and, for slots whose state
+// is about to be replaced, restart the CFL minimum.  clock_slot maps clock
+// index -> batch slot; mask[slot] bit 0: a new state comes in.
+__global__ void k_clock_close_multi(Clock *const *clocks, const double *cfl, const int *clock_slot,
+                                    const int *mask, int n) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  clock_step(clocks[k], cfl[k], 1);
+  if (mask[clock_slot[k]] & 1) clocks[k]->cfl_min = 0x7ff0000000000000ull;
+}
+
+// New states in, one block per cell tile of the slots that take one: AoS rows
+// -> the step and stage states (SoA) and, in the mixed form, their FP32 pairs
+// (as k_state_in); the CFL candidates of the new state go to the slot's clock
+// (as k_cfl).
+template <int NV>
+__global__ void km_io_state_in(const BatchInst *__restrict__ inst, const SlotIO *__restrict__ io,
+                               const Tile *__restrict__ tiles, const int *mask, int mixed) {
+  const Tile tl = tiles[blockIdx.x];
+  const SlotIO &o = io[tl.slot];
+  if (!(mask[o.slot] & 1)) return;  // block-uniform: a tile belongs to one slot
+  const BatchInst &I = inst[tl.slot];
+  const DevData &d = I.d;
+  const int i = tl.begin + threadIdx.x, ld = d.ld;
+  double cand = INFINITY;
+  if (i < d.n_cells) {
+    double w[NV];
+    float w32[NV];
+    const size_t half = (size_t)NV * ld;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const double x = o.aos[(size_t)i * 5 + (v == NV - 1 ? 4 : v)];
+      w[v] = x;
+      w32[v] = __double2float_rn(x);
+      I.a[0].u0[(size_t)v * ld + i] = x;
+      I.a[0].ux[(size_t)v * ld + i] = x;
+      if (o.pairs) {
+        const float2 pr = make_float2(w32[v], __double2float_rn(x - (double)w32[v]));
+        o.pairs[(size_t)v * ld + i] = pr;
+        o.pairs[half + (size_t)v * ld + i] = pr;
+      }
+    }
+    if (d.flags[i] & (kInterior | kFrozen))
+      cand = mixed ? double(cfl_candidate_f32<NV>(w32, I.P.gamma32, float(d.r_eff[i])))
+                   : cfl_candidate<NV>(w, I.P.gamma, d.r_eff[i]);
+  }
+  block_min_to_clock(cand, d.clock);
+}
+
+// States out, one block per cell tile of the slots read back: the step state
+// (SoA) -> AoS rows, ghost rows from their periodic source (as k_soa_to_aos).
+template <int NV>
+__global__ void km_io_state_out(const BatchInst *__restrict__ inst, const SlotIO *__restrict__ io,
+                                const Tile *__restrict__ tiles, const int *mask) {
+  const Tile tl = tiles[blockIdx.x];
+  const SlotIO &o = io[tl.slot];
+  if (!(mask[o.slot] & 2)) return;
+  const BatchInst &I = inst[tl.slot];
+  const int i = tl.begin + threadIdx.x, ld = I.d.ld;
+  if (i >= I.d.n_cells) return;
+  const int j = o.src[i];
+  double r[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int v = 0; v < NV - 1; ++v) r[v] = I.a[0].u0[(size_t)v * ld + j];
+  r[4] = I.a[0].u0[(size_t)(NV - 1) * ld + j];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) o.aos[(size_t)i * 5 + v] = r[v];
+}
+
 // number of slots still running
 __global__ void k_count_running(Clock *const *clocks, int n, int *running) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,6 +126,7 @@ struct Group {
   GroupKey key;
   std::vector<int> slots;
   DBuf<BatchInst> inst;
+  DBuf<SlotIO> io;
   DBuf<Tile> cell_tiles, face_tiles;
   int n_ct = 0, n_ft = 0;
   int block = 128;          // threads per block = cells or faces per tile
@@ -64,6 +143,9 @@ struct zfvm_batch {
   std::map<GroupKey, std::unique_ptr<Group>> groups;
   DBuf<Clock *> clock_ptrs;
   DBuf<double> cfls;
+  DBuf<int> clock_slot;    // clock index -> slot
+  DBuf<int> io_mask;       // per slot, for a host round trip: bit 0 state in, bit 1 state out
+  std::vector<int> io_mask_host;
   DBuf<int> running;
   int n_clock = 0;
   // captured step loops: `graph` replays graph_steps steps, `graph_tail` the
@@ -128,6 +210,7 @@ void rebuild(zfvm_batch *b) {
   for (auto &kv : b->groups) kv.second->slots.clear();
   std::vector<Clock *> clocks;
   std::vector<double> cfls;
+  std::vector<int> clock_slot;
   for (int k = 0; k < (int)b->slots.size(); ++k) {
     zfvm_solver *s = b->slots[k];
     if (!s) continue;
@@ -141,13 +224,16 @@ void rebuild(zfvm_batch *b) {
     g->slots.push_back(k);
     clocks.push_back(s->clock.p);
     cfls.push_back(s->P.cfl);
+    clock_slot.push_back(k);
   }
   for (auto &kv : b->groups) {
     Group &g = *kv.second;
     std::vector<BatchInst> inst;
+    std::vector<SlotIO> io;
     std::vector<Tile> ct, ft;
     for (size_t j = 0; j < g.slots.size(); ++j) {
       zfvm_solver *s = b->slots[g.slots[j]];
+      io.push_back(SlotIO{s->aos.p, s->qsplit.p, s->src_map.p, g.slots[j], s->nv});
       BatchInst I{};
       I.d = s->D;
       I.P = s->P;
@@ -157,6 +243,7 @@ void rebuild(zfvm_batch *b) {
       for (int e = 0; e < s->n_edges; e += g.block) ft.push_back(Tile{(int)j, e});
     }
     g.inst.upload(inst);
+    g.io.upload(io);
     g.cell_tiles.upload(ct);
     g.face_tiles.upload(ft);
     g.n_ct = (int)ct.size();
@@ -164,6 +251,7 @@ void rebuild(zfvm_batch *b) {
   }
   b->clock_ptrs.upload(clocks);
   b->cfls.upload(cfls);
+  b->clock_slot.upload(clock_slot);
   b->n_clock = (int)clocks.size();
   drop_graphs(b);
   b->dirty = false;
@@ -315,6 +403,80 @@ extern "C" int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_r
   wait_for_slots(b);
   launch_graphs(b, max_steps, chunk);
   int r = running_count(b);
+  if (n_running) *n_running = r;
+  return ZFVM_OK;
+  BATCH_GUARD_END
+}
+
+// The batch form of zfvm_step_host: one host round trip for every slot.
+// Slots with a state in states_in[slot] take it at the time their clock holds
+// (the open step of every slot is closed first, a rejected one put back, as
+// zfvm_batch_remove does), the batch advances up to max_steps steps, and slots
+// with a buffer in states_out[slot] are read back.  Copies run on the batch
+// stream, one per slot and direction; the layout and CFL work is one launch
+// per kernel group and direction; the host synchronises once, at the end.
+extern "C" int zfvm_batch_step_host(zfvm_batch *b, const double *const *states_in, double *const *states_out,
+                                    int32_t max_steps, int32_t *n_running) {
+  if (!b || max_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
+  BATCH_GUARD_BEGIN
+  const int chunk = prepare_graphs(b, max_steps, 8);
+  wait_for_slots(b);
+  const int n_slots = (int)b->slots.size();
+  std::vector<int> &mask = b->io_mask_host;
+  mask.assign(n_slots, 0);
+  bool any_in = false, any_out = false;
+  for (int k = 0; k < n_slots; ++k) {
+    if (!b->slots[k]) continue;
+    if (states_in && states_in[k]) mask[k] |= 1, any_in = true;
+    if (states_out && states_out[k]) mask[k] |= 2, any_out = true;
+  }
+  if ((any_in || any_out) && b->n_clock) {
+    if (b->io_mask.n < (size_t)n_slots) b->io_mask.alloc(n_slots);
+    CK(cudaMemcpyAsync(b->io_mask.p, mask.data(), n_slots * sizeof(int), cudaMemcpyHostToDevice, b->stream));
+  }
+  if (any_in && b->n_clock) {
+    k_clock_close_multi<<<(b->n_clock + 127) / 128, 128, 0, b->stream>>>(b->clock_ptrs.p, b->cfls.p,
+                                                                          b->clock_slot.p, b->io_mask.p, b->n_clock);
+    CK(cudaGetLastError());
+    for (zfvm_solver *s : b->slots)
+      if (s && s->uprev.p) solver_restore_on(s, b->stream);
+    for (int k = 0; k < n_slots; ++k)
+      if (mask[k] & 1) {
+        zfvm_solver *s = b->slots[k];
+        CK(cudaMemcpyAsync(s->aos.p, states_in[k], (size_t)s->n_cells * 5 * sizeof(double), cudaMemcpyHostToDevice,
+                           b->stream));
+      }
+    for (auto &kv : b->groups) {
+      Group &g = *kv.second;
+      if (g.n_ct == 0) continue;
+      if (g.key.shape >= 2)
+        km_io_state_in<5><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p,
+                                                              g.key.mixed);
+      else
+        km_io_state_in<4><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p,
+                                                              g.key.mixed);
+      CK(cudaGetLastError());
+    }
+  }
+  launch_graphs(b, max_steps, chunk);
+  if (any_out) {
+    for (auto &kv : b->groups) {
+      Group &g = *kv.second;
+      if (g.n_ct == 0) continue;
+      if (g.key.shape >= 2)
+        km_io_state_out<5><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p);
+      else
+        km_io_state_out<4><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p);
+      CK(cudaGetLastError());
+    }
+    for (int k = 0; k < n_slots; ++k)
+      if (mask[k] & 2) {
+        zfvm_solver *s = b->slots[k];
+        CK(cudaMemcpyAsync(states_out[k], s->aos.p, (size_t)s->n_cells * 5 * sizeof(double),
+                           cudaMemcpyDeviceToHost, b->stream));
+      }
+  }
+  const int r = running_count(b);
   if (n_running) *n_running = r;
   return ZFVM_OK;
   BATCH_GUARD_END
