@@ -132,7 +132,24 @@ struct Group {
   int block = 128;          // threads per block = cells or faces per tile
   int grid[3] = {0, 0, 0};  // persistent grid of the three kernels (0: one block per tile)
   bool tuned = false;
+  // host round trips run the batch in parts (consecutive slot ranges):
+  // part p's cell and face tiles are [part_ct[p], part_ct[p + 1]) and
+  // [part_ft[p], part_ft[p + 1])
+  std::vector<int> part_ct, part_ft;
 };
+
+// One part of a pipelined host round trip: its slot and clock ranges, stream,
+// completion event and step graphs.
+struct Part {
+  int slot_lo = 0, slot_hi = 0, clk_lo = 0, clk_hi = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  cudaGraphExec_t graph = nullptr, graph_tail = nullptr;
+  int graph_steps = 0, graph_tail_steps = 0;
+};
+// parts of a pipelined host round trip: the copies of one part overlap the
+// steps of the others
+constexpr int kIoParts = 4;
 
 }  // namespace
 
@@ -152,13 +169,22 @@ struct zfvm_batch {
   // remainder of a step count that is not a multiple of it
   cudaGraphExec_t graph = nullptr, graph_tail = nullptr;
   int graph_steps = 0, graph_tail_steps = 0;
+  std::vector<Part> parts;  // slot ranges of a pipelined host round trip (rebuild)
+  std::vector<cudaStream_t> part_streams;
+  std::vector<cudaEvent_t> part_events;
+  cudaEvent_t ev_fork = nullptr;
   bool dirty = true;
   int sms = 0;
 };
 
 namespace {
 
-void launch_group_stage(zfvm_batch *b, Group &g, int stage, cudaEvent_t *ev = nullptr) {
+// One RK stage of group g over its tiles of part `part` (all tiles when part < 0).
+void launch_group_stage(zfvm_batch *b, Group &g, int stage, cudaEvent_t *ev = nullptr, int part = -1,
+                        cudaStream_t stream = nullptr) {
+  const int c0 = part < 0 ? 0 : g.part_ct[part], c1 = part < 0 ? g.n_ct : g.part_ct[part + 1];
+  const int f0 = part < 0 ? 0 : g.part_ft[part], f1 = part < 0 ? g.n_ft : g.part_ft[part + 1];
+  if (c1 <= c0) return;
   BatchCfg c;
   c.ev = ev;
   c.eq = g.key.eq;
@@ -169,32 +195,42 @@ void launch_group_stage(zfvm_batch *b, Group &g, int stage, cudaEvent_t *ev = nu
   c.grid_recon = g.grid[0];
   c.grid_face = g.grid[1];
   c.grid_update = g.grid[2];
-  c.stream = b->stream;
+  c.stream = stream ? stream : b->stream;
+  const Tile *ct = g.cell_tiles.p + c0, *ft = g.face_tiles.p + f0;
+  const int nc = c1 - c0, nf = f1 - f0;
   switch (g.key.shape) {
-    case 0: launch_batch_stage_s2o3(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
-    case 1: launch_batch_stage_s2o2(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
-    case 2: launch_batch_stage_s3o3(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
-    case 3: launch_batch_stage_s3o2(g.inst.p, g.cell_tiles.p, g.n_ct, g.face_tiles.p, g.n_ft, stage, c); break;
+    case 0: launch_batch_stage_s2o3(g.inst.p, ct, nc, ft, nf, stage, c); break;
+    case 1: launch_batch_stage_s2o2(g.inst.p, ct, nc, ft, nf, stage, c); break;
+    case 2: launch_batch_stage_s3o3(g.inst.p, ct, nc, ft, nf, stage, c); break;
+    case 3: launch_batch_stage_s3o2(g.inst.p, ct, nc, ft, nf, stage, c); break;
   }
   CK(cudaGetLastError());
 }
 
-void enqueue_batch_step(zfvm_batch *b) {
+// One batched step of every slot, or of the slots of part `part` on its stream.
+void enqueue_batch_step(zfvm_batch *b, int part = -1) {
   if (b->n_clock == 0) return;
-  k_clock_multi<<<(b->n_clock + 127) / 128, 128, 0, b->stream>>>(b->clock_ptrs.p, b->cfls.p, b->n_clock, 0);
+  const Part *pt = part < 0 ? nullptr : &b->parts[part];
+  const int k0 = pt ? pt->clk_lo : 0, k1 = pt ? pt->clk_hi : b->n_clock;
+  const int s0 = pt ? pt->slot_lo : 0, s1 = pt ? pt->slot_hi : (int)b->slots.size();
+  cudaStream_t stream = pt ? pt->stream : b->stream;
+  if (k1 <= k0) return;
+  k_clock_multi<<<(k1 - k0 + 127) / 128, 128, 0, stream>>>(b->clock_ptrs.p + k0, b->cfls.p + k0, k1 - k0, 0);
   CK(cudaGetLastError());
   // slots with step rejection put back the start of a rejected step
-  for (zfvm_solver *s : b->slots)
-    if (s && s->uprev.p) solver_restore_on(s, b->stream);
+  for (int k = s0; k < s1; ++k)
+    if (b->slots[k] && b->slots[k]->uprev.p) solver_restore_on(b->slots[k], stream);
   int stages = 0;
   for (auto &kv : b->groups) stages = std::max(stages, kv.second->key.stages);
   for (int st = 0; st < stages; ++st) {
     for (auto &kv : b->groups)
-      if (kv.second->n_ct > 0 && st < kv.second->key.stages) launch_group_stage(b, *kv.second, st);
+      if (kv.second->n_ct > 0 && st < kv.second->key.stages) launch_group_stage(b, *kv.second, st, nullptr, part, stream);
     // advected variables: the slot's own three kernels after the stage, which
     // read the stage's face states before the next stage overwrites them
-    for (zfvm_solver *s : b->slots)
-      if (s && s->na && st < s->P.n_stages) solver_tracers_on(s, st, b->stream);
+    for (int k = s0; k < s1; ++k) {
+      zfvm_solver *s = b->slots[k];
+      if (s && s->na && st < s->P.n_stages) solver_tracers_on(s, st, stream);
+    }
   }
 }
 
@@ -203,11 +239,44 @@ void drop_graphs(zfvm_batch *b) {
   if (b->graph_tail) cudaGraphExecDestroy(b->graph_tail);
   b->graph = b->graph_tail = nullptr;
   b->graph_steps = b->graph_tail_steps = 0;
+  for (Part &pt : b->parts) {
+    if (pt.graph) cudaGraphExecDestroy(pt.graph);
+    if (pt.graph_tail) cudaGraphExecDestroy(pt.graph_tail);
+    pt.graph = pt.graph_tail = nullptr;
+    pt.graph_steps = pt.graph_tail_steps = 0;
+  }
 }
 
 // Rebuild the device tables of every group from the current slots.
 void rebuild(zfvm_batch *b) {
+  drop_graphs(b);
   for (auto &kv : b->groups) kv.second->slots.clear();
+  // parts: consecutive slot ranges of about equal cell counts
+  {
+    int64_t total = 0;
+    int active = 0;
+    for (zfvm_solver *s : b->slots)
+      if (s) total += s->n_cells, ++active;
+    const int np = std::min(kIoParts, active);
+    b->parts.assign(np, Part{});
+    int64_t acc = 0;
+    int q = 0;
+    for (int k = 0; k < (int)b->slots.size() && np > 0; ++k) {
+      if (!b->slots[k]) continue;
+      // part q ends once it holds its share of the cells (every part keeps a slot)
+      if (q < np - 1 && acc >= total * (q + 1) / np) {
+        b->parts[q].slot_hi = k;
+        b->parts[++q].slot_lo = k;
+      }
+      acc += b->slots[k]->n_cells;
+    }
+    if (np > 0) {
+      b->parts[0].slot_lo = 0;
+      b->parts[np - 1].slot_hi = (int)b->slots.size();
+      b->parts.resize(q + 1);
+      b->parts[q].slot_hi = (int)b->slots.size();
+    }
+  }
   std::vector<Clock *> clocks;
   std::vector<double> cfls;
   std::vector<int> clock_slot;
@@ -231,8 +300,11 @@ void rebuild(zfvm_batch *b) {
     std::vector<BatchInst> inst;
     std::vector<SlotIO> io;
     std::vector<Tile> ct, ft;
+    std::vector<int> ct_at(g.slots.size() + 1), ft_at(g.slots.size() + 1);  // first tile of each instance
     for (size_t j = 0; j < g.slots.size(); ++j) {
       zfvm_solver *s = b->slots[g.slots[j]];
+      ct_at[j] = (int)ct.size();
+      ft_at[j] = (int)ft.size();
       io.push_back(SlotIO{s->aos.p, s->qsplit.p, s->src_map.p, g.slots[j], s->nv});
       BatchInst I{};
       I.d = s->D;
@@ -241,6 +313,17 @@ void rebuild(zfvm_batch *b) {
       inst.push_back(I);
       for (int c = 0; c < s->n_cells; c += g.block) ct.push_back(Tile{(int)j, c});
       for (int e = 0; e < s->n_edges; e += g.block) ft.push_back(Tile{(int)j, e});
+    }
+    ct_at[g.slots.size()] = (int)ct.size();
+    ft_at[g.slots.size()] = (int)ft.size();
+    // tile boundaries of the parts: the group's instances are in slot order
+    g.part_ct.assign(b->parts.size() + 1, (int)ct.size());
+    g.part_ft.assign(b->parts.size() + 1, (int)ft.size());
+    for (size_t q = 0; q < b->parts.size(); ++q) {
+      size_t j = 0;
+      while (j < g.slots.size() && g.slots[j] < b->parts[q].slot_lo) ++j;
+      g.part_ct[q] = ct_at[j];
+      g.part_ft[q] = ft_at[j];
     }
     g.inst.upload(inst);
     g.io.upload(io);
@@ -253,25 +336,68 @@ void rebuild(zfvm_batch *b) {
   b->cfls.upload(cfls);
   b->clock_slot.upload(clock_slot);
   b->n_clock = (int)clocks.size();
-  drop_graphs(b);
+  for (Part &pt : b->parts) {
+    pt.clk_lo = (int)(std::lower_bound(clock_slot.begin(), clock_slot.end(), pt.slot_lo) - clock_slot.begin());
+    pt.clk_hi = (int)(std::lower_bound(clock_slot.begin(), clock_slot.end(), pt.slot_hi) - clock_slot.begin());
+  }
   b->dirty = false;
 }
 
-void capture_steps(zfvm_batch *b, int steps, cudaGraphExec_t *out) {
+void capture_steps(zfvm_batch *b, int steps, cudaGraphExec_t *out, int part = -1) {
   cudaGraph_t g;
-  CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaStream_t stream = part < 0 ? b->stream : b->parts[part].stream;
+  CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
   try {
-    for (int k = 0; k < steps; ++k) enqueue_batch_step(b);
+    for (int k = 0; k < steps; ++k) enqueue_batch_step(b, part);
   } catch (...) {
     // end the capture, so the thread and the stream are usable again
     cudaGraph_t broken = nullptr;
-    cudaStreamEndCapture(b->stream, &broken);
+    cudaStreamEndCapture(stream, &broken);
     if (broken) cudaGraphDestroy(broken);
     throw;
   }
-  CK(cudaStreamEndCapture(b->stream, &g));
+  CK(cudaStreamEndCapture(stream, &g));
   CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);
+}
+
+// Streams and graphs of the parts for `n_steps` steps (at most 8 per graph).
+int prepare_part_graphs(zfvm_batch *b, int n_steps) {
+  if (b->dirty) rebuild(b);
+  if (b->part_streams.size() < b->parts.size()) {
+    // earlier parts first: their copies back overlap the later parts' steps
+    int lo = 0, hi = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    while (b->part_streams.size() < b->parts.size()) {
+      const int q = (int)b->part_streams.size();
+      cudaStream_t st = nullptr;
+      cudaEvent_t ev = nullptr;
+      CK(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, std::min(lo, hi + q)));
+      CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      b->part_streams.push_back(st);
+      b->part_events.push_back(ev);
+    }
+  }
+  if (!b->ev_fork) CK(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+  const int chunk = std::min(n_steps, 8), tail = n_steps % chunk;
+  for (size_t q = 0; q < b->parts.size(); ++q) {
+    Part &pt = b->parts[q];
+    pt.stream = b->part_streams[q];
+    pt.done = b->part_events[q];
+    if (!pt.graph || pt.graph_steps != chunk) {
+      if (pt.graph) cudaGraphExecDestroy(pt.graph);
+      pt.graph = nullptr;
+      capture_steps(b, chunk, &pt.graph, (int)q);
+      pt.graph_steps = chunk;
+    }
+    if (tail && (!pt.graph_tail || pt.graph_tail_steps != tail)) {
+      if (pt.graph_tail) cudaGraphExecDestroy(pt.graph_tail);
+      pt.graph_tail = nullptr;
+      capture_steps(b, tail, &pt.graph_tail, (int)q);
+      pt.graph_tail_steps = tail;
+    }
+  }
+  return chunk;
 }
 
 // The graphs that replay exactly n_steps steps: n_steps / chunk replays of a
@@ -357,6 +483,12 @@ extern "C" int zfvm_batch_destroy(zfvm_batch *b) {
     cudaStreamSynchronize(b->stream);
     cudaStreamDestroy(b->stream);
   }
+  for (cudaStream_t st : b->part_streams) {
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+  }
+  for (cudaEvent_t ev : b->part_events) cudaEventDestroy(ev);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
   delete b;
   return ZFVM_OK;
 }
@@ -412,15 +544,16 @@ extern "C" int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_r
 // Slots with a state in states_in[slot] take it at the time their clock holds
 // (the open step of every slot is closed first, a rejected one put back, as
 // zfvm_batch_remove does), the batch advances up to max_steps steps, and slots
-// with a buffer in states_out[slot] are read back.  Copies run on the batch
-// stream, one per slot and direction; the layout and CFL work is one launch
-// per kernel group and direction; the host synchronises once, at the end.
+// with a buffer in states_out[slot] are read back.  The slots run in parts
+// (consecutive slot ranges of about equal cell counts), each on its own stream
+// with its own step graphs, so one part's copies overlap the other parts'
+// steps; the layout and CFL work is one launch per part, kernel group and
+// direction.  The host synchronises once, at the end.
 extern "C" int zfvm_batch_step_host(zfvm_batch *b, const double *const *states_in, double *const *states_out,
                                     int32_t max_steps, int32_t *n_running) {
   if (!b || max_steps <= 0) return fail(ZFVM_EINVAL, "bad argument");
   BATCH_GUARD_BEGIN
-  const int chunk = prepare_graphs(b, max_steps, 8);
-  wait_for_slots(b);
+  if (b->dirty) rebuild(b);
   const int n_slots = (int)b->slots.size();
   std::vector<int> &mask = b->io_mask_host;
   mask.assign(n_slots, 0);
@@ -430,51 +563,67 @@ extern "C" int zfvm_batch_step_host(zfvm_batch *b, const double *const *states_i
     if (states_in && states_in[k]) mask[k] |= 1, any_in = true;
     if (states_out && states_out[k]) mask[k] |= 2, any_out = true;
   }
-  if ((any_in || any_out) && b->n_clock) {
+  if (b->n_clock == 0) {
+    if (n_running) *n_running = 0;
+    return ZFVM_OK;
+  }
+  const int chunk = prepare_part_graphs(b, max_steps);
+  wait_for_slots(b);
+  if (any_in || any_out) {
     if (b->io_mask.n < (size_t)n_slots) b->io_mask.alloc(n_slots);
     CK(cudaMemcpyAsync(b->io_mask.p, mask.data(), n_slots * sizeof(int), cudaMemcpyHostToDevice, b->stream));
   }
-  if (any_in && b->n_clock) {
-    k_clock_close_multi<<<(b->n_clock + 127) / 128, 128, 0, b->stream>>>(b->clock_ptrs.p, b->cfls.p,
-                                                                          b->clock_slot.p, b->io_mask.p, b->n_clock);
-    CK(cudaGetLastError());
-    for (zfvm_solver *s : b->slots)
-      if (s && s->uprev.p) solver_restore_on(s, b->stream);
-    for (int k = 0; k < n_slots; ++k)
-      if (mask[k] & 1) {
-        zfvm_solver *s = b->slots[k];
-        CK(cudaMemcpyAsync(s->aos.p, states_in[k], (size_t)s->n_cells * 5 * sizeof(double), cudaMemcpyHostToDevice,
-                           b->stream));
-      }
-    for (auto &kv : b->groups) {
-      Group &g = *kv.second;
-      if (g.n_ct == 0) continue;
-      if (g.key.shape >= 2)
-        km_io_state_in<5><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p,
-                                                              g.key.mixed);
-      else
-        km_io_state_in<4><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p,
-                                                              g.key.mixed);
+  CK(cudaEventRecord(b->ev_fork, b->stream));
+  for (size_t q = 0; q < b->parts.size(); ++q) {
+    Part &pt = b->parts[q];
+    cudaStream_t st = pt.stream;
+    CK(cudaStreamWaitEvent(st, b->ev_fork, 0));
+    if (any_in && pt.clk_hi > pt.clk_lo) {
+      const int nk = pt.clk_hi - pt.clk_lo;
+      k_clock_close_multi<<<(nk + 127) / 128, 128, 0, st>>>(b->clock_ptrs.p + pt.clk_lo, b->cfls.p + pt.clk_lo,
+                                                            b->clock_slot.p + pt.clk_lo, b->io_mask.p, nk);
       CK(cudaGetLastError());
-    }
-  }
-  launch_graphs(b, max_steps, chunk);
-  if (any_out) {
-    for (auto &kv : b->groups) {
-      Group &g = *kv.second;
-      if (g.n_ct == 0) continue;
-      if (g.key.shape >= 2)
-        km_io_state_out<5><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p);
-      else
-        km_io_state_out<4><<<g.n_ct, g.block, 0, b->stream>>>(g.inst.p, g.io.p, g.cell_tiles.p, b->io_mask.p);
-      CK(cudaGetLastError());
-    }
-    for (int k = 0; k < n_slots; ++k)
-      if (mask[k] & 2) {
-        zfvm_solver *s = b->slots[k];
-        CK(cudaMemcpyAsync(states_out[k], s->aos.p, (size_t)s->n_cells * 5 * sizeof(double),
-                           cudaMemcpyDeviceToHost, b->stream));
+      for (int k = pt.slot_lo; k < pt.slot_hi; ++k)
+        if (b->slots[k] && b->slots[k]->uprev.p) solver_restore_on(b->slots[k], st);
+      for (int k = pt.slot_lo; k < pt.slot_hi; ++k)
+        if (mask[k] & 1) {
+          zfvm_solver *s = b->slots[k];
+          CK(cudaMemcpyAsync(s->aos.p, states_in[k], (size_t)s->n_cells * 5 * sizeof(double),
+                             cudaMemcpyHostToDevice, st));
+        }
+      for (auto &kv : b->groups) {
+        Group &g = *kv.second;
+        const int c0 = g.part_ct[q], nc = g.part_ct[q + 1] - c0;
+        if (nc <= 0) continue;
+        if (g.key.shape >= 2)
+          km_io_state_in<5><<<nc, g.block, 0, st>>>(g.inst.p, g.io.p, g.cell_tiles.p + c0, b->io_mask.p, g.key.mixed);
+        else
+          km_io_state_in<4><<<nc, g.block, 0, st>>>(g.inst.p, g.io.p, g.cell_tiles.p + c0, b->io_mask.p, g.key.mixed);
+        CK(cudaGetLastError());
       }
+    }
+    for (int k = 0; k + chunk <= max_steps; k += chunk) CK(cudaGraphLaunch(pt.graph, st));
+    if (max_steps % chunk) CK(cudaGraphLaunch(pt.graph_tail, st));
+    if (any_out) {
+      for (auto &kv : b->groups) {
+        Group &g = *kv.second;
+        const int c0 = g.part_ct[q], nc = g.part_ct[q + 1] - c0;
+        if (nc <= 0) continue;
+        if (g.key.shape >= 2)
+          km_io_state_out<5><<<nc, g.block, 0, st>>>(g.inst.p, g.io.p, g.cell_tiles.p + c0, b->io_mask.p);
+        else
+          km_io_state_out<4><<<nc, g.block, 0, st>>>(g.inst.p, g.io.p, g.cell_tiles.p + c0, b->io_mask.p);
+        CK(cudaGetLastError());
+      }
+      for (int k = pt.slot_lo; k < pt.slot_hi; ++k)
+        if (mask[k] & 2) {
+          zfvm_solver *s = b->slots[k];
+          CK(cudaMemcpyAsync(states_out[k], s->aos.p, (size_t)s->n_cells * 5 * sizeof(double),
+                             cudaMemcpyDeviceToHost, st));
+        }
+    }
+    CK(cudaEventRecord(pt.done, st));
+    CK(cudaStreamWaitEvent(b->stream, pt.done, 0));
   }
   const int r = running_count(b);
   if (n_running) *n_running = r;

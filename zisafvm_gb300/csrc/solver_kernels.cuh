@@ -508,6 +508,15 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
   EqEval ev{gamma, gamma - 1.0, P.inv_gm1};
 
   const int j0 = ld_once(&d.l2g[i]);
+  if constexpr (kRowsInShared<S, EQ, MIXED>) {
+    // all stencil indices first, as independent loads in flight during the
+    // FP64 work below, parked in the first slot of their own row until the
+    // row is computed
+    extern __shared__ float rows_park[];
+#pragma unroll
+    for (int l = 1; l < S::MAXL; ++l)
+      rows_park[((l - 1) * NV) * blockDim.x + threadIdx.x] = __int_as_float(ld_once(&d.l2g[l * ld + i]));
+  }
   double u0[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) u0[v] = q[v * ld + j0];
@@ -729,10 +738,7 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
     // rows[((l - 1) * NV + v) * blockDim.x + thread], and all fits read it there.
     extern __shared__ float rows_smem[];
     const int bd = blockDim.x, tid = threadIdx.x;
-    // all stencil indices first, as independent loads, parked in the first
-    // slot of their own row until the row is computed
-#pragma unroll
-    for (int l = 1; l < S::MAXL; ++l) rows_smem[((l - 1) * NV) * bd + tid] = __int_as_float(ld_once(&d.l2g[l * ld + i]));
+    // (the stencil indices are parked in the rows' first slots)
 #pragma unroll 2
     for (int l = 1; l < S::MAXL; ++l) {
       const int j = __float_as_int(rows_smem[((l - 1) * NV) * bd + tid]);
@@ -746,7 +752,8 @@ __device__ __forceinline__ void recon_cell(const DevData &d, const Params &P, co
 #pragma unroll
       for (int v = 0; v < NV; ++v) rows_smem[((l - 1) * NV + v) * bd + tid] = dq[v];
     }
-#pragma unroll 2
+    // fully unrolled: the operator's loads of every row can be in flight together
+#pragma unroll
     for (int r = 0; r < S::R0; ++r) {
 #pragma unroll
       for (int c = 0; c < S::C0; ++c) {
