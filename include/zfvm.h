@@ -369,7 +369,8 @@ int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_running);
  * whole batch: each slot k with states_in[k] non-null takes that state
  * (n_cells x 5 AoS doubles) at the time its clock holds, the batch advances up
  * to max_steps steps (zfvm_batch_advance), and each slot k with states_out[k]
- * non-null is read back into it (states_out[k] may be states_in[k]).  Both
+ * non-null is read back into it (states_out[k] may be states_in[k]) once its
+ * last step is closed (a rejected step is put back first).  Both
  * arrays are indexed by slot, max_slots long, and may be null.  Every slot's
  * open step is closed before the new states land (a rejected one put back), as
  * zfvm_batch_remove does; advected variables keep their device values.  Host

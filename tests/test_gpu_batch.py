@@ -249,3 +249,51 @@ def test_batch_step_host_matches_device_resident_steps(zlib, precision):
     b2.step_host({k2[1]: hosts[k2[1]]}, None, 1)
     with pytest.raises(z.ZfvmError):
         b2.step_host({k2[0]: np.zeros((3, 5))}, None, 1)
+
+
+def test_batch_step_host_parts_groups_rejection_tracers(zlib):
+    """The pipelined host round trip over more slots than parts, two kernel
+    groups (FP64 and mixed), a periodic mesh, advected variables and step
+    rejection: the same states, times and accepted steps as a batch that
+    keeps its states on the device, FP64 and mixed bit for bit."""
+    from problems import tracers
+    raw, mesh, scheme, u0 = polytrope_2d(n_rings=16, amplitude=1e-1)
+    rej = z.Scheme(**{**scheme.__dict__, "step_rejection_drho": 2.4e-3, "step_rejection_max_exponent": 6})
+    tr = z.Scheme(**{**scheme.__dict__, "n_avars": 1})
+    mix = z.Scheme(**{**scheme.__dict__, "precision": z.MIXED})
+    mix_rej = z.Scheme(**{**rej.__dict__, "precision": z.MIXED})
+    raw2, mesh2, sch2, u2 = polytrope_2d(n_rings=24, amplitude=1e-3, seed=5)
+    rawv, meshv, schv, uv = vortex_2d(n=16, halo=3)
+    cases = [(mesh, scheme, u0, None), (mesh, rej, u0, None), (mesh2, sch2, u2, None), (mesh, tr, u0, tracers(mesh, u0, 1)),
+             (mesh, mix, u0, None), (mesh, mix_rej, u0, None), (meshv, schv, uv, None),
+             (mesh2, z.Scheme(**{**sch2.__dict__, "precision": z.MIXED}), u2, None)]
+
+    def make():
+        b = z.Batch(len(cases))
+        solvers, slots = [], []
+        for m, sc, u, q in cases:
+            s = z.Solver(m, sc)
+            s.set_state(u)
+            if q is not None:
+                s.set_avars(q)
+            solvers.append(s)
+            slots.append(b.add(s, n_steps=1000))
+        return b, solvers, slots
+
+    n = 10
+    b1, s1, k1 = make()
+    b1.advance(n)
+    b2, s2, k2 = make()
+    hosts = {k: c[2].copy() for k, c in zip(k2, cases)}
+    for _ in range(n):
+        b2.step_host(hosts, hosts, 1)
+    for j, (m, sc, u, q) in enumerate(cases):
+        st1 = b1.status(k1[j])
+        b1.remove(k1[j])  # closes the last step (puts back a rejected one)
+        u1, t1 = s1[j].get_state()
+        st2 = b2.status(k2[j])
+        assert (st1["steps"], st1["t"]) == (st2["steps"], st2["t"]), (j, st1, st2)
+        assert np.array_equal(hosts[k2[j]], u1), (j, np.abs(hosts[k2[j]] - u1).max())
+        if q is not None:
+            assert np.array_equal(s2[j].get_avars(), s1[j].get_avars())
+    assert s1[1].step_rejections() > 0 and s1[5].step_rejections() > 0

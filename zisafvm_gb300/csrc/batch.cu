@@ -544,7 +544,8 @@ extern "C" int zfvm_batch_advance(zfvm_batch *b, int32_t max_steps, int32_t *n_r
 // Slots with a state in states_in[slot] take it at the time their clock holds
 // (the open step of every slot is closed first, a rejected one put back, as
 // zfvm_batch_remove does), the batch advances up to max_steps steps, and slots
-// with a buffer in states_out[slot] are read back.  The slots run in parts
+// with a buffer in states_out[slot] are read back after their last step is
+// closed (a rejected step put back).  The slots run in parts
 // (consecutive slot ranges of about equal cell counts), each on its own stream
 // with its own step graphs, so one part's copies overlap the other parts'
 // steps; the layout and CFL work is one launch per part, kernel group and
@@ -605,6 +606,15 @@ extern "C" int zfvm_batch_step_host(zfvm_batch *b, const double *const *states_i
     for (int k = 0; k + chunk <= max_steps; k += chunk) CK(cudaGraphLaunch(pt.graph, st));
     if (max_steps % chunk) CK(cudaGraphLaunch(pt.graph_tail, st));
     if (any_out) {
+      // close the last step first, so a rejected one is put back before its
+      // state goes out (the next step then opens with the shorter retry step)
+      if (pt.clk_hi > pt.clk_lo) {
+        const int nk = pt.clk_hi - pt.clk_lo;
+        k_clock_multi<<<(nk + 127) / 128, 128, 0, st>>>(b->clock_ptrs.p + pt.clk_lo, b->cfls.p + pt.clk_lo, nk, 1);
+        CK(cudaGetLastError());
+        for (int k = pt.slot_lo; k < pt.slot_hi; ++k)
+          if (b->slots[k] && b->slots[k]->uprev.p) solver_restore_on(b->slots[k], st);
+      }
       for (auto &kv : b->groups) {
         Group &g = *kv.second;
         const int c0 = g.part_ct[q], nc = g.part_ct[q + 1] - c0;
