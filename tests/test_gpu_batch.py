@@ -297,3 +297,42 @@ def test_batch_step_host_parts_groups_rejection_tracers(zlib):
         if q is not None:
             assert np.array_equal(s2[j].get_avars(), s1[j].get_avars())
     assert s1[1].step_rejections() > 0 and s1[5].step_rejections() > 0
+
+
+def test_batch_step_host_several_steps_and_membership_changes(zlib):
+    """Round trips of several steps (a chunk graph and a tail graph per part),
+    with a slot removed and another added between them: every remaining slot
+    ends where a batch that keeps its states on the device ends."""
+    sizes = (10, 14, 18, 22, 12)
+    probs = [polytrope_2d(n_rings=r, amplitude=1e-2, seed=r, precision=z.MIXED) for r in sizes]
+
+    def make(k):
+        raw, mesh, scheme, u0 = probs[k]
+        s = z.Solver(mesh, scheme)
+        s.set_state(u0)
+        return s
+
+    b1, b2 = z.Batch(8), z.Batch(8)
+    s1 = {k: make(k) for k in range(4)}
+    s2 = {k: make(k) for k in range(4)}
+    k1 = {k: b1.add(s, n_steps=1000) for k, s in s1.items()}
+    k2 = {k: b2.add(s, n_steps=1000) for k, s in s2.items()}
+    hosts = {k2[k]: probs[k][3].copy() for k in range(4)}
+    b1.advance(11)
+    assert b2.step_host(hosts, hosts, 11) == 4
+    # slot 1 leaves, instance 4 joins both batches
+    b1.remove(k1[1])
+    b2.remove(k2[1])
+    del hosts[k2[1]]
+    s1[4], s2[4] = make(4), make(4)
+    k1[4] = b1.add(s1[4], n_steps=1000)
+    k2[4] = b2.add(s2[4], n_steps=1000)
+    hosts[k2[4]] = probs[4][3].copy()
+    b1.advance(5)
+    assert b2.step_host(hosts, hosts, 5) == 4
+    for k in (0, 2, 3, 4):
+        b1.remove(k1[k])
+        u1, t1 = s1[k].get_state()
+        st2 = b2.status(k2[k])
+        assert st2["steps"] == (16 if k != 4 else 5), (k, st2)
+        assert np.array_equal(hosts[k2[k]], u1), (k, np.abs(hosts[k2[k]] - u1).max())
