@@ -26,7 +26,8 @@ value    whole-job cell-stage updates/s of the headline workload, state
          ranks); inputs larger than L2.
 e2e      the same metric through the public API with host buffers: every step
          copies the states from pinned host memory to the device, advances one
-         CFL step and reads the new states back.
+         CFL step and reads the new states back (C4: Batch.step_host, one host
+         round trip for all 256 instances; single meshes: zfvm_step_host).
 roofline the dominant kernel (the reconstruction): algorithmic bytes per launch
          / its event-timed launch duration, against the measured HBM copy
          bandwidth; the FP64 form also against its FP64 pipe.
