@@ -416,8 +416,29 @@ int build_solver(zfvm_solver *s) {
   // ---- per-cell arrays
   std::vector<uint8_t> h_flags(ld, 0), h_bloc((size_t)NB * RB * ld, 0);
   std::vector<int> h_l2g((size_t)MAXL * ld, 0), h_cface((size_t)nf * ld, -1), h_src(ld, 0);
-  std::vector<double> h_pinv((size_t)NP * ld, 0.0), h_center((size_t)nd * ld, 0.0), h_il(ld, 0.0),
-      h_mom((size_t)NC * ld, 0.0), h_iv(ld, 0.0), h_reff(ld, 1e300);
+  // the pseudo-inverses in FP64 (the FP64 form, and the advected variables of
+  // either form) and in FP32 (the mixed form), written straight into the
+  // precision each needs
+  const bool want64 = !s->mixed || s->na > 0, want32 = s->mixed;
+  std::vector<double> h_pinv;
+  std::vector<float> h_pinv32;
+  if (want64) h_pinv.resize((size_t)NP * ld, 0.0);
+  if (want32) h_pinv32.resize((size_t)NP * ld, 0.f);
+  auto put_pinv = [&](size_t at, double v) {
+    if (want64) h_pinv[at] = v;
+    if (want32) h_pinv32[at] = (float)v;
+  };
+  std::vector<double> h_center((size_t)nd * ld, 0.0), h_il(ld, 0.0), h_mom((size_t)NC * ld, 0.0), h_iv(ld, 0.0),
+      h_reff(ld, 1e300);
+  // cells in parallel (each writes its own column of every table); the first
+  // inconsistency found is reported after the loop
+  std::string setup_err;
+  bool setup_bad = false;
+  auto bad = [&](const char *msg) {
+#pragma omp critical(zfvm_setup_error)
+    if (!setup_bad) setup_bad = true, setup_err = msg;
+  };
+#pragma omp parallel for schedule(static)
   for (index_t i = 0; i < n; ++i) {
     h_flags[i] = g.flags[i] | (((g.flags[i] & kGhost) && g.source[i] == i) ? kFrozen : 0);
     h_src[i] = (int)g.source[i];
@@ -430,12 +451,17 @@ int build_solver(zfvm_solver *s) {
       int side = g.left[e] == i ? 0 : 1;
       h_cface[f * ld + i] = (int)(2 * e + side);
     }
-    h_reff[g.source[i]] = std::min(h_reff[g.source[i]], g.inradii[i]);
     const bool active = (g.flags[i] & kInterior) || (g.flags[i] & kGhostL1);
     if (!active) continue;
-    if (fam.k_high[i] != 0) return fail(ZFVM_EINVAL, "cell whose highest-order stencil is not the central one");
+    if (fam.k_high[i] != 0) {
+      bad("cell whose highest-order stencil is not the central one");
+      continue;
+    }
     const int nl = fam.n_l2g[i];
-    if (nl > MAXL) return fail(ZFVM_EINVAL, "combined stencil larger than the kernel's capacity");
+    if (nl > MAXL) {
+      bad("combined stencil larger than the kernel's capacity");
+      continue;
+    }
     for (int l = 0; l < MAXL; ++l) {
       index_t gl = l < nl ? fam.l2g[i * kMaxL2G + l] : i;
       h_l2g[(size_t)l * ld + i] = (int)g.source[gl];
@@ -445,31 +471,45 @@ int build_solver(zfvm_solver *s) {
       const int k = 0;
       const size_t id = i * kMaxStencils + k;
       const int sz = fam.size[id];
-      for (int r = 0; r < sz; ++r)
-        if (fam.local[id * kMaxStencilSize + r] != r) return fail(ZFVM_EINVAL, "unexpected central stencil layout");
+      bool layout_ok = true;
+      for (int r = 0; r < sz; ++r) layout_ok = layout_ok && fam.local[id * kMaxStencilSize + r] == r;
       const int rows = m->pinv_rows[id], cols = m->pinv_cols[id];
-      if (rows > R0 || cols > C0) return fail(ZFVM_EINVAL, "central stencil larger than the kernel shape");
+      if (!layout_ok) {
+        bad("unexpected central stencil layout");
+        continue;
+      }
+      if (rows > R0 || cols > C0) {
+        bad("central stencil larger than the kernel shape");
+        continue;
+      }
       for (int c = 0; c < cols; ++c)
-        for (int r = 0; r < rows; ++r) h_pinv[((size_t)c * R0 + r) * ld + i] = m->pinv[id][(size_t)c * rows + r];
+        for (int r = 0; r < rows; ++r) put_pinv(((size_t)c * R0 + r) * ld + i, m->pinv[id][(size_t)c * rows + r]);
     }
     for (int k = 1; k < ns; ++k) {
       const size_t id = i * kMaxStencils + k;
       const int rows = m->pinv_rows[id], cols = m->pinv_cols[id];
-      if (rows > RB || cols > CB) return fail(ZFVM_EINVAL, "one-sided stencil larger than the kernel shape");
+      if (rows > RB || cols > CB) {
+        bad("one-sided stencil larger than the kernel shape");
+        break;
+      }
       for (int r = 0; r < RB; ++r)
         h_bloc[((size_t)(k - 1) * RB + r) * ld + i] =
             r < rows ? (uint8_t)fam.local[id * kMaxStencilSize + r + 1] : 0;
       for (int c = 0; c < cols; ++c)
         for (int r = 0; r < rows; ++r)
-          h_pinv[((size_t)R0 * C0 + ((k - 1) * CB + c) * RB + r) * ld + i] = m->pinv[id][(size_t)c * rows + r];
+          put_pinv(((size_t)R0 * C0 + ((k - 1) * CB + c) * RB + r) * ld + i, m->pinv[id][(size_t)c * rows + r]);
     }
   }
+  if (setup_bad) return fail(ZFVM_EINVAL, setup_err);
+  // a periodic image's in-radius bounds its source's CFL length
+  for (index_t i = 0; i < n; ++i) h_reff[g.source[i]] = std::min(h_reff[g.source[i]], g.inradii[i]);
   // ---- faces
   const int nqf = s->nqf;
   std::vector<int> h_fL(lde, 0), h_fR(lde, -1);
   std::vector<uint8_t> h_fkL(lde, 0), h_fkR(lde, 0), h_fact(lde, 0);
   std::vector<double> h_fqx((size_t)nqf * nd * lde, 0.0), h_fqw((size_t)nqf * lde, 0.0),
       h_frame((size_t)nd * nd * lde, 0.0), h_farea(lde, 0.0);
+#pragma omp parallel for schedule(static)
   for (index_t e = 0; e < g.n_edges; ++e) {
     index_t L = g.left[e], R = g.right[e];
     h_fL[e] = (int)L;
@@ -505,14 +545,14 @@ int build_solver(zfvm_solver *s) {
   }
   if (s->has_src) {
     const RadialPotential &pot = s->pot;
+    bool uncovered = false;
+#pragma omp parallel for schedule(static) reduction(|| : uncovered)
     for (index_t i = 0; i < n; ++i)
-      for (int q = 0; q < nqc; ++q)
-        if (!pot.covers(norm(g.cell_qx[i * nqc + q])))
-          return fail(ZFVM_EINVAL, "the tabulated potential ends before the mesh does");
+      for (int q = 0; q < nqc; ++q) uncovered = uncovered || !pot.covers(norm(g.cell_qx[i * nqc + q]));
+#pragma omp parallel for schedule(static) reduction(|| : uncovered)
     for (index_t e = 0; e < g.n_edges; ++e)
-      for (int q = 0; q < g.n_face_qp; ++q)
-        if (!pot.covers(norm(g.face_qx[e * g.n_face_qp + q])))
-          return fail(ZFVM_EINVAL, "the tabulated potential ends before the mesh does");
+      for (int q = 0; q < g.n_face_qp; ++q) uncovered = uncovered || !pot.covers(norm(g.face_qx[e * g.n_face_qp + q]));
+    if (uncovered) return fail(ZFVM_EINVAL, "the tabulated potential ends before the mesh does");
     auto phi = [&](const Vec3 &x) { return pot.phi(x); };
     auto gphi = [&](const Vec3 &x, int dir) { return pot.dphi_dx(x, dir); };
     h_phi_cq.assign((size_t)nqc * ld, 0.0);
@@ -522,6 +562,7 @@ int build_solver(zfvm_solver *s) {
     h_cqx.assign((size_t)nqc * nd * ld, 0.0);
     h_cqw.assign((size_t)nqc * ld, 0.0);
     h_phi_fq.assign((size_t)nqf * lde, 0.0);
+#pragma omp parallel for schedule(static)
     for (index_t i = 0; i < n; ++i)
       for (int q = 0; q < nqc; ++q) {
         const Vec3 &x = g.cell_qx[i * nqc + q];
@@ -533,6 +574,7 @@ int build_solver(zfvm_solver *s) {
         }
       }
     // <phi> and <(phi - <phi>)^2> with the reference-cell weights
+#pragma omp parallel for schedule(static)
     for (index_t i = 0; i < n; ++i) {
       double m1 = P.what_c[0] * h_phi_cq[i];
       for (int q = 1; q < nqc; ++q) m1 += P.what_c[q] * h_phi_cq[(size_t)q * ld + i];
@@ -544,6 +586,7 @@ int build_solver(zfvm_solver *s) {
       h_phi_m1[i] = m1;
       h_phi_var[i] = var;
     }
+#pragma omp parallel for schedule(static)
     for (index_t e = 0; e < g.n_edges; ++e)
       for (int q = 0; q < nqf; ++q) h_phi_fq[(size_t)q * lde + e] = phi(g.face_qx[e * nqf + q]);
   }
@@ -558,8 +601,7 @@ int build_solver(zfvm_solver *s) {
   s->cface.upload(h_cface);
   s->src_map.upload(h_src);
   s->src_host.assign(h_src.begin(), h_src.begin() + n);
-  // FP64 pseudo-inverses: the FP64 form, and the advected variables of either form
-  if (!s->mixed || s->na) s->pinv.upload(h_pinv);
+  if (want64) s->pinv.upload(h_pinv);
   s->center.upload(h_center);
   s->inv_len.upload(h_il);
   s->mom.upload(h_mom);
@@ -607,13 +649,13 @@ int build_solver(zfvm_solver *s) {
   s->ux.alloc((size_t)nv * ld);
   if (!s->mixed) s->kbuf.alloc((size_t)std::max(1, sc.rk_stages - 1) * nv * ld);
   if (s->mixed) {
-    std::vector<float> h32(h_pinv.begin(), h_pinv.end());
-    s->pinv32.upload(h32);
+    s->pinv32.upload(h_pinv32);
     // FP32 copies: face frames, moments, scaled offsets of the quadrature points
     s->frame32.upload(std::vector<float>(h_frame.begin(), h_frame.end()));
     s->mom32.upload(std::vector<float>(h_mom.begin(), h_mom.end()));
     s->fqw32.upload(std::vector<float>(h_fqw.begin(), h_fqw.end()));
     std::vector<float> hxf((size_t)nf * nqf * nd * ld, 0.f), hxc((size_t)nqc * nd * ld, 0.f);
+#pragma omp parallel for schedule(static)
     for (index_t i = 0; i < n; ++i) {
       const double il = 1.0 / g.char_length[i];
       for (int f = 0; f < nf; ++f) {
@@ -637,6 +679,7 @@ int build_solver(zfvm_solver *s) {
     if (s->has_src) {
       std::vector<double> hg((size_t)nd * ld, 0.0);
       std::vector<float> hwg((size_t)nqc * nd * ld, 0.f);
+#pragma omp parallel for schedule(static)
       for (index_t i = 0; i < n; ++i)
         for (int k = 0; k < nd; ++k) {
           double acc = 0.0;
