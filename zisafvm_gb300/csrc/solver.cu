@@ -381,6 +381,7 @@ int build_solver(zfvm_solver *s) {
   P.n_stages = sc.rk_stages;
   P.gamma2 = sc.gamma == 2.0 ? 1 : 0;
   P.inv_gm1 = 1.0 / (sc.gamma - 1.0);
+  P.gm1 = sc.gamma - 1.0;
   if (sc.reconstruction != ZFVM_RC_CWENO_AO && sc.reconstruction != ZFVM_RC_WENO_AO)
     return fail(ZFVM_EINVAL, "unknown reconstruction mode");
   if (sc.step_rejection_drho < 0.0) return fail(ZFVM_EINVAL, "negative step_rejection_drho");

@@ -161,6 +161,7 @@ struct Params {
   int n_stages;
   int gamma2;        // gamma == 2: closed-form equilibrium cell averages (and, mixed, fit)
   double inv_gm1;    // 1 / (gamma - 1), computed once on the host
+  double gm1;        // gamma - 1, computed once on the host
   int weno_ao;       // reconstruction: 0 CWENO-AO, 1 WENO-AO
   double a[4][4], b[4];
   // FP32 copies for the mixed form, rounded once on the host
@@ -1198,7 +1199,7 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
   if (!d.factive[e]) return;
   const int lde = d.lde, ld = d.ld;
   const int L = d.fL[e], R = d.fR[e];
-  EqEval ev{P.gamma, P.gamma - 1.0, P.inv_gm1};
+  EqEval ev{P.gamma, P.gm1, P.inv_gm1};
   double nf[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) nf[v] = 0.0;

@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(128) k_tracer_face(const DevData d, const Para
     return;
   }
   const int kL = d.fkL[e], kR = d.fkR[e];
-  EqEval ev{P.gamma, P.gamma - 1.0, P.inv_gm1};
+  EqEval ev{P.gamma, P.gm1, P.inv_gm1};
   // the wave fan at every face point, from the stage's Euler face states
   HllcWaves<double> w[NQF];
   double wq[NQF];
