@@ -1088,10 +1088,11 @@ __global__ void __launch_bounds__(128) k_reconstruct(const DevData d, const Para
 // register count that fits kMixedReconBlocks blocks of 128 threads per SM
 // (2D: 96 registers, five blocks -- the well-balanced one also holds 5 x 38.9 KB
 // of stencil rows in shared memory; 3D order 2: 128, four; 3D order 3: 168,
-// three; the 3D well-balanced builds keep their own allocation, which a bound
-// would only turn into spills).
+// three; the 3D well-balanced builds 168, three, where some 200 bytes of
+// spills cost less than the third block gains: 384,000 tetrahedra 0.539 ->
+// 0.442 ms per launch against their unbounded 222 registers and two blocks).
 template <class S, int EQ>
-constexpr int kMixedReconBlocks = S::ND == 2 ? 5 : (EQ ? 1 : (S::C0 <= 3 ? 4 : 3));
+constexpr int kMixedReconBlocks = S::ND == 2 ? 5 : (EQ ? 3 : (S::C0 <= 3 ? 4 : 3));
 
 template <class S, int EQ, int SRC, bool MIXED>
 __global__ void __launch_bounds__(128, kMixedReconBlocks<S, EQ>) k_reconstruct_mixed(const DevData d, const Params P,
