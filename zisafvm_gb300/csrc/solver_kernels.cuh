@@ -1421,11 +1421,16 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
 }
 
 // Blocks of 128 threads per SM the face kernel is held to: the mixed
-// well-balanced fluxes are latency-bound and gain from more resident warps
-// (2D: 96 registers, five blocks; 3D: 126 registers, four blocks, no spills);
-// the other forms keep the compiler's choice.
+// well-balanced fluxes are latency-bound on their gathers and gain from more
+// resident warps even with the spills a tight bound brings (2D: 48 registers,
+// ten blocks, 0.40-0.74 KB of spills per thread; 3D: 64 registers, eight
+// blocks).  Measured per launch: batched C4 ensemble of 48 disks 0.204 ms at
+// the compiler's 118 registers and four blocks, 0.180 at 96 and five, 0.120
+// now; 384,000 tetrahedra 0.138 ms at 126 registers and four blocks, 0.098
+// now.
+// The other forms keep the compiler's choice.
 template <class S, int EQ, bool MIXED>
-constexpr int kFaceBlocks = (MIXED && EQ) ? (S::ND == 2 ? 5 : 4) : 1;
+constexpr int kFaceBlocks = (MIXED && EQ) ? (S::ND == 2 ? 10 : 8) : 1;
 
 template <class S, int FLUX, int EQ, bool MIXED>
 __global__ void __launch_bounds__(128, (kFaceBlocks<S, EQ, MIXED>)) k_face_flux(const DevData d, const Params P, StageArgs a) {
@@ -1716,8 +1721,7 @@ constexpr auto batch_recon_kernel() {
 }
 
 // The batched face kernel takes the single-solver kernel's register budget per
-// thread (some 200 bytes of spills in the mixed well-balanced build, which cost
-// less than the fifth block per SM gains: C4 face 0.204 -> 0.180 ms per launch).
+// thread (kFaceBlocks 128-thread blocks per SM, scaled to the block size).
 template <class S, int EQ, bool MIXED, int BS>
 constexpr int kBatchFaceBlocks = (kFaceBlocks<S, EQ, MIXED> * 128 + BS - 1) / BS;
 
