@@ -1427,10 +1427,11 @@ __device__ __forceinline__ void face_one(const DevData &d, const Params &P, cons
 // blocks).  Measured per launch: batched C4 ensemble of 48 disks 0.204 ms at
 // the compiler's 118 registers and four blocks, 0.180 at 96 and five, 0.120
 // now; 384,000 tetrahedra 0.138 ms at 126 registers and four blocks, 0.098
-// now.
-// The other forms keep the compiler's choice.
+// now.  The mixed form without well-balancing takes the same bounds (C3 vortex
+// tube, 2,058,000 tetrahedra: 0.272 -> 0.250 ms); the FP64 form, bound by its
+// FP64 pipe, keeps the compiler's choice.
 template <class S, int EQ, bool MIXED>
-constexpr int kFaceBlocks = (MIXED && EQ) ? (S::ND == 2 ? 10 : 8) : 1;
+constexpr int kFaceBlocks = MIXED ? (S::ND == 2 ? 10 : 8) : 1;
 
 template <class S, int FLUX, int EQ, bool MIXED>
 __global__ void __launch_bounds__(128, (kFaceBlocks<S, EQ, MIXED>)) k_face_flux(const DevData d, const Params P, StageArgs a) {
