@@ -1,4 +1,4 @@
-"""The reference's grid tests, restated for this build's host set-up through the
+"""The reference's grid tests, restated for the package's host set-up through the
 mesh exports (zfvm_mesh_get_connectivity, zfvm_mesh_get_faces,
 zfvm_mesh_get_geometry), on generated meshes (the reference's grid files are
 missing):

@@ -12,7 +12,7 @@ oracle at 1e-12 only with identical quadrature):
   only where the error is above round-off (math/quadrature.cpp:17-74 for
   triangles, math/tetrahedral_rule.cpp:19-58 for tetrahedra).
 
-The meshes are this build's generated unit square and unit cube (jittered);
+The meshes are the package's generated unit square and unit cube (jittered);
 the reference's grid files are missing.
 """
 import numpy as np

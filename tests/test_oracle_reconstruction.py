@@ -137,7 +137,7 @@ def test_constant_data_are_reproduced(zlib, olib):
 
 
 def test_well_balanced_reconstruction_of_small_perturbations(zlib, olib):
-    """well_balanced_reconstruction.cpp:16-95 with this build's polytrope: gamma = 2,
+    """well_balanced_reconstruction.cpp:16-95 with the package's polytrope: gamma = 2,
     K = 1, phi = r^2 / 2 (rho_eq = 1 - r^2 / 4, p = rho^2, E = p), cell averages
     with the volume rule of degree 2, E perturbed by -1e-8, 0 or +1e-8 per cell,
     CWENO-AO {2, 2, 2, 2} / {2.0, 1.5, 1.5, 1.5}, weights {100, 1, 1, 1},

@@ -1,4 +1,4 @@
-"""The reference's stencil tests, restated for this build's host set-up on
+"""The reference's stencil tests, restated for the package's host set-up on
 generated meshes (the reference's grid files are missing):
 
 - deduce_max_order (test/zisa/unit_test/reconstruction/stencil.cpp:126-145):

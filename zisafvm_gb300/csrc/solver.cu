@@ -361,7 +361,7 @@ int build_solver(zfvm_solver *s) {
   s->mixed = sc.precision == ZFVM_MIXED;
   s->has_src = sc.gravity != ZFVM_GRAVITY_NONE;
   if (s->has_eq && !s->has_src) return fail(ZFVM_EINVAL, "isentropic well-balancing needs gravity");
-  if (sc.heating_rate != 0.0 && !s->has_src) return fail(ZFVM_EINVAL, "heating needs a gravity source in this build");
+  if (sc.heating_rate != 0.0 && !s->has_src) return fail(ZFVM_EINVAL, "heating needs a gravity source here");
   if (sc.gravity < ZFVM_GRAVITY_NONE || sc.gravity > ZFVM_GRAVITY_RADIAL_TABLE)
     return fail(ZFVM_EINVAL, "unknown gravity kind");
   if (sc.flux_bc == ZFVM_FLUX_BC_ISENTROPIC && !s->has_eq)
